@@ -1,0 +1,207 @@
+"""ctypes front end of the CPU oracle (oracle/farm_oracle.c).
+
+TEST INFRASTRUCTURE ONLY. Only tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline leg import this module, and only as the checker or the timed CPU
+baseline; the engine never routes through it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+_lib = None
+
+
+class FoLayer(C.Structure):
+    _fields_ = [("mbr", C.c_double * 4), ("dimx", C.c_int32), ("dimy", C.c_int32), ("step_x", C.c_double),
+                ("step_y", C.c_double), ("offset", C.c_uint32)]
+
+
+class FoRaster(C.Structure):
+    _fields_ = [("mbr", C.c_double * 4), ("dimx", C.c_int32), ("dimy", C.c_int32), ("step_x", C.c_double),
+                ("step_y", C.c_double), ("nv", C.c_uint32), ("status_size", C.c_uint32),
+                ("status", C.POINTER(C.c_uint8)), ("P", C.c_uint32), ("offset", C.POINTER(C.c_uint32)),
+                ("n_seq", C.c_uint32), ("seq", C.POINTER(C.c_uint32)), ("n_hlines", C.c_uint32),
+                ("n_hnodes", C.c_uint32), ("hoff", C.POINTER(C.c_uint32)), ("hnodes", C.POINTER(C.c_double)),
+                ("n_vlines", C.c_uint32), ("n_vnodes", C.c_uint32), ("voff", C.POINTER(C.c_uint32)),
+                ("vnodes", C.POINTER(C.c_double)), ("areas", C.POINTER(C.c_double)), ("num_layers", C.c_uint32),
+                ("layers", C.POINTER(FoLayer))]
+
+
+class FoOpts(C.Structure):
+    _fields_ = [("vpr", C.c_int), ("hierarchy", C.c_int), ("category_count", C.c_int), ("merge_carry", C.c_int)]
+
+
+class FoCounters(C.Structure):
+    _fields_ = [("window_pixels", C.c_uint64), ("pixel_pairs", C.c_uint64), ("segment_tests", C.c_uint64),
+                ("seq_pairs", C.c_uint64)]
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        path = HERE / "liboracle.so"
+        if not path.exists():
+            from farm_gb300 import build
+            build.build_oracle()
+        L = C.CDLL(str(path))
+        fp = C.POINTER(C.c_float)
+        L.fo_rasterize.argtypes = [fp, C.c_uint32, C.POINTER(FoOpts), C.POINTER(FoRaster)]
+        L.fo_raster_free.argtypes = [C.POINTER(FoRaster)]
+        L.fo_raster_free.restype = None
+        L.fo_intersect.argtypes = [C.POINTER(FoRaster), fp, C.POINTER(FoRaster), fp, C.POINTER(FoCounters)]
+        L.fo_within.argtypes = [C.POINTER(FoRaster), fp, C.POINTER(FoRaster), fp, C.c_double, C.c_int,
+                                C.POINTER(FoCounters)]
+        L.fo_segment_intersect.argtypes = [fp, fp, fp, fp]
+        L.fo_point_to_segment_distance.argtypes = [fp, fp, fp, C.c_int]
+        L.fo_point_to_segment_distance.restype = C.c_double
+        L.fo_segment_contain.argtypes = [C.POINTER(FoRaster), fp, C.c_float, C.c_float]
+        L.fo_intersection_area.argtypes = [fp, C.c_uint32, fp, C.c_uint32]
+        L.fo_intersection_area.restype = C.c_double
+        L.fo_degree_per_km_longitude.argtypes = [C.c_double]
+        L.fo_degree_per_km_longitude.restype = C.c_double
+        _lib = L
+    return _lib
+
+
+def mem_ring(stored: np.ndarray) -> np.ndarray:
+    """The ring the reference decodes from a stored record: stored vertices, one
+    more copy of the first (vertex_sequence.cpp:206-219), and the pad vertex the
+    single-pixel sequence reads (a copy of the first)."""
+    s = np.ascontiguousarray(stored, dtype=np.float32)
+    return np.ascontiguousarray(np.concatenate([s, s[:1], s[:1]]), dtype=np.float32)
+
+
+class Raster:
+    """One rasterized polygon (owns the C allocation)."""
+
+    def __init__(self, stored: np.ndarray, vpr: int, hierarchy: bool = False, category_count: int = 16,
+                 merge_carry: int = 1):
+        self.ring = mem_ring(stored)
+        self.nv = len(stored) + 1
+        self.r = FoRaster()
+        o = FoOpts(vpr, int(hierarchy), category_count, merge_carry)
+        rc = lib().fo_rasterize(self.ring.ctypes.data_as(C.POINTER(C.c_float)), self.nv, C.byref(o), C.byref(self.r))
+        self.rc = rc
+        if rc != 0:
+            raise RuntimeError(f"oracle rasterize failed: {rc}")
+
+    def __del__(self):
+        try:
+            lib().fo_raster_free(C.byref(self.r))
+        except Exception:
+            pass
+
+    def arrays(self) -> dict:
+        r = self.r
+
+        def arr(p, n, dt):
+            if n == 0:
+                return np.zeros(0, dtype=dt)
+            return np.ctypeslib.as_array(p, shape=(n,)).astype(dt, copy=True)
+
+        out = {
+            "mbr": np.array(r.mbr[:], dtype=np.float64), "dimx": r.dimx, "dimy": r.dimy,
+            "step": np.array([r.step_x, r.step_y]), "status": arr(r.status, r.status_size, np.uint8),
+            "offset": arr(r.offset, r.P + 1, np.uint32), "seq": arr(r.seq, 2 * r.n_seq, np.uint32).reshape(-1, 2),
+            "hoff": arr(r.hoff, r.n_hlines, np.uint32), "hnodes": arr(r.hnodes, r.n_hnodes, np.float64),
+            "voff": arr(r.voff, r.n_vlines, np.uint32), "vnodes": arr(r.vnodes, r.n_vnodes, np.float64),
+            "areas": arr(r.areas, r.P, np.float64), "num_layers": r.num_layers,
+        }
+        layers = []
+        for i in range(r.num_layers):
+            L = r.layers[i]
+            layers.append((tuple(L.mbr[:]), L.dimx, L.dimy, L.step_x, L.step_y, L.offset))
+        out["layers"] = layers
+        return out
+
+
+def rasterize_set(ps, vpr: int, hierarchy: bool = False, category_count: int = 16, merge_carry: int = 1):
+    return [Raster(ps.ring(k), vpr, hierarchy, category_count, merge_carry) for k in range(ps.n)]
+
+
+def intersect(rs: Raster, rt: Raster, counters: bool = False):
+    c = FoCounters()
+    fp = C.POINTER(C.c_float)
+    v = lib().fo_intersect(C.byref(rs.r), rs.ring.ctypes.data_as(fp), C.byref(rt.r), rt.ring.ctypes.data_as(fp),
+                           C.byref(c))
+    if v < 0:
+        raise RuntimeError(f"oracle intersect failed: {v}")
+    return (bool(v), c) if counters else bool(v)
+
+
+def within(rs: Raster, rt: Raster, distance: float = 10.0, geography: bool = True, counters: bool = False):
+    c = FoCounters()
+    fp = C.POINTER(C.c_float)
+    v = lib().fo_within(C.byref(rs.r), rs.ring.ctypes.data_as(fp), C.byref(rt.r), rt.ring.ctypes.data_as(fp),
+                        float(distance), int(geography), C.byref(c))
+    if v < 0:
+        raise RuntimeError(f"oracle within failed: {v}")
+    return (bool(v), c) if counters else bool(v)
+
+
+def intersection_area(a: np.ndarray, b: np.ndarray) -> float:
+    fp = C.POINTER(C.c_float)
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    b = np.ascontiguousarray(b, dtype=np.float32)
+    return lib().fo_intersection_area(a.ctypes.data_as(fp), len(a), b.ctypes.data_as(fp), len(b))
+
+
+def read_ref_rasters(path: str) -> list[dict]:
+    """Parse a raster dump written by oracle/ref/harness.cpp."""
+    buf = open(path, "rb").read()
+    pos = 0
+
+    def take(dt, n):
+        nonlocal pos
+        a = np.frombuffer(buf, dtype=dt, count=n, offset=pos)
+        pos += a.nbytes
+        return a.copy()
+
+    magic, n = take(np.uint32, 2)
+    assert magic == 0x46415231
+    out = []
+    for _ in range(int(n)):
+        mbr = take(np.float64, 4)
+        dimx, dimy = take(np.int32, 2)
+        step = take(np.float64, 2)
+        nv = int(take(np.uint32, 1)[0])
+        ss = int(take(np.uint32, 1)[0])
+        status = take(np.uint8, ss)
+        P = int(take(np.uint32, 1)[0])
+        offset = take(np.uint32, P + 1)
+        les = int(take(np.uint32, 1)[0])
+        seq = take(np.uint32, 2 * les).reshape(-1, 2)
+        nl = int(take(np.uint32, 1)[0])
+        hoff = take(np.uint32, nl)
+        nc = int(take(np.uint32, 1)[0])
+        hnodes = take(np.float64, nc)
+        nl = int(take(np.uint32, 1)[0])
+        voff = take(np.uint32, nl)
+        nc = int(take(np.uint32, 1)[0])
+        vnodes = take(np.float64, nc)
+        areas = take(np.float64, P)
+        L = int(take(np.uint32, 1)[0])
+        layers = []
+        for _ in range(L):
+            lm = take(np.float64, 4)
+            ldx, ldy = take(np.int32, 2)
+            lst = take(np.float64, 2)
+            lo = int(take(np.uint32, 1)[0])
+            layers.append((tuple(lm), int(ldx), int(ldy), float(lst[0]), float(lst[1]), lo))
+        out.append({"mbr": mbr, "dimx": int(dimx), "dimy": int(dimy), "step": step, "nv": nv, "status": status,
+                    "offset": offset, "seq": seq, "hoff": hoff, "hnodes": hnodes, "voff": voff, "vnodes": vnodes,
+                    "areas": areas, "num_layers": L, "layers": layers})
+    return out
+
+
+def read_ref_pairs(path: str) -> np.ndarray:
+    """Parse a pair-decision file written by oracle/ref/harness.cpp: [k, 3] (s, t, result)."""
+    buf = open(path, "rb").read()
+    n = int(np.frombuffer(buf, dtype=np.uint64, count=1)[0])
+    rec = np.dtype([("s", "<u4"), ("t", "<u4"), ("r", "u1")])
+    a = np.frombuffer(buf, dtype=rec, count=n, offset=8)
+    return np.stack([a["s"].astype(np.int64), a["t"].astype(np.int64), a["r"].astype(np.int64)], axis=1)
