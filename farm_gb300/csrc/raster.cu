@@ -1,0 +1,1523 @@
+// Stage (a): rasterization of every loaded polygon on the GPU, reproducing the
+// reference's CPU raster exactly (status bytes, per-pixel edge-sequence CSR,
+// sorted grid-line crossing nodes, FP64 fill areas, hierarchy layers).
+//
+// Reference: preprocessing.cpp:4-29, MyRaster.cpp:8-33 (dims), :444-491
+// (grid_align), Ideal.cpp:90-183 (process_crosses), :185-238
+// (process_intersection), :252-538 (evaluate_edges), :540-573 (scanline),
+// :575-918 (fill), :1008-1099 (layering / merge).
+//
+// The reference walks each polygon sequentially and accumulates per-pixel
+// lists in std::map. Here the same lists come out of a flattened pipeline over
+// all polygons at once: per-edge count -> scan -> fill, then stable radix
+// sorts by pixel / line / column / cell, which reproduce the map iteration
+// order (key order, then insertion order) exactly. The fill clip (strip, then
+// cell) is scattered per edge into the columns and cells it touches, so its
+// cost is linear in the output, not columns x vertices.
+#include <cub/cub.cuh>
+
+#include <cmath>
+#include <cstring>
+
+#include "common.cuh"
+
+namespace farm {
+
+struct RasterParams {
+    int vpr, cc, hier;
+    double gstep;           // UniversalGrid step: round_sig(360 / 2^25, 2)
+    int pow2_ceil[40];      // ceil(log(2^k) / log(2.0)) as the host's libm evaluates it
+};
+
+enum Scratch {
+    S_SIZES = 0,  // per-polygon size table [9][npoly+1]
+    S_SCAN,       // scanned size table
+    S_CNT_E,      // per-edge counts [3][nedges+1]
+    S_SCAN_E,
+    S_CFROM,      // crossings: from pixel, to pixel, edge
+    S_CTO,
+    S_CEDGE,
+    S_VKEY,       // visits
+    S_VVAL,
+    S_VKEY2,
+    S_VVAL2,
+    S_SEQW,       // seq widths / positions
+    S_PIXCNT,     // per pixel u32 counts (seqs, then cells)
+    S_PIXSCAN,
+    S_HKEY,
+    S_HVAL,
+    S_VNKEY,
+    S_VNVAL,
+    S_LINECNT,
+    S_LINESCAN,
+    S_COLX,       // sweep lines
+    S_ROWY,
+    S_TMP_A,
+    S_TMP_B,
+};
+
+// ------------------------------------------------------------ headers ----
+
+__device__ void init_raster(PolyHdr &h, int num_pixels) {
+    const double *m = h.mbr;
+    double multi = fabs((m[3] - m[1]) / (m[2] - m[0]));
+    // MyRaster.cpp:12 uses pow(x, 0.5); sqrt is the correctly rounded square root
+    h.dimx = (int)sqrt(num_pixels / multi);
+    h.dimy = (int)(h.dimx * multi);
+    if (h.dimx == 0) h.dimx = 1;
+    if (h.dimy == 0) h.dimy = 1;
+    h.step_x = (m[2] - m[0]) / h.dimx;
+    h.step_y = (m[3] - m[1]) / h.dimy;
+    if (h.step_x < 0.00001) {
+        h.step_x = 0.00001;
+        h.dimx = (int)((m[2] - m[0]) / h.step_x + 1);
+    }
+    if (h.step_y < 0.00001) {
+        h.step_y = 0.00001;
+        h.dimy = (int)((m[3] - m[1]) / h.step_y + 1);
+    }
+}
+
+__device__ bool grid_align(PolyHdr &h, double gstep) {
+    bool f1 = false, f2 = false;
+    double x = gstep, y = gstep;
+    if (h.step_x <= x) { h.step_x = x; f1 = true; }
+    if (h.step_y <= y) { h.step_y = y; f2 = true; }
+    for (int i = 25; i > 0; i--) {
+        if (!f1 && h.step_x > x && h.step_x < x * 2) {
+            f1 = true;
+            h.step_x = fabs(h.step_x - x) < fabs(h.step_x - x * 2) ? x : x * 2;
+        }
+        if (!f2 && h.step_y > y && h.step_y < y * 2) {
+            f2 = true;
+            h.step_y = fabs(h.step_y - y) < fabs(h.step_y - y * 2) ? y : y * 2;
+        }
+        if (f1 && f2) break;
+        x *= 2;
+        y *= 2;
+    }
+    if (!(f1 && f2)) return false;
+    h.step_x = h.step_x < h.step_y ? h.step_x : h.step_y;
+    h.step_y = h.step_x;
+    double *m = h.mbr;
+    m[0] = floor(m[0] / h.step_x) * h.step_x;
+    m[1] = floor(m[1] / h.step_y) * h.step_y;
+    m[2] = ceil(m[2] / h.step_x) * h.step_x;
+    m[3] = ceil(m[3] / h.step_y) * h.step_y;
+    h.dimx = (int)round((m[2] - m[0]) / h.step_x);
+    h.dimy = (int)round((m[3] - m[1]) / h.step_y);
+    return true;
+}
+
+__device__ int log2_ceil(int n, const RasterParams &rp) {
+    // ceil(log(n) / log(2.0)): exact for non powers of two (the quotient is
+    // then irrational and far from an integer); powers of two use the host
+    // library's own rounding.
+    if (n <= 1) return 0;
+    if ((n & (n - 1)) == 0) return rp.pow2_ceil[__ffs(n) - 1];
+    return 32 - __clz(n - 1);
+}
+
+__device__ void layering(PolyHdr &h, const RasterParams &rp) {
+    int a = log2_ceil(h.dimx, rp), b = log2_ceil(h.dimy, rp);
+    int high = a > b ? a : b;
+    int low = high;
+    double dx = h.dimx, dy = h.dimy;
+    for (int i = high - 1; i >= 0; i--) {
+        if (dx * dy <= 1) break;
+        dx = (int)ceil(dx / 2.0);
+        dy = (int)ceil(dy / 2.0);
+        low--;
+    }
+    h.num_layers = (uint32_t)(high - low + 1);
+}
+
+// One warp per polygon: MBR (vertex_sequence.cpp:152-168), raster geometry.
+__global__ void k_header(const float2 *__restrict__ ring, const uint64_t *__restrict__ off, uint32_t npoly,
+                         RasterParams rp, PolyHdr *__restrict__ hdr, uint64_t *__restrict__ sizes) {
+    uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t p = warp; p < npoly; p += nwarps) {
+        uint64_t b = off[p], e = off[p + 1];
+        const float2 *r = ring + b + 2ull * p;
+        uint32_t m = (uint32_t)(e - b);
+        double lx = 100000.0, ly = 100000.0, hx = -100000.0, hy = -100000.0;
+        for (uint32_t j = lane; j < m; j += 32) {
+            float2 q = r[j];
+            lx = fmin(lx, (double)q.x);
+            hx = fmax(hx, (double)q.x);
+            ly = fmin(ly, (double)q.y);
+            hy = fmax(hy, (double)q.y);
+        }
+        for (int o = 16; o; o >>= 1) {
+            lx = fmin(lx, __shfl_xor_sync(0xffffffffu, lx, o));
+            hx = fmax(hx, __shfl_xor_sync(0xffffffffu, hx, o));
+            ly = fmin(ly, __shfl_xor_sync(0xffffffffu, ly, o));
+            hy = fmax(hy, __shfl_xor_sync(0xffffffffu, hy, o));
+        }
+        if (lane == 0) {
+            PolyHdr h;
+            memset(&h, 0, sizeof h);
+            const double bias = (double)1e-9f;
+            h.mbr[0] = lx - bias;
+            h.mbr[1] = ly - bias;
+            h.mbr[2] = hx + bias;
+            h.mbr[3] = hy + bias;
+            h.nv = m + 1;
+            h.ring = b + 2ull * p;
+            h.edge = b;
+            init_raster(h, (int)(h.nv / (uint32_t)rp.vpr));
+            if (rp.hier) {
+                if (!grid_align(h, rp.gstep)) h.err = FARM_EASSERT;
+                layering(h, rp);
+            } else {
+                h.num_layers = 0;
+            }
+            h.P = (uint32_t)h.dimx * (uint32_t)h.dimy;
+            uint32_t ss = h.P;
+            if (rp.hier && h.num_layers > 1) {
+                LayerGeom g;
+                layer_geom(h, 0, g);
+                ss = g.offset + (uint32_t)(g.dimx * g.dimy);
+            }
+            h.status_size = ss;
+            hdr[p] = h;
+            uint64_t n1 = (uint64_t)npoly + 1;
+            sizes[0 * n1 + p] = h.P;
+            sizes[1 * n1 + p] = h.status_size;
+            sizes[2 * n1 + p] = (uint64_t)h.P + 1;
+            sizes[3 * n1 + p] = (uint64_t)h.dimy + 2;
+            sizes[4 * n1 + p] = (uint64_t)h.dimx + 2;
+            sizes[5 * n1 + p] = (uint64_t)h.dimx + 2;  // fill sweep columns
+            sizes[6 * n1 + p] = (uint64_t)h.dimy + 2;  // fill sweep rows
+            sizes[7 * n1 + p] = (uint64_t)h.dimy;      // scanline rows
+        }
+    }
+}
+
+// Bases from the scanned sizes, and the fill sweep lines (Ideal.cpp:829-851,
+// :869-875): Xi accumulates by repeated addition, exactly as the loop does.
+__global__ void k_bases(PolyHdr *__restrict__ hdr, uint32_t npoly, const uint64_t *__restrict__ scan,
+                        double *__restrict__ colx, double *__restrict__ rowy) {
+    uint64_t n1 = (uint64_t)npoly + 1;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npoly; p += gridDim.x * blockDim.x) {
+        PolyHdr h = hdr[p];
+        h.pix = scan[0 * n1 + p];
+        h.st = scan[1 * n1 + p];
+        h.off = scan[2 * n1 + p];
+        h.hline = scan[3 * n1 + p];
+        h.vline = scan[4 * n1 + p];
+        h.col = scan[5 * n1 + p];
+        h.row = scan[6 * n1 + p];
+        double Xi = h.mbr[0];
+        double Xi1 = Xi + h.step_x;
+        double kx = Xi + h.dimx * h.step_x;
+        int c = 0;
+        while (Xi1 < kx + 1e-9) {
+            if (c > h.dimx) {  // the reference's get_id asserts x < dimx
+                h.err = FARM_EASSERT;
+                break;
+            }
+            colx[h.col + c] = Xi;
+            Xi += h.step_x;
+            Xi1 = Xi + h.step_x;
+            c++;
+        }
+        if (c > h.dimx) h.err = FARM_EASSERT;
+        h.ncols = c;
+        double Yi = h.mbr[1];
+        double Yi1 = Yi + h.step_y;
+        double ky = h.mbr[1] + h.dimy * h.step_y;
+        int r = 0;
+        while (Yi1 < ky + 1e-9) {
+            if (r > h.dimy) {
+                h.err = FARM_EASSERT;
+                break;
+            }
+            rowy[h.row + r] = Yi;
+            Yi += h.step_y;
+            Yi1 = Yi + h.step_y;
+            r++;
+        }
+        if (r > h.dimy) h.err = FARM_EASSERT;
+        h.nrows = r;
+        hdr[p] = h;
+    }
+}
+
+// ---------------------------------------------------------- edge walk ----
+// Ideal.cpp:259-521 for one edge. Sink receives: border(x, y), cross(from,
+// to) (a LEAVE/ENTER pair), hnode(line, value), vnode(line, value).
+template <typename Sink>
+__device__ void walk_edge(const PolyHdr &h, float2 A, float2 B, Sink &s) {
+    const double start_x = h.mbr[0], start_y = h.mbr[1];
+    const double step_x = h.step_x, step_y = h.step_y;
+    const int dimx = h.dimx, dimy = h.dimy;
+    double x1 = A.x, y1 = A.y, x2 = B.x, y2 = B.y;
+    int cur_startx = double_to_int((x1 - start_x) / step_x);
+    int cur_endx = double_to_int((x2 - start_x) / step_x);
+    int cur_starty = double_to_int((y1 - start_y) / step_y);
+    int cur_endy = double_to_int((y2 - start_y) / step_y);
+    if (cur_startx == dimx) cur_startx--;
+    if (cur_endx == dimx) cur_endx--;
+    if (cur_starty == dimy) cur_starty--;
+    if (cur_endy == dimy) cur_endy--;
+    if (cur_startx >= dimx || cur_endx >= dimx || cur_starty >= dimy || cur_endy >= dimy) {
+        s.fail();
+        return;
+    }
+    s.border(cur_startx, cur_starty);
+    s.border(cur_endx, cur_endy);
+    if (cur_startx == cur_endx && cur_starty == cur_endy) return;
+    if (y1 == y2) {
+        if (cur_startx < cur_endx) {
+            for (int x = cur_startx; x < cur_endx; x++) {
+                s.vnode(x + 1, y1);
+                s.cross(x, cur_starty, x + 1, cur_starty);
+            }
+        } else {
+            for (int x = cur_startx; x > cur_endx; x--) {
+                s.vnode(x, y1);
+                s.cross(x, cur_starty, x - 1, cur_starty);
+            }
+        }
+        return;
+    }
+    if (x1 == x2) {
+        if (cur_starty < cur_endy) {
+            for (int y = cur_starty; y < cur_endy; y++) {
+                s.hnode(y + 1, x1);
+                s.cross(cur_startx, y, cur_startx, y + 1);
+            }
+        } else {
+            for (int y = cur_starty; y > cur_endy; y--) {
+                s.hnode(y, x1);
+                s.cross(cur_startx, y, cur_startx, y - 1);
+            }
+        }
+        return;
+    }
+    double a = (y1 - y2) / (x1 - x2);
+    double b = (x1 * y2 - x2 * y1) / (x1 - x2);
+    int x = cur_startx, y = cur_starty;
+    long guard = 4L * (labs((long)cur_endx - cur_startx) + labs((long)cur_endy - cur_starty) + 4);
+    while (x != cur_endx || y != cur_endy) {
+        if (--guard <= 0 || s.failed()) {
+            s.fail();
+            return;
+        }
+        bool passed = false;
+        double yval = 0, xval = 0;
+        if (x != cur_endx) {
+            if (cur_startx < cur_endx)
+                xval = ((double)x + 1) * step_x + start_x;
+            else
+                xval = (double)x * step_x + start_x;
+            yval = xval * a + b;
+            if (fabs((yval - start_y) / step_y - round((yval - start_y) / step_y)) < 1e-9) {
+                // Ideal.cpp:396-422: through a grid corner
+                if (cur_startx < cur_endx && cur_starty < cur_endy) {
+                    s.vnode(x + 1, yval);
+                    s.cross(x, y, x + 1, y + 1);
+                    x++;
+                    y++;
+                } else if (cur_startx < cur_endx && cur_starty > cur_endy) {
+                    s.vnode(x, yval);
+                    s.cross(x, y, x + 1, y - 1);
+                    x++;
+                    y--;
+                } else if (cur_startx > cur_endx && cur_starty < cur_endy) {
+                    s.cross(x, y, x - 1, y + 1);
+                    x--;
+                    y++;
+                } else if (cur_startx > cur_endx && cur_starty > cur_endy) {
+                    s.cross(x, y, x - 1, y - 1);
+                    x--;
+                    y--;
+                }
+                continue;
+            }
+            int cur_y = (int)((yval - start_y) / step_y);
+            int ymax = cur_endy > cur_starty ? cur_endy : cur_starty;
+            int ymin = cur_endy < cur_starty ? cur_endy : cur_starty;
+            if (cur_y > ymax) cur_y = ymax;
+            if (cur_y < ymin) cur_y = ymin;
+            if (cur_y == y) {
+                passed = true;
+                if (cur_startx < cur_endx) {
+                    s.vnode(x + 1, yval);
+                    s.cross(x, y, x + 1, y);
+                    x++;
+                } else {
+                    s.vnode(x, yval);
+                    s.cross(x, y, x - 1, y);
+                    x--;
+                }
+            }
+        }
+        if (y != cur_endy) {
+            if (cur_starty < cur_endy)
+                yval = (double)(y + 1) * step_y + start_y;
+            else
+                yval = (double)y * step_y + start_y;
+            xval = (yval - b) / a;
+            int cur_x = (int)((xval - start_x) / step_x);
+            int xmax = cur_endx > cur_startx ? cur_endx : cur_startx;
+            int xmin = cur_endx < cur_startx ? cur_endx : cur_startx;
+            if (cur_x > xmax) cur_x = xmax;
+            if (cur_x < xmin) cur_x = xmin;
+            if (cur_x == x) {
+                passed = true;
+                if (cur_starty < cur_endy) {
+                    s.hnode(y + 1, xval);
+                    s.cross(x, y, x, y + 1);
+                    y++;
+                } else {
+                    s.hnode(y, xval);
+                    s.cross(x, y, x, y - 1);
+                    y--;
+                }
+            }
+        }
+        if (!passed) {
+            s.fail();
+            return;
+        }
+    }
+}
+
+struct CountSink {
+    uint8_t *status;
+    int dimx, dimy;
+    uint32_t nc = 0, nh = 0, nv = 0;
+    bool bad = false;
+    __device__ bool inb(int x, int y) const { return x >= 0 && x < dimx && y >= 0 && y < dimy; }
+    __device__ void border(int x, int y) {
+        if (!inb(x, y)) {
+            bad = true;
+            return;
+        }
+        status[y * dimx + x] = 1;
+    }
+    __device__ void cross(int fx, int fy, int tx, int ty) {
+        if (!inb(fx, fy) || !inb(tx, ty)) {
+            bad = true;
+            return;
+        }
+        status[fy * dimx + fx] = 1;
+        status[ty * dimx + tx] = 1;
+        nc++;
+    }
+    __device__ void hnode(int line, double) {
+        if (line < 0 || line > dimy + 1) { bad = true; return; }
+        nh++;
+    }
+    __device__ void vnode(int line, double) {
+        if (line < 0 || line > dimx + 1) { bad = true; return; }
+        nv++;
+    }
+    __device__ void fail() { bad = true; }
+    __device__ bool failed() const { return bad; }
+};
+
+// Emits exactly what CountSink counted: the walk is deterministic and both
+// sinks drop the same out-of-range items.
+struct FillSink {
+    int dimx, dimy;
+    uint32_t edge;
+    uint64_t c, hn, vn;           // output cursors
+    uint32_t *from, *to, *cedge;  // crossings
+    uint64_t *hkey, *vkey;
+    double *hval, *vval;
+    uint64_t hline, vline;
+    bool bad = false;
+    __device__ bool inb(int x, int y) const { return x >= 0 && x < dimx && y >= 0 && y < dimy; }
+    __device__ void border(int x, int y) {
+        if (!inb(x, y)) bad = true;
+    }
+    __device__ void cross(int fx, int fy, int tx, int ty) {
+        if (!inb(fx, fy) || !inb(tx, ty)) {
+            bad = true;
+            return;
+        }
+        from[c] = (uint32_t)(fy * dimx + fx);
+        to[c] = (uint32_t)(ty * dimx + tx);
+        cedge[c] = edge;
+        c++;
+    }
+    __device__ void hnode(int line, double v) {
+        if (line < 0 || line > dimy + 1) { bad = true; return; }
+        hkey[hn] = hline + (uint64_t)line;
+        hval[hn] = v;
+        hn++;
+    }
+    __device__ void vnode(int line, double v) {
+        if (line < 0 || line > dimx + 1) { bad = true; return; }
+        vkey[vn] = vline + (uint64_t)line;
+        vval[vn] = v;
+        vn++;
+    }
+    __device__ void fail() { bad = true; }
+    __device__ bool failed() const { return bad; }
+};
+
+__global__ void k_walk_count(const StoreView sv, PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off,
+                             uint32_t npoly, uint64_t nedges, uint32_t *__restrict__ cnt) {
+    uint64_t n1 = nedges + 1;
+    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nedges;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t p = find_segment(off, npoly, e);
+        const PolyHdr &h = hdr[p];
+        uint32_t i = (uint32_t)(e - h.edge);
+        const float2 *r = sv.ring + h.ring;
+        CountSink s;
+        s.status = sv.status + h.st;
+        s.dimx = h.dimx;
+        s.dimy = h.dimy;
+        if (h.err == 0) walk_edge(h, r[i], r[i + 1], s);
+        if (s.bad) atomicMin(&hdr[p].err, FARM_EASSERT);
+        cnt[e] = s.nc;
+        cnt[n1 + e] = s.nh;
+        cnt[2 * n1 + e] = s.nv;
+    }
+}
+
+__global__ void k_walk_fill(const StoreView sv, const PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off,
+                            uint32_t npoly, uint64_t nedges, const uint64_t *__restrict__ scan, uint32_t *from,
+                            uint32_t *to, uint32_t *cedge, uint64_t *hkey, double *hval, uint64_t *vkey,
+                            double *vval) {
+    uint64_t n1 = nedges + 1;
+    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nedges;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t p = find_segment(off, npoly, e);
+        const PolyHdr &h = hdr[p];
+        uint32_t i = (uint32_t)(e - h.edge);
+        const float2 *r = sv.ring + h.ring;
+        // walk exactly the edges the count pass walked (those with output)
+        if (scan[e + 1] == scan[e] && scan[n1 + e + 1] == scan[n1 + e] && scan[2 * n1 + e + 1] == scan[2 * n1 + e])
+            continue;
+        FillSink s;
+        s.dimx = h.dimx;
+        s.dimy = h.dimy;
+        s.edge = i;
+        s.c = scan[e];
+        s.hn = scan[n1 + e];
+        s.vn = scan[2 * n1 + e];
+        s.from = from;
+        s.to = to;
+        s.cedge = cedge;
+        s.hkey = hkey;
+        s.hval = hval;
+        s.vkey = vkey;
+        s.vval = vval;
+        s.hline = h.hline;
+        s.vline = h.vline;
+        walk_edge(h, r[i], r[i + 1], s);
+    }
+}
+
+// per polygon crossing base and sequence count
+__global__ void k_cross_base(PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off, uint32_t npoly,
+                             const uint64_t *__restrict__ escan, uint64_t *__restrict__ cbase,
+                             uint64_t *__restrict__ nseq) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p <= npoly; p += gridDim.x * blockDim.x) {
+        uint64_t cb = escan[off[p]];
+        cbase[p] = cb;
+        if (p < npoly) {
+            uint64_t ce = escan[off[p + 1]];
+            uint64_t c = ce - cb;
+            hdr[p].cross = cb;
+            nseq[p] = c ? c + 1 : 1;
+            if (!c && hdr[p].P != 1) hdr[p].err = FARM_EASSERT;
+        } else {
+            nseq[p] = 0;
+        }
+    }
+}
+
+// Visits: crossing c enters pixel to[c]; the visit ends at the next crossing
+// (which must leave that pixel). The ring's last crossing closes the visit to
+// the start pixel that the first crossing left; it is placed first so that,
+// after a stable sort by pixel, its two sequences lead that pixel's list, as
+// the LEAVE-first case of Ideal.cpp:158-165 orders them.
+__global__ void k_visits(PolyHdr *__restrict__ hdr, uint32_t npoly, const uint64_t *__restrict__ cbase,
+                         uint64_t ncross, const uint32_t *__restrict__ from, const uint32_t *__restrict__ to,
+                         const uint32_t *__restrict__ cedge, uint64_t *__restrict__ vkey,
+                         uint64_t *__restrict__ vval) {
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncross;
+         c += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t p = find_segment(cbase, npoly, c);
+        uint64_t cb = cbase[p], ce = cbase[p + 1];
+        const PolyHdr &h = hdr[p];
+        uint64_t pos;
+        uint32_t ein = cedge[c], eout;
+        bool wrap = (c == ce - 1);
+        uint64_t nxt = wrap ? cb : c + 1;
+        eout = cedge[nxt];
+        if (from[nxt] != to[c]) atomicMin(&hdr[p].err, FARM_EASSERT);
+        pos = wrap ? cb : c + 1;
+        vkey[pos] = h.pix + to[c];
+        vval[pos] = ((uint64_t)ein << 32) | (uint64_t)eout | (wrap ? (1ull << 63) : 0ull);
+    }
+}
+
+__global__ void k_seq_width(const uint64_t *__restrict__ vkey, const uint64_t *__restrict__ vval, uint64_t n,
+                            uint64_t *__restrict__ w, uint32_t *__restrict__ pixcnt) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t wd = (vval[k] >> 63) ? 2u : 1u;
+        w[k] = wd;
+        atomicAdd(&pixcnt[vkey[k]], wd);
+    }
+}
+
+__global__ void k_seq_fill(PolyHdr *__restrict__ hdr, uint32_t npoly, const uint64_t *__restrict__ cbase,
+                           const uint64_t *__restrict__ seqbase, const uint64_t *__restrict__ vval,
+                           const uint64_t *__restrict__ wscan, uint64_t n, uint2 *__restrict__ seq) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t p = find_segment(cbase, npoly, k);
+        uint64_t cb = cbase[p];
+        uint64_t at = seqbase[p] + (wscan[k] - wscan[cb]);
+        uint64_t v = vval[k];
+        uint32_t ein = (uint32_t)((v >> 32) & 0x7FFFFFFFu), eout = (uint32_t)(v & 0xFFFFFFFFu);
+        uint32_t nv = hdr[p].nv;
+        if (v >> 63) {
+            // add_edge(0, first leave) and add_edge(last enter, nv - 2)
+            seq[at] = make_uint2(0u, eout + 1u);
+            seq[at + 1] = make_uint2(ein, nv - 2u - ein + 1u);
+        } else {
+            if (eout < ein) atomicMin(&hdr[p].err, FARM_EASSERT);
+            seq[at] = make_uint2(ein, eout - ein + 1u);
+        }
+    }
+}
+
+// Polygons without crossings: one sequence covering the ring (Ideal.cpp:523-529).
+__global__ void k_seq_single(PolyHdr *__restrict__ hdr, uint32_t npoly, const uint64_t *__restrict__ seqbase,
+                             const uint64_t *__restrict__ cbase, uint2 *__restrict__ seq, uint32_t *__restrict__ pixcnt) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npoly; p += gridDim.x * blockDim.x) {
+        PolyHdr &h = hdr[p];
+        h.seq = seqbase[p];
+        h.n_seq = (uint32_t)(seqbase[p + 1] - seqbase[p]);
+        if (cbase[p + 1] == cbase[p]) {
+            seq[h.seq] = make_uint2(0u, h.nv);
+            pixcnt[h.pix] += 1;
+        }
+    }
+}
+
+// CSR offsets: offset[i] = sequences in pixels before i (Ideal.cpp:35-45 makes
+// non-BORDER pixels repeat the next start, which is the same prefix).
+__global__ void k_offsets(const PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ pixbase, uint32_t npoly,
+                          uint64_t totP, const uint64_t *__restrict__ pscan, uint32_t *__restrict__ offset) {
+    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < totP; g += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t p = find_segment(pixbase, npoly, g);
+        const PolyHdr &h = hdr[p];
+        uint32_t i = (uint32_t)(g - h.pix);
+        offset[h.off + i] = (uint32_t)(pscan[g] - pscan[h.pix]);
+        if (i == 0) offset[h.off + h.P] = h.n_seq;
+    }
+}
+
+__global__ void k_line_count(const uint64_t *__restrict__ key, uint64_t n, uint32_t *__restrict__ cnt) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
+        atomicAdd(&cnt[key[k]], 1u);
+}
+
+__global__ void k_line_scatter(const uint64_t *__restrict__ key, const double *__restrict__ val, uint64_t n,
+                               const uint64_t *__restrict__ start, uint32_t *__restrict__ fillc,
+                               double *__restrict__ out) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t l = key[k];
+        uint32_t r = atomicAdd(&fillc[l], 1u);
+        out[start[l] + r] = val[k];
+    }
+}
+
+// Grid-line offsets (Ideal.cpp:185-238): lines with nodes get their start,
+// others keep 0; the end entries get the node count.
+__global__ void k_line_offsets(PolyHdr *__restrict__ hdr, uint32_t npoly, int vertical,
+                               const uint32_t *__restrict__ cnt, const uint64_t *__restrict__ start,
+                               uint32_t *__restrict__ loff) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npoly; p += gridDim.x * blockDim.x) {
+        PolyHdr &h = hdr[p];
+        uint64_t lb = vertical ? h.vline : h.hline;
+        int dim = vertical ? h.dimx : h.dimy;
+        uint64_t nb = start[lb];
+        uint32_t total = (uint32_t)(start[lb + dim + 2] - nb);
+        for (int l = 0; l < dim + 2; l++) loff[lb + l] = cnt[lb + l] ? (uint32_t)(start[lb + l] - nb) : 0u;
+        loff[lb + dim] = total;
+        if (vertical) {
+            loff[lb + dim + 1] = total;
+            h.vnode = nb;
+            h.n_vnodes = total;
+        } else {
+            h.hnode = nb;
+            h.n_hnodes = total;
+        }
+    }
+}
+
+// Ideal.cpp:540-573, one thread per row.
+__global__ void k_scanline(const PolyHdr *__restrict__ hdr, uint32_t npoly, const uint64_t *__restrict__ rowbase,
+                           uint64_t nrows, uint8_t *__restrict__ status, const uint32_t *__restrict__ hoff,
+                           const double *__restrict__ hnodes, int cc) {
+    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < nrows; g += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t p = find_segment(rowbase, npoly, g);
+        const PolyHdr &h = hdr[p];
+        int y = (int)(g - rowbase[p]);
+        if (y < 1 || y >= h.dimy || h.err) continue;
+        const double start_x = h.mbr[0];
+        bool isin = false;
+        uint32_t i = hoff[h.hline + y], j = hoff[h.hline + y + 1];
+        const double *nodes = hnodes + h.hnode;
+        uint8_t *st = status + h.st + (uint64_t)y * h.dimx;
+        for (int x = 0; x < h.dimx; x++) {
+            if (show_status(st[x], cc) != 1) {
+                st[x] = isin ? 2 : 0;
+                continue;
+            }
+            int pass = 0;
+            while (i < j && nodes[i] <= start_x + h.step_x * (x + 1)) {
+                pass++;
+                i++;
+            }
+            if (pass % 2 == 1) isin = !isin;
+        }
+    }
+}
+
+// ------------------------------------------------------------ fill ----
+
+__device__ inline bool in_rng(double lo, double hi, double v) { return !(v < lo || v > hi); }
+
+__device__ inline float2 mk(double x, double y) { return make_float2((float)x, (float)y); }
+
+// Points one edge contributes to column c's clip (Ideal.cpp:575-678), in order.
+// Returns the count; writes up to 4 points when out != nullptr.
+__device__ int clip_x_points(float2 A, float2 B, double Xi, double Xi1, float2 *out) {
+    int n = 0;
+    double yi, yi1;
+    if (A.x == B.x) {
+        yi = A.y < B.y ? A.y : B.y;
+        yi1 = yi;
+    } else {
+        double slope = ((double)B.y - A.y) / (double)(B.x - A.x);
+        yi = slope * (Xi - B.x) + B.y;
+        yi1 = slope * (Xi1 - B.x) + B.y;
+    }
+    float2 pi = mk(Xi, yi), pi1 = mk(Xi1, yi1);
+    double mny = A.y < B.y ? A.y : B.y, mxy = A.y < B.y ? B.y : A.y;
+    double mnx = A.x < B.x ? A.x : B.x, mxx = A.x < B.x ? B.x : A.x;
+    if (in_rng(Xi, Xi1, A.x)) {
+        if (out) out[n] = A;
+        n++;
+    }
+    bool c0 = in_rng(mny, mxy, pi.y) && in_rng(mnx, mxx, pi.x);
+    bool c1 = in_rng(mny, mxy, pi1.y) && in_rng(mnx, mxx, pi1.x);
+    if (A.x < B.x) {
+        if (c0) { if (out) out[n] = pi; n++; }
+        if (c1) { if (out) out[n] = pi1; n++; }
+    } else {
+        if (c1) { if (out) out[n] = pi1; n++; }
+        if (c0) { if (out) out[n] = pi; n++; }
+    }
+    if (in_rng(Xi, Xi1, B.x)) {
+        if (out) out[n] = B;
+        n++;
+    }
+    return n;
+}
+
+// Points one column-polygon edge contributes to row r's clip (Ideal.cpp:680-818).
+__device__ int clip_y_points(float2 A, float2 B, double Yi, double Yi1, float2 *out) {
+    int n = 0;
+    bool parallels = false;
+    double xi = 0, xi1 = 0;
+    if (A.x == B.x) {
+        xi = A.x;
+        xi1 = A.x;
+    } else {
+        double slope = ((double)B.y - A.y) / (double)(B.x - A.x);
+        if (A.y == B.y) {
+            if (A.y == Yi) {
+                xi = A.x;
+                xi1 = -INFINITY;  // -DBL_MAX, which converts to -inf in float
+            } else if (A.y == Yi1) {
+                xi = -INFINITY;
+                xi1 = A.x;
+            } else {
+                parallels = true;
+            }
+        } else {
+            xi = ((Yi - B.y) / slope) + B.x;
+            xi1 = ((Yi1 - B.y) / slope) + B.x;
+        }
+    }
+    if (in_rng(Yi, Yi1, A.y)) {
+        if (out) out[n] = A;
+        n++;
+    }
+    if (!parallels) {
+        float2 pi = mk(xi, Yi), pi1 = mk(xi1, Yi1);
+        double mny = A.y < B.y ? A.y : B.y, mxy = A.y < B.y ? B.y : A.y;
+        double mnx = A.x < B.x ? A.x : B.x, mxx = A.x < B.x ? B.x : A.x;
+        bool c0 = in_rng(mnx, mxx, pi.x) && in_rng(mny, mxy, pi.y);
+        bool c1 = in_rng(mnx, mxx, pi1.x) && in_rng(mny, mxy, pi1.y);
+        if (A.y < B.y) {
+            if (c0) { if (out) out[n] = pi; n++; }
+            if (c1) { if (out) out[n] = pi1; n++; }
+        } else {
+            if (c1) { if (out) out[n] = pi1; n++; }
+            if (c0) { if (out) out[n] = pi; n++; }
+        }
+    }
+    return n;
+}
+
+// first index i in [0, n) with lines[i] + step >= v, scanning down from a
+// binary-search guess (lines ascending)
+__device__ int first_line(const double *lines, int n, double step, double v) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (lines[mid] + step < v)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// margin covering the float rounding of a clip line coordinate
+__device__ inline double fmargin(double a, double b) { return (fabs(a) + fabs(b)) * 1.2e-7 + 1e-30; }
+
+// Per edge: points contributed to every column (count pass or emit pass).
+__global__ void k_clipx(const StoreView sv, const PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off,
+                        uint32_t npoly, uint64_t nedges, const double *__restrict__ colx, uint32_t *__restrict__ cnt,
+                        const uint64_t *__restrict__ scan, uint64_t *__restrict__ okey, float2 *__restrict__ opt) {
+    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nedges;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t p = find_segment(off, npoly, e);
+        const PolyHdr &h = hdr[p];
+        if (h.err) {
+            if (cnt) cnt[e] = 0;
+            continue;
+        }
+        uint32_t i = (uint32_t)(e - h.edge);
+        const float2 *r = sv.ring + h.ring;
+        float2 A = r[i], B = r[i + 1];
+        double mnx = A.x < B.x ? A.x : B.x, mxx = A.x < B.x ? B.x : A.x;
+        double mg = fmargin(mnx, mxx);
+        const double *lines = colx + h.col;
+        int c = first_line(lines, h.ncols, h.step_x, mnx - mg);
+        uint32_t total = 0;
+        uint64_t at = scan ? scan[e] : 0;
+        float2 buf[4];
+        for (; c < h.ncols && lines[c] <= mxx + mg; c++) {
+            double Xi = lines[c], Xi1 = Xi + h.step_x;
+            int k = clip_x_points(A, B, Xi, Xi1, okey ? buf : nullptr);
+            if (okey) {
+                for (int q = 0; q < k; q++) {
+                    okey[at] = h.col + (uint64_t)c;
+                    opt[at] = buf[q];
+                    at++;
+                }
+            }
+            total += (uint32_t)k;
+        }
+        if (cnt) cnt[e] = total;
+    }
+}
+
+// "Small" points: a coordinate below 2^-5 in magnitude, where two distinct
+// floats can be closer than the 1e-9 of Point::operator==. Elsewhere that
+// equality is bit equality (float spacing there exceeds 1e-9).
+__device__ inline bool small_pt(float2 q) { return fabsf(q.x) < 0.03125f || fabsf(q.y) < 0.03125f; }
+
+__device__ inline uint64_t pt_bits(float2 q) {
+    return ((uint64_t)__float_as_uint(q.x) << 32) | (uint64_t)__float_as_uint(q.y);
+}
+
+__global__ void k_ptbits(const float2 *__restrict__ pt, uint64_t n, uint64_t *__restrict__ bits,
+                         uint32_t *__restrict__ idx) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        bits[k] = pt_bits(pt[k]);
+        idx[k] = (uint32_t)k;
+    }
+}
+
+// After sorting by (column, bits, position): a non-first element of a run of
+// identical large points is a later duplicate (MyPolygon.h:49-58 drops it).
+__global__ void k_dup_large(const uint64_t *__restrict__ col, const uint32_t *__restrict__ pos,
+                            const float2 *__restrict__ pt, uint64_t n, uint8_t *__restrict__ drop,
+                            uint8_t *__restrict__ colsmall_flag_unused) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t me = pos[k];
+        float2 q = pt[me];
+        if (small_pt(q)) continue;
+        if (k > 0 && col[k - 1] == col[k]) {
+            float2 o = pt[pos[k - 1]];
+            if (pt_bits(o) == pt_bits(q)) drop[me] = 1;
+        }
+    }
+}
+
+__global__ void k_col_count(const uint64_t *__restrict__ colkey, const float2 *__restrict__ pt, uint64_t n,
+                            uint32_t *__restrict__ colcnt, uint8_t *__restrict__ colsmall) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        atomicAdd(&colcnt[colkey[k]], 1u);
+        if (small_pt(pt[k])) colsmall[colkey[k]] = 1;
+    }
+}
+
+// Columns holding small points: the reference's sequential rule, restricted to
+// the small points (a small point never equals a large one).
+__global__ void k_dup_small(const uint64_t *__restrict__ colstart, uint64_t ncol, const uint8_t *__restrict__ colsmall,
+                            const float2 *__restrict__ pt, uint8_t *__restrict__ drop) {
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncol; c += (uint64_t)gridDim.x * blockDim.x) {
+        if (!colsmall[c]) continue;
+        uint64_t b = colstart[c], e = colstart[c + 1];
+        for (uint64_t k = b; k < e; k++) {
+            float2 q = pt[k];
+            if (!small_pt(q)) continue;
+            bool dup = false;
+            for (uint64_t j = b; j < k && !dup; j++)
+                if (!drop[j] && small_pt(pt[j]) && pt_eq(pt[j], q)) dup = true;
+            if (dup) drop[k] = 1;
+        }
+    }
+}
+
+// Column polygons: kept points in order plus the closing copy of the first.
+__global__ void k_col_polys(const uint64_t *__restrict__ colkey, const float2 *__restrict__ pt,
+                            const uint8_t *__restrict__ drop, const uint64_t *__restrict__ keptscan, uint64_t n,
+                            const uint64_t *__restrict__ colstart, const uint64_t *__restrict__ cpstart,
+                            float2 *__restrict__ cpoly) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        if (drop[k]) continue;
+        uint64_t c = colkey[k];
+        uint64_t rank = keptscan[k] - keptscan[colstart[c]];
+        cpoly[cpstart[c] + rank] = pt[k];
+        if (rank == 0) {
+            uint64_t nk = keptscan[colstart[c + 1]] - keptscan[colstart[c]];
+            cpoly[cpstart[c] + nk] = pt[k];
+        }
+    }
+}
+
+__global__ void k_cp_sizes(const uint64_t *__restrict__ colstart, const uint8_t *__restrict__ drop_unused,
+                           const uint64_t *__restrict__ keptscan, uint64_t ncol, uint64_t *__restrict__ cpsize) {
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncol; c += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t nk = keptscan[colstart[c + 1]] - keptscan[colstart[c]];
+        cpsize[c] = nk ? nk + 1 : 0;
+    }
+}
+
+// Per column-polygon edge: points contributed to each row (count or emit).
+__global__ void k_clipy(const PolyHdr *__restrict__ hdr, uint32_t npoly, const uint64_t *__restrict__ colbase,
+                        const uint64_t *__restrict__ cpstart, uint64_t ncol, const float2 *__restrict__ cpoly,
+                        uint64_t ncp, const double *__restrict__ rowy, uint32_t *__restrict__ cnt,
+                        const uint64_t *__restrict__ scan, uint64_t *__restrict__ okey, float2 *__restrict__ opt,
+                        uint32_t *__restrict__ cellcnt) {
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < ncp; j += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t c = find_segment(cpstart, (uint32_t)ncol, j);
+        uint32_t total = 0;
+        if (j + 1 < cpstart[c + 1]) {
+            uint32_t p = find_segment(colbase, npoly, c);
+            const PolyHdr &h = hdr[p];
+            int x = (int)(c - h.col);
+            float2 A = cpoly[j], B = cpoly[j + 1];
+            double mny = A.y < B.y ? A.y : B.y, mxy = A.y < B.y ? B.y : A.y;
+            double mg = fmargin(mny, mxy);
+            const double *lines = rowy + h.row;
+            int r = first_line(lines, h.nrows, h.step_y, mny - mg);
+            uint64_t at = scan ? scan[j] : 0;
+            float2 buf[4];
+            for (; r < h.nrows && lines[r] <= mxy + mg; r++) {
+                double Yi = lines[r], Yi1 = Yi + h.step_y;
+                int k = clip_y_points(A, B, Yi, Yi1, okey ? buf : nullptr);
+                if (okey && k) {
+                    uint64_t cell = h.pix + (uint64_t)r * h.dimx + x;
+                    for (int q = 0; q < k; q++) {
+                        okey[at] = cell;
+                        opt[at] = buf[q];
+                        at++;
+                    }
+                    atomicAdd(&cellcnt[cell], (uint32_t)k);
+                }
+                total += (uint32_t)k;
+            }
+        }
+        if (cnt) cnt[j] = total;
+    }
+}
+
+// Per pixel: cell area (geometry_computation.h:275-297 over the cell's clip,
+// closed as Ideal.cpp:805-808 does) and the fill class (Ideal.cpp:880-914).
+__global__ void k_cells(PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ pixbase, uint32_t npoly, uint64_t totP,
+                        const uint64_t *__restrict__ cellstart, const float2 *__restrict__ cpt,
+                        const uint64_t *__restrict__ cpstart, uint8_t *__restrict__ status,
+                        double *__restrict__ areas, int cc) {
+    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < totP; g += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t p = find_segment(pixbase, npoly, g);
+        const PolyHdr &h = hdr[p];
+        if (h.err) continue;
+        uint32_t id = (uint32_t)(g - h.pix);
+        int x = (int)(id % (uint32_t)h.dimx), y = (int)(id / (uint32_t)h.dimx);
+        if (x >= h.ncols || y >= h.nrows) continue;
+        uint64_t cidx = h.col + (uint64_t)x;
+        if (cpstart[cidx + 1] == cpstart[cidx]) continue;  // empty column: not visited
+        uint64_t b = cellstart[g], e = cellstart[g + 1];
+        uint64_t n = e - b;
+        bool close = n > 0 && pt_ne(cpt[b], cpt[e - 1]);
+        uint64_t m = n + (close ? 1 : 0);
+        double area = 0.0;
+        if (m >= 3) {
+            for (uint64_t k = 0; k + 1 < m; k++) {
+                float2 p1 = cpt[b + k];
+                float2 p2 = (k + 1 < n) ? cpt[b + k + 1] : cpt[b];
+                area += ((double)p1.x * p2.y - (double)p2.x * p1.y);
+            }
+            area = fabs(area) / 2.0;
+        }
+        double pa = h.step_x * h.step_y;
+        int type = classify(area, pa, cc);
+        uint8_t *st = status + h.st + id;
+        uint8_t raw = *st;
+        if (raw == 1) {
+            int t = type < cc - 2 ? type : cc - 2;
+            *st = (uint8_t)(t > 1 ? t : 1);
+            areas[g] = area;
+        } else if (raw == 2) {
+            *st = (uint8_t)(cc - 1);
+            areas[g] = pa;
+        } else {
+            *st = 0;
+            areas[g] = 0.0;
+        }
+    }
+}
+
+// ---------------------------------------------------------- hierarchy --
+// Ideal.cpp:1008-1059: each coarse pixel sums the finest areas under it. The
+// reference leaves merge_area's status argument uninitialised; compiled, it
+// carries over from the previous coarse pixel (x outer, y inner), so once a
+// BORDER is seen the rest of the layer is classified as BORDER. Pass 1 finds
+// the first such pixel per layer; pass 2 classifies.
+__global__ void k_merge(const PolyHdr *__restrict__ hdr, uint32_t npoly, uint8_t *__restrict__ status,
+                        const double *__restrict__ areas, int cc, int pass, uint32_t *__restrict__ firstb,
+                        const uint64_t *__restrict__ lbase) {
+    uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t p = warp; p < npoly; p += nw) {
+        const PolyHdr &h = hdr[p];
+        if (h.err || h.num_layers < 2) continue;
+        for (int li = (int)h.num_layers - 2; li >= 0; li--) {
+            LayerGeom g;
+            layer_geom(h, (uint32_t)li, g);
+            uint32_t *fb = firstb + lbase[p] + li;
+            uint32_t np = (uint32_t)(g.dimx * g.dimy);
+            for (uint32_t k = lane; k < np; k += 32) {
+                int x = (int)(k / (uint32_t)g.dimy), y = (int)(k % (uint32_t)g.dimy);  // x outer
+                double lowx = g.mbr[0] + x * g.step_x, lowy = g.mbr[1] + y * g.step_y;
+                double highx = g.mbr[0] + (x + 1) * g.step_x, highy = g.mbr[1] + (y + 1) * g.step_y;
+                int sx = offset_x(h.mbr, h.step_x, h.dimx, lowx);
+                int sy = offset_y(h.mbr, h.step_y, h.dimy, lowy);
+                int ex = offset_x(h.mbr, h.step_x, h.dimx, highx) - 1;
+                int ey = offset_y(h.mbr, h.step_y, h.dimy, highy) - 1;
+                if (ey < sy) ey = sy;
+                if (ex < sx) ex = sx;
+                const uint8_t *fs = status + h.st;
+                bool border = false;
+                double area = 0.0;
+                for (int i = sx; i <= ex; i++)
+                    for (int j = sy; j <= ey; j++) {
+                        uint32_t id = (uint32_t)(j * h.dimx + i);
+                        if (show_status(fs[id], cc) == 1) border = true;
+                        if (pass == 1) area += areas[h.pix + id];
+                    }
+                if (pass == 0) {
+                    if (border) atomicMin(fb, k);
+                } else {
+                    int st = (k >= *fb) ? 1 : show_status(fs[sy * h.dimx + sx], cc);
+                    uint8_t full = st == 1 ? (uint8_t)classify(area, g.step_x * g.step_y, cc)
+                                           : (st == 2 ? (uint8_t)(cc - 1) : 0);
+                    status[h.st + g.offset + (uint32_t)(y * g.dimx + x)] = full;
+                }
+            }
+        }
+    }
+}
+
+__global__ void k_layer_count(const PolyHdr *__restrict__ hdr, uint32_t npoly, uint64_t *__restrict__ cnt) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npoly; p += gridDim.x * blockDim.x)
+        cnt[p] = hdr[p].num_layers;
+}
+
+__global__ void k_fill_u32(uint32_t *a, uint64_t n, uint32_t v) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
+        a[k] = v;
+}
+
+__global__ void k_u32_to_u64(const uint32_t *__restrict__ a, uint64_t n, uint64_t *__restrict__ b) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
+        b[k] = a[k];
+}
+
+__global__ void k_not_u8(const uint8_t *__restrict__ a, uint64_t n, uint64_t *__restrict__ b) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
+        b[k] = a[k] ? 0 : 1;
+}
+
+__global__ void k_err_reduce(const PolyHdr *__restrict__ hdr, uint32_t npoly, int *__restrict__ out) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npoly; p += gridDim.x * blockDim.x)
+        if (hdr[p].err) atomicMin(out, hdr[p].err);
+}
+
+__global__ void k_gather_u64(const uint64_t *src, const uint32_t *idx, uint64_t n, uint64_t *out) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
+        out[k] = src[idx[k]];
+}
+
+// ------------------------------------------------------------ host ----
+
+struct Launch {
+    cudaStream_t st;
+    int blocks_cap;
+    int count = 0;
+};
+
+template <typename F>
+static int cub_call(farm_store *s, F f) {
+    size_t bytes = 0;
+    FARM_CUDA(f(nullptr, bytes));
+    FARM_TRY(s->cub_tmp.ensure(bytes + 16));
+    FARM_CUDA(f(s->cub_tmp.p, bytes));
+    return FARM_OK;
+}
+
+// exclusive scan of n u64 values into out (n entries); returns total via host copy of out[n-1]+in[n-1]
+static int excl_scan(farm_store *s, const uint64_t *in, uint64_t *out, uint64_t n) {
+    if (n == 0) return FARM_OK;
+    return cub_call(s, [&](void *t, size_t &b) {
+        return cub::DeviceScan::ExclusiveSum(t, b, in, out, (int64_t)n, s->stream);
+    });
+}
+
+static int d2h_u64(farm_store *s, const uint64_t *d, uint64_t &v) {
+    FARM_CUDA(cudaMemcpyAsync(&v, d, 8, cudaMemcpyDeviceToHost, s->stream));
+    FARM_CUDA(cudaStreamSynchronize(s->stream));
+    return FARM_OK;
+}
+
+static int key_bits(uint64_t maxkey) {
+    int b = 1;
+    while (b < 64 && (maxkey >> b)) b++;
+    return b;
+}
+
+template <typename K, typename V>
+static int sort_pairs(farm_store *s, const K *kin, K *kout, const V *vin, V *vout, uint64_t n, int bits) {
+    if (n == 0) return FARM_OK;
+    return cub_call(s, [&](void *t, size_t &b) {
+        return cub::DeviceRadixSort::SortPairs(t, b, kin, kout, vin, vout, (int64_t)n, 0, bits, s->stream);
+    });
+}
+
+static unsigned gb(uint64_t n) {
+    uint64_t g = (n + 255) / 256;
+    uint64_t cap = 64ull * sm_count();
+    if (g > cap) g = cap;
+    return (unsigned)(g ? g : 1);
+}
+
+int rasterize(farm_store *s, const farm_raster_opts *o, int *launches) {
+    int L = 0;
+    uint32_t np = (uint32_t)s->n_poly;
+    uint64_t ne = s->n_edges;
+    if (np == 0) {
+        set_error("no polygons loaded");
+        return FARM_EINVAL;
+    }
+    RasterParams rp;
+    memset(&rp, 0, sizeof rp);
+    rp.vpr = o->vpr;
+    rp.cc = o->category_count;
+    rp.hier = o->hierarchy;
+    {
+        // UniversalGrid::configure(25) (UniversalGrid.h:29-35) with util.h:53-66
+        double num = 360.0 / pow(2, 25);
+        double d = ceil(log10(num < 0 ? -num : num));
+        int power = 2 - (int)d;
+        double magnitude = pow(10.0, power);
+        rp.gstep = round(num * magnitude) / magnitude;
+        for (int k = 0; k < 40; k++) rp.pow2_ceil[k] = (int)ceil(log((double)(1ull << (k < 62 ? k : 62))) / log(2.0));
+    }
+    cudaStream_t st = s->stream;
+    const uint64_t *doff = s->d_off.as<uint64_t>();
+    uint64_t n1 = (uint64_t)np + 1;
+    FARM_TRY(s->d_hdr.ensure(sizeof(PolyHdr) * np));
+    FARM_TRY(s->s[S_SIZES].ensure(9 * n1 * 8));
+    FARM_TRY(s->s[S_SCAN].ensure(9 * n1 * 8));
+    FARM_CUDA(cudaMemsetAsync(s->s[S_SIZES].p, 0, 9 * n1 * 8, st));
+    PolyHdr *hdr = s->d_hdr.as<PolyHdr>();
+    uint64_t *sizes = s->s[S_SIZES].as<uint64_t>(), *scan = s->s[S_SCAN].as<uint64_t>();
+    k_header<<<gb(32ull * np), 256, 0, st>>>(s->d_ring.as<float2>(), doff, np, rp, hdr, sizes);
+    L++;
+    for (int t = 0; t < 8; t++) FARM_TRY(excl_scan(s, sizes + t * n1, scan + t * n1, n1));
+    uint64_t tot[8];
+    FARM_CUDA(cudaMemcpyAsync(tot, scan, 8, cudaMemcpyDeviceToHost, st));
+    for (int t = 0; t < 8; t++) FARM_CUDA(cudaMemcpyAsync(&tot[t], scan + t * n1 + np, 8, cudaMemcpyDeviceToHost, st));
+    FARM_CUDA(cudaStreamSynchronize(st));
+    const uint64_t totP = tot[0], totStatus = tot[1], totOff = tot[2], totH = tot[3], totV = tot[4], totCol = tot[5],
+                   totRow = tot[6], totScanRows = tot[7];
+    FARM_TRY(s->d_status.ensure(totStatus + 16));
+    FARM_TRY(s->d_offset.ensure(4 * totOff + 16));
+    FARM_TRY(s->d_areas.ensure(8 * totP + 16));
+    FARM_TRY(s->d_hoff.ensure(4 * totH + 16));
+    FARM_TRY(s->d_voff.ensure(4 * totV + 16));
+    FARM_TRY(s->s[S_COLX].ensure(8 * totCol + 16));
+    FARM_TRY(s->s[S_ROWY].ensure(8 * totRow + 16));
+    FARM_CUDA(cudaMemsetAsync(s->d_status.p, 0, totStatus + 16, st));
+    FARM_CUDA(cudaMemsetAsync(s->d_areas.p, 0, 8 * totP + 16, st));
+    double *colx = s->s[S_COLX].as<double>(), *rowy = s->s[S_ROWY].as<double>();
+    k_bases<<<gb(np), 256, 0, st>>>(hdr, np, scan, colx, rowy);
+    L++;
+    StoreView sv = s->view();
+    sv.category_count = o->category_count;
+
+    // ---- edge walk: count, scan, fill
+    uint64_t ne1 = ne + 1;
+    FARM_TRY(s->s[S_CNT_E].ensure(3 * ne1 * 4 + 16));
+    FARM_TRY(s->s[S_TMP_A].ensure(3 * ne1 * 8 + 16));
+    FARM_TRY(s->s[S_SCAN_E].ensure(3 * ne1 * 8 + 16));
+    uint32_t *ecnt = s->s[S_CNT_E].as<uint32_t>();
+    FARM_CUDA(cudaMemsetAsync(ecnt, 0, 3 * ne1 * 4, st));
+    k_walk_count<<<gb(ne), 256, 0, st>>>(sv, hdr, doff, np, ne, ecnt);
+    L++;
+    uint64_t *ecnt64 = s->s[S_TMP_A].as<uint64_t>(), *escan = s->s[S_SCAN_E].as<uint64_t>();
+    k_u32_to_u64<<<gb(3 * ne1), 256, 0, st>>>(ecnt, 3 * ne1, ecnt64);
+    L++;
+    for (int t = 0; t < 3; t++) FARM_TRY(excl_scan(s, ecnt64 + t * ne1, escan + t * ne1, ne1));
+    uint64_t nC, nH, nV;
+    FARM_TRY(d2h_u64(s, escan + ne, nC));
+    FARM_TRY(d2h_u64(s, escan + ne1 + ne, nH));
+    FARM_TRY(d2h_u64(s, escan + 2 * ne1 + ne, nV));
+    FARM_TRY(s->s[S_CFROM].ensure(4 * nC + 16));
+    FARM_TRY(s->s[S_CTO].ensure(4 * nC + 16));
+    FARM_TRY(s->s[S_CEDGE].ensure(4 * nC + 16));
+    FARM_TRY(s->s[S_HKEY].ensure(8 * nH + 16));
+    FARM_TRY(s->s[S_HVAL].ensure(8 * nH + 16));
+    FARM_TRY(s->s[S_VNKEY].ensure(8 * nV + 16));
+    FARM_TRY(s->s[S_VNVAL].ensure(8 * nV + 16));
+    uint32_t *cfrom = s->s[S_CFROM].as<uint32_t>(), *cto = s->s[S_CTO].as<uint32_t>(),
+             *cedge = s->s[S_CEDGE].as<uint32_t>();
+    k_walk_fill<<<gb(ne), 256, 0, st>>>(sv, hdr, doff, np, ne, escan, cfrom, cto, cedge, s->s[S_HKEY].as<uint64_t>(),
+                                        s->s[S_HVAL].as<double>(), s->s[S_VNKEY].as<uint64_t>(),
+                                        s->s[S_VNVAL].as<double>());
+    L++;
+
+    // ---- visits -> edge sequences (process_crosses)
+    FARM_TRY(s->s[S_TMP_B].ensure(2 * n1 * 8 + 16));
+    uint64_t *cbase = s->s[S_TMP_B].as<uint64_t>(), *nseq = cbase + n1;
+    k_cross_base<<<gb(n1), 256, 0, st>>>(hdr, doff, np, escan, cbase, nseq);
+    L++;
+    FARM_TRY(s->s[S_VKEY].ensure(8 * nC + 16));
+    FARM_TRY(s->s[S_VVAL].ensure(8 * nC + 16));
+    FARM_TRY(s->s[S_VKEY2].ensure(8 * nC + 16));
+    FARM_TRY(s->s[S_VVAL2].ensure(8 * nC + 16));
+    uint64_t *vkey = s->s[S_VKEY].as<uint64_t>(), *vval = s->s[S_VVAL].as<uint64_t>();
+    uint64_t *vkey2 = s->s[S_VKEY2].as<uint64_t>(), *vval2 = s->s[S_VVAL2].as<uint64_t>();
+    if (nC) {
+        k_visits<<<gb(nC), 256, 0, st>>>(hdr, np, cbase, nC, cfrom, cto, cedge, vkey, vval);
+        L++;
+        FARM_TRY(sort_pairs(s, vkey, vkey2, vval, vval2, nC, key_bits(totP)));
+    }
+    FARM_TRY(s->s[S_PIXCNT].ensure(4 * (totP + 1) + 16));
+    uint32_t *pixcnt = s->s[S_PIXCNT].as<uint32_t>();
+    FARM_CUDA(cudaMemsetAsync(pixcnt, 0, 4 * (totP + 1), st));
+    FARM_TRY(s->s[S_SEQW].ensure(2 * 8 * (nC + 1) + 16));
+    uint64_t *w = s->s[S_SEQW].as<uint64_t>(), *wscan = w + nC + 1;
+    // per polygon sequence bases
+    FARM_TRY(s->s[S_PIXSCAN].ensure(8 * (totP + 1) + 8 * n1 + 16));
+    uint64_t *seqbase = s->s[S_PIXSCAN].as<uint64_t>() + (totP + 1);
+    FARM_TRY(excl_scan(s, nseq, seqbase, n1));
+    uint64_t totSeq;
+    FARM_TRY(d2h_u64(s, seqbase + np, totSeq));
+    FARM_TRY(s->d_seq.ensure(8 * totSeq + 16));
+    uint2 *seq = s->d_seq.as<uint2>();
+    if (nC) {
+        k_seq_width<<<gb(nC), 256, 0, st>>>(vkey2, vval2, nC, w, pixcnt);
+        L++;
+        FARM_TRY(excl_scan(s, w, wscan, nC + 1));
+        k_seq_fill<<<gb(nC), 256, 0, st>>>(hdr, np, cbase, seqbase, vval2, wscan, nC, seq);
+        L++;
+    }
+    k_seq_single<<<gb(np), 256, 0, st>>>(hdr, np, seqbase, cbase, seq, pixcnt);
+    L++;
+    // offsets
+    {
+        uint64_t *p64 = s->s[S_TMP_A].as<uint64_t>();  // reuse: totP+1 u64 needed
+        FARM_TRY(s->s[S_TMP_A].ensure(8 * (totP + 1) + 16));
+        p64 = s->s[S_TMP_A].as<uint64_t>();
+        k_u32_to_u64<<<gb(totP + 1), 256, 0, st>>>(pixcnt, totP + 1, p64);
+        L++;
+        uint64_t *pscan = s->s[S_PIXSCAN].as<uint64_t>();
+        FARM_TRY(excl_scan(s, p64, pscan, totP + 1));
+        k_offsets<<<gb(totP), 256, 0, st>>>(hdr, scan + 0 * n1, np, totP, pscan, s->d_offset.as<uint32_t>());
+        L++;
+    }
+
+    // ---- grid lines (process_intersection)
+    for (int vert = 0; vert < 2; vert++) {
+        uint64_t nn = vert ? nV : nH;
+        uint64_t nl = vert ? totV : totH;
+        const uint64_t *key = vert ? s->s[S_VNKEY].as<uint64_t>() : s->s[S_HKEY].as<uint64_t>();
+        const double *val = vert ? s->s[S_VNVAL].as<double>() : s->s[S_HVAL].as<double>();
+        DevBuf &nodes = vert ? s->d_vnodes : s->d_hnodes;
+        FARM_TRY(nodes.ensure(8 * nn + 16));
+        FARM_TRY(s->s[S_LINECNT].ensure(2 * 4 * (nl + 1) + 16));
+        FARM_TRY(s->s[S_LINESCAN].ensure(2 * 8 * (nl + 1) + 16));
+        uint32_t *lcnt = s->s[S_LINECNT].as<uint32_t>(), *lfill = lcnt + (nl + 1);
+        uint64_t *lc64 = s->s[S_LINESCAN].as<uint64_t>(), *lstart = lc64 + (nl + 1);
+        FARM_CUDA(cudaMemsetAsync(lcnt, 0, 2 * 4 * (nl + 1), st));
+        if (nn) {
+            k_line_count<<<gb(nn), 256, 0, st>>>(key, nn, lcnt);
+            L++;
+        }
+        k_u32_to_u64<<<gb(nl + 1), 256, 0, st>>>(lcnt, nl + 1, lc64);
+        L++;
+        FARM_TRY(excl_scan(s, lc64, lstart, nl + 1));
+        FARM_TRY(s->s[S_TMP_B].ensure(2 * n1 * 8 + 8 * nn + 16));
+        cbase = s->s[S_TMP_B].as<uint64_t>();  // (re-fetched: buffer may have moved)
+        double *unsorted = reinterpret_cast<double *>(cbase + 2 * n1);
+        if (nn) {
+            k_line_scatter<<<gb(nn), 256, 0, st>>>(key, val, nn, lstart, lfill, unsorted);
+            L++;
+            FARM_TRY(cub_call(s, [&](void *t, size_t &b) {
+                return cub::DeviceSegmentedSort::SortKeys(t, b, unsorted, nodes.as<double>(), (int64_t)nn, (int64_t)nl,
+                                                          lstart, lstart + 1, st);
+            }));
+        }
+        k_line_offsets<<<gb(np), 256, 0, st>>>(hdr, np, vert, lcnt, lstart,
+                                               vert ? s->d_voff.as<uint32_t>() : s->d_hoff.as<uint32_t>());
+        L++;
+    }
+
+    // ---- scanline
+    sv = s->view();
+    sv.category_count = o->category_count;
+    k_scanline<<<gb(totScanRows), 256, 0, st>>>(hdr, np, scan + 7 * n1, totScanRows, s->d_status.as<uint8_t>(),
+                                                s->d_hoff.as<uint32_t>(), s->d_hnodes.as<double>(), o->category_count);
+    L++;
+
+    // ---- fill: strip clip per column
+    uint32_t *xcnt = s->s[S_CNT_E].as<uint32_t>();
+    k_clipx<<<gb(ne), 256, 0, st>>>(sv, hdr, doff, np, ne, colx, xcnt, nullptr, nullptr, nullptr);
+    L++;
+    uint64_t *x64 = s->s[S_TMP_A].as<uint64_t>();
+    FARM_TRY(s->s[S_TMP_A].ensure(8 * ne1 + 16));
+    x64 = s->s[S_TMP_A].as<uint64_t>();
+    FARM_CUDA(cudaMemsetAsync(xcnt + ne, 0, 4, st));
+    k_u32_to_u64<<<gb(ne1), 256, 0, st>>>(xcnt, ne1, x64);
+    L++;
+    uint64_t *xscan = s->s[S_SCAN_E].as<uint64_t>();
+    FARM_TRY(excl_scan(s, x64, xscan, ne1));
+    uint64_t nX;
+    FARM_TRY(d2h_u64(s, xscan + ne, nX));
+    // buffers: keys/points (emit order), then sorted by column
+    FARM_TRY(s->s[S_VKEY].ensure(8 * nX + 16));
+    FARM_TRY(s->s[S_VVAL].ensure(8 * nX + 16));
+    FARM_TRY(s->s[S_VKEY2].ensure(8 * nX + 16));
+    FARM_TRY(s->s[S_VVAL2].ensure(8 * nX + 16));
+    uint64_t *xkey = s->s[S_VKEY].as<uint64_t>(), *xkey_s = s->s[S_VKEY2].as<uint64_t>();
+    float2 *xpt = s->s[S_VVAL].as<float2>(), *xpt_s = s->s[S_VVAL2].as<float2>();
+    if (nX) {
+        k_clipx<<<gb(ne), 256, 0, st>>>(sv, hdr, doff, np, ne, colx, nullptr, xscan, xkey, xpt);
+        L++;
+        FARM_TRY(sort_pairs(s, xkey, xkey_s, reinterpret_cast<uint64_t *>(xpt), reinterpret_cast<uint64_t *>(xpt_s),
+                            nX, key_bits(totCol)));
+    }
+    // duplicates: sort (bits, position) then stable by column
+    FARM_TRY(s->s[S_HKEY].ensure(8 * nX + 16));
+    FARM_TRY(s->s[S_HVAL].ensure(8 * nX + 16));
+    FARM_TRY(s->s[S_VNKEY].ensure(8 * nX + 16));
+    FARM_TRY(s->s[S_VNVAL].ensure(8 * nX + 16));
+    FARM_TRY(s->s[S_CFROM].ensure(4 * nX + 16));
+    FARM_TRY(s->s[S_CTO].ensure(4 * nX + 16));
+    FARM_TRY(s->s[S_SEQW].ensure(nX + 32 + 8 * (nX + 1) * 2));
+    uint64_t *bits = s->s[S_HKEY].as<uint64_t>(), *bits_s = s->s[S_HVAL].as<uint64_t>();
+    uint64_t *ck = s->s[S_VNKEY].as<uint64_t>(), *ck_s = s->s[S_VNVAL].as<uint64_t>();
+    uint32_t *pos = s->s[S_CFROM].as<uint32_t>(), *pos_s = s->s[S_CTO].as<uint32_t>();
+    uint8_t *drop = s->s[S_SEQW].as<uint8_t>();
+    uint64_t *keptscan = reinterpret_cast<uint64_t *>(s->s[S_SEQW].as<uint8_t>() + ((nX + 16 + 7) & ~7ull));
+    uint64_t *kept64 = keptscan + (nX + 1);
+    FARM_CUDA(cudaMemsetAsync(drop, 0, nX + 1, st));
+    if (nX) {
+        k_ptbits<<<gb(nX), 256, 0, st>>>(xpt_s, nX, bits, pos);
+        L++;
+        FARM_TRY(sort_pairs(s, bits, bits_s, pos, pos_s, nX, 64));
+        // column of each element in (bits) order, then stable sort by column
+        FARM_TRY(s->s[S_CEDGE].ensure(4 * nX + 16));
+        // gather column keys for pos_s
+        uint32_t *pos2 = s->s[S_CEDGE].as<uint32_t>();
+        // ck[k] = column of the k-th element in bit order
+        k_gather_u64<<<gb(nX), 256, 0, st>>>(xkey_s, pos_s, nX, ck);
+        L++;
+        FARM_TRY(sort_pairs(s, ck, ck_s, pos_s, pos2, nX, key_bits(totCol)));
+        k_dup_large<<<gb(nX), 256, 0, st>>>(ck_s, pos2, xpt_s, nX, drop, nullptr);
+        L++;
+    }
+    // column starts and small-point columns
+    FARM_TRY(s->s[S_LINECNT].ensure(4 * (totCol + 1) + (totCol + 1) + 16));
+    FARM_TRY(s->s[S_LINESCAN].ensure(8 * (totCol + 1) * 2 + 16));
+    uint32_t *colcnt = s->s[S_LINECNT].as<uint32_t>();
+    uint8_t *colsmall = reinterpret_cast<uint8_t *>(colcnt + (totCol + 1));
+    uint64_t *cc64 = s->s[S_LINESCAN].as<uint64_t>(), *colstart = cc64 + (totCol + 1);
+    FARM_CUDA(cudaMemsetAsync(colcnt, 0, 4 * (totCol + 1) + (totCol + 1), st));
+    if (nX) {
+        k_col_count<<<gb(nX), 256, 0, st>>>(xkey_s, xpt_s, nX, colcnt, colsmall);
+        L++;
+    }
+    k_u32_to_u64<<<gb(totCol + 1), 256, 0, st>>>(colcnt, totCol + 1, cc64);
+    L++;
+    FARM_TRY(excl_scan(s, cc64, colstart, totCol + 1));
+    k_dup_small<<<gb(totCol), 256, 0, st>>>(colstart, totCol, colsmall, xpt_s, drop);
+    L++;
+    // kept scan and column polygons
+    k_not_u8<<<gb(nX + 1), 256, 0, st>>>(drop, nX + 1, kept64);
+    L++;
+    FARM_TRY(excl_scan(s, kept64, keptscan, nX + 1));
+    FARM_TRY(s->s[S_PIXSCAN].ensure(8 * (totCol + 1) * 2 + 16));
+    uint64_t *cpsize = s->s[S_PIXSCAN].as<uint64_t>(), *cpstart = cpsize + (totCol + 1);
+    FARM_CUDA(cudaMemsetAsync(cpsize, 0, 8 * (totCol + 1), st));
+    k_cp_sizes<<<gb(totCol), 256, 0, st>>>(colstart, drop, keptscan, totCol, cpsize);
+    L++;
+    FARM_TRY(excl_scan(s, cpsize, cpstart, totCol + 1));
+    uint64_t nCP;
+    FARM_TRY(d2h_u64(s, cpstart + totCol, nCP));
+    DevBuf cpbuf;
+    FARM_TRY(cpbuf.ensure(8 * nCP + 16));
+    float2 *cpoly = cpbuf.as<float2>();
+    if (nX) {
+        k_col_polys<<<gb(nX), 256, 0, st>>>(xkey_s, xpt_s, drop, keptscan, nX, colstart, cpstart, cpoly);
+        L++;
+    }
+
+    // ---- fill: cell clip per row
+    FARM_TRY(s->s[S_CNT_E].ensure(4 * (nCP + 1) + 16));
+    uint32_t *ycnt = s->s[S_CNT_E].as<uint32_t>();
+    FARM_CUDA(cudaMemsetAsync(ycnt, 0, 4 * (nCP + 1), st));
+    FARM_TRY(s->s[S_PIXCNT].ensure(4 * (totP + 1) + 16));
+    uint32_t *cellcnt = s->s[S_PIXCNT].as<uint32_t>();
+    FARM_CUDA(cudaMemsetAsync(cellcnt, 0, 4 * (totP + 1), st));
+    const uint64_t *colbase = scan + 5 * n1;
+    if (nCP) {
+        k_clipy<<<gb(nCP), 256, 0, st>>>(hdr, np, colbase, cpstart, totCol, cpoly, nCP, rowy, ycnt, nullptr, nullptr,
+                                         nullptr, nullptr);
+        L++;
+    }
+    FARM_TRY(s->s[S_TMP_A].ensure(8 * (nCP + 1) + 16));
+    uint64_t *y64 = s->s[S_TMP_A].as<uint64_t>();
+    k_u32_to_u64<<<gb(nCP + 1), 256, 0, st>>>(ycnt, nCP + 1, y64);
+    L++;
+    FARM_TRY(s->s[S_SCAN_E].ensure(8 * (nCP + 1) + 16));
+    uint64_t *yscan = s->s[S_SCAN_E].as<uint64_t>();
+    FARM_TRY(excl_scan(s, y64, yscan, nCP + 1));
+    uint64_t nY;
+    FARM_TRY(d2h_u64(s, yscan + nCP, nY));
+    DevBuf ykb, ypb, yks, yps;
+    FARM_TRY(ykb.ensure(8 * nY + 16));
+    FARM_TRY(ypb.ensure(8 * nY + 16));
+    FARM_TRY(yks.ensure(8 * nY + 16));
+    FARM_TRY(yps.ensure(8 * nY + 16));
+    if (nY) {
+        k_clipy<<<gb(nCP), 256, 0, st>>>(hdr, np, colbase, cpstart, totCol, cpoly, nCP, rowy, nullptr, yscan,
+                                         ykb.as<uint64_t>(), ypb.as<float2>(), cellcnt);
+        L++;
+        FARM_TRY(sort_pairs(s, ykb.as<uint64_t>(), yks.as<uint64_t>(), ypb.as<uint64_t>(), yps.as<uint64_t>(), nY,
+                            key_bits(totP)));
+    }
+    FARM_TRY(s->s[S_TMP_A].ensure(8 * (totP + 1) * 2 + 16));
+    uint64_t *c64 = s->s[S_TMP_A].as<uint64_t>(), *cellstart = c64 + (totP + 1);
+    k_u32_to_u64<<<gb(totP + 1), 256, 0, st>>>(cellcnt, totP + 1, c64);
+    L++;
+    FARM_TRY(excl_scan(s, c64, cellstart, totP + 1));
+    k_cells<<<gb(totP), 256, 0, st>>>(hdr, scan + 0 * n1, np, totP, cellstart, yps.as<float2>(), cpstart,
+                                      s->d_status.as<uint8_t>(), s->d_areas.as<double>(), o->category_count);
+    L++;
+
+    // ---- hierarchy
+    if (o->hierarchy) {
+        FARM_TRY(s->s[S_TMP_B].ensure(2 * 8 * n1 + 16));
+        uint64_t *lc = s->s[S_TMP_B].as<uint64_t>(), *lb = lc + n1;
+        FARM_CUDA(cudaMemsetAsync(lc, 0, 8 * n1, st));
+        k_layer_count<<<gb(np), 256, 0, st>>>(hdr, np, lc);
+        L++;
+        FARM_TRY(excl_scan(s, lc, lb, n1));
+        uint64_t nl;
+        FARM_TRY(d2h_u64(s, lb + np, nl));
+        DevBuf fb;
+        FARM_TRY(fb.ensure(4 * nl + 16));
+        k_fill_u32<<<gb(nl), 256, 0, st>>>(fb.as<uint32_t>(), nl, 0xFFFFFFFFu);
+        L++;
+        k_merge<<<gb(32ull * np), 256, 0, st>>>(hdr, np, s->d_status.as<uint8_t>(), s->d_areas.as<double>(),
+                                               o->category_count, 0, fb.as<uint32_t>(), lb);
+        k_merge<<<gb(32ull * np), 256, 0, st>>>(hdr, np, s->d_status.as<uint8_t>(), s->d_areas.as<double>(),
+                                               o->category_count, 1, fb.as<uint32_t>(), lb);
+        L += 2;
+        FARM_CUDA(cudaStreamSynchronize(st));
+        fb.release();
+    }
+    FARM_CUDA(cudaGetLastError());
+    // errors
+    int *derr;
+    FARM_TRY(s->d_counters.ensure(64));
+    derr = s->d_counters.as<int>();
+    FARM_CUDA(cudaMemsetAsync(derr, 0, 4, st));
+    k_err_reduce<<<gb(np), 256, 0, st>>>(hdr, np, derr);
+    L++;
+    int herr = 0;
+    FARM_CUDA(cudaMemcpyAsync(&herr, derr, 4, cudaMemcpyDeviceToHost, st));
+    FARM_CUDA(cudaStreamSynchronize(st));
+    cpbuf.release();
+    ykb.release();
+    ypb.release();
+    yks.release();
+    yps.release();
+    s->tot_P = totP;
+    s->tot_status = totStatus;
+    s->tot_seq = totSeq;
+    if (launches) *launches = L;
+    if (herr) {
+        set_error("a polygon violated a condition the reference asserts on (see farm_raster_fetch err)");
+        return herr;
+    }
+    return FARM_OK;
+}
+
+}  // namespace farm
+
+extern "C" int farm_rasterize(farm_store *s, const farm_raster_opts *o) {
+    using namespace farm;
+    if (!s || !o || o->vpr <= 0) {
+        set_error("invalid arguments to farm_rasterize");
+        return FARM_EINVAL;
+    }
+    if (!(o->category_count == 4 || o->category_count == 16 || o->category_count == 256)) {
+        set_error("category_count must be 4, 16 or 256");
+        return FARM_EINVAL;
+    }
+    s->rasterized = false;
+    s->ropts = *o;
+    int launches = 0;
+    int rc = rasterize(s, o, &launches);
+    s->launches += (uint64_t)launches;
+    // with FARM_EASSERT the other polygons' rasters stay valid and inspectable;
+    // queries refuse to run on such a store
+    if (rc == FARM_OK || rc == FARM_EASSERT) s->rasterized = true;
+    s->raster_err = rc == FARM_EASSERT ? rc : 0;
+    return rc;
+}

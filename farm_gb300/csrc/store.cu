@@ -1,0 +1,305 @@
+// Store lifetime, ring upload and the C ABI plumbing (errors, device info,
+// raster inspection). Replaces the reference's cuda_create_buffer /
+// preprocess_for_gpu (src/cuda/preprocessing.cu:5-358): rings go to HBM once,
+// in a 64-bit-offset layout, and the store owns every device allocation.
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "common.cuh"
+
+namespace farm {
+
+static thread_local std::string g_error;
+
+void set_error(const std::string &msg) { g_error = msg; }
+
+int cuda_fail(cudaError_t e, const char *what) {
+    g_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return FARM_ECUDA;
+}
+
+int DevBuf::ensure(size_t bytes) {
+    if (bytes <= cap && p) return FARM_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = bytes < 256 ? 256 : bytes;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        p = nullptr;
+        set_error("device allocation of " + std::to_string(want) + " bytes failed");
+        return FARM_ENOMEM;
+    }
+    cap = want;
+    return FARM_OK;
+}
+
+void DevBuf::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+}
+
+int sm_count() {
+    static int n = 0;
+    static std::once_flag once;
+    std::call_once(once, []() {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    });
+    return n;
+}
+
+// Copy stored rings into the padded layout: per polygon the stored vertices,
+// then a copy of the first (the vertex the reference's decode appends,
+// vertex_sequence.cpp:206-219) and one more copy as the pad vertex read by the
+// whole-ring sequence of single-pixel polygons (Ideal.cpp:523-529).
+__global__ void k_pad_rings(const float2 *__restrict__ xy, const uint64_t *__restrict__ off, uint32_t npoly,
+                            uint64_t first_poly, float2 *__restrict__ ring) {
+    // off: this side's slice of the concatenated (global) vertex offsets;
+    // xy: this side's vertices, indexed from its own first vertex
+    uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    uint64_t base = off[0];
+    uint64_t total = off[npoly] - base;
+    for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < total; v += stride) {
+        uint64_t gv = v + base;
+        uint32_t p = find_segment(off, npoly, gv);
+        uint64_t gp = first_poly + p;
+        float2 q = xy[v];
+        ring[gv + 2 * gp] = q;
+        if (gv == off[p]) {
+            uint64_t end = off[p + 1] + 2 * gp;
+            ring[end] = q;
+            ring[end + 1] = q;
+        }
+    }
+}
+
+}  // namespace farm
+
+using namespace farm;
+
+farm::StoreView farm_store::view() const {
+    farm::StoreView v;
+    v.ring = d_ring.as<float2>();
+    v.hdr = d_hdr.as<PolyHdr>();
+    v.status = d_status.as<uint8_t>();
+    v.offset = d_offset.as<uint32_t>();
+    v.seq = d_seq.as<uint2>();
+    v.hoff = d_hoff.as<uint32_t>();
+    v.hnodes = d_hnodes.as<double>();
+    v.voff = d_voff.as<uint32_t>();
+    v.vnodes = d_vnodes.as<double>();
+    v.areas = d_areas.as<double>();
+    v.category_count = ropts.category_count ? ropts.category_count : 16;
+    return v;
+}
+
+extern "C" {
+
+const char *farm_last_error(void) { return g_error.c_str(); }
+
+int farm_device_info(int *ordinal, char *name, size_t name_len) {
+    int dev = 0;
+    FARM_CUDA(cudaGetDevice(&dev));
+    cudaDeviceProp prop;
+    FARM_CUDA(cudaGetDeviceProperties(&prop, dev));
+    if (ordinal) *ordinal = dev;
+    if (name && name_len) {
+        strncpy(name, prop.name, name_len - 1);
+        name[name_len - 1] = 0;
+    }
+    return FARM_OK;
+}
+
+int farm_store_create(farm_store **out) {
+    if (!out) {
+        set_error("null output pointer");
+        return FARM_EINVAL;
+    }
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        set_error("no CUDA device is available");
+        return FARM_ECUDA;
+    }
+    farm_store *s = new (std::nothrow) farm_store();
+    if (!s) {
+        set_error("host allocation failed");
+        return FARM_ENOMEM;
+    }
+    cudaGetDevice(&s->device);
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete s;
+        return cuda_fail(cudaGetLastError(), "cudaStreamCreate");
+    }
+    for (auto &ev : s->ev) cudaEventCreate(&ev);
+    *out = s;
+    return FARM_OK;
+}
+
+void farm_store_destroy(farm_store *s) {
+    if (!s) return;
+    cudaStreamSynchronize(s->stream);
+    DevBuf *bufs[] = {&s->d_xy_in, &s->d_off, &s->d_ring, &s->d_hdr, &s->d_status, &s->d_offset, &s->d_seq,
+                      &s->d_hoff, &s->d_hnodes, &s->d_voff, &s->d_vnodes, &s->d_areas, &s->cub_tmp,
+                      &s->d_pairs, &s->d_out, &s->d_counters};
+    for (DevBuf *b : bufs) b->release();
+    for (auto &b : s->s) b.release();
+    for (auto &ev : s->ev)
+        if (ev) cudaEventDestroy(ev);
+    cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+int farm_sync(farm_store *s) {
+    if (!s) return FARM_EINVAL;
+    FARM_CUDA(cudaStreamSynchronize(s->stream));
+    return FARM_OK;
+}
+
+int farm_store_load(farm_store *s, int side, uint64_t n, const uint64_t *off, const float *xy, int mem) {
+    if (!s || side < 0 || side > 1 || !off || (n && !xy)) {
+        set_error("invalid arguments to farm_store_load");
+        return FARM_EINVAL;
+    }
+    if (n > 0x7FFFFFFFull) {
+        set_error("more than 2^31 polygons on one side");
+        return FARM_EOVERFLOW;
+    }
+    if (side == 1 && s->n_side[0] == 0) {
+        set_error("load the source side (0) before the target side (1)");
+        return FARM_EINVAL;
+    }
+    std::vector<uint64_t> h(n + 1);
+    if (mem == FARM_MEM_DEVICE)
+        FARM_CUDA(cudaMemcpy(h.data(), off, (n + 1) * 8, cudaMemcpyDeviceToHost));
+    else
+        memcpy(h.data(), off, (n + 1) * 8);
+    for (uint64_t k = 0; k < n; k++) {
+        if (h[k + 1] < h[k] + 2) {
+            set_error("polygon " + std::to_string(k) + " has fewer than 2 stored vertices");
+            return FARM_EINVAL;
+        }
+        if (h[k + 1] - h[k] > 0x3FFFFFFFull) {
+            set_error("polygon " + std::to_string(k) + " exceeds 2^30 vertices");
+            return FARM_EOVERFLOW;
+        }
+    }
+    uint64_t o0 = h[0];
+    for (auto &v : h) v -= o0;
+    s->rasterized = false;
+    if (side == 0) {  // a new source side drops any target side
+        s->n_side[1] = 0;
+        s->h_off[1].clear();
+    }
+    s->h_off[side] = h;
+    s->n_side[side] = n;
+    uint64_t n0 = s->n_side[0], n1 = s->n_side[1];
+    uint64_t t0 = s->h_off[0][n0], t1 = n1 ? s->h_off[1][n1] : 0;
+    std::vector<uint64_t> cat(n0 + n1 + 1);
+    for (uint64_t k = 0; k <= n0; k++) cat[k] = s->h_off[0][k];
+    for (uint64_t k = 1; k <= n1; k++) cat[n0 + k] = t0 + s->h_off[1][k];
+    uint64_t total = t0 + t1;
+    // padded layout: polygon p's ring starts at cat[p] + 2p
+    DevBuf nr;
+    FARM_TRY(nr.ensure((total + 2 * (n0 + n1)) * sizeof(float2) + 64));
+    if (side == 1 && s->d_ring.p)
+        FARM_CUDA(cudaMemcpyAsync(nr.p, s->d_ring.p, (t0 + 2 * n0) * sizeof(float2), cudaMemcpyDeviceToDevice,
+                                  s->stream));
+    uint64_t side_total = side == 0 ? t0 : t1;
+    const float2 *src;
+    if (mem == FARM_MEM_DEVICE) {
+        src = reinterpret_cast<const float2 *>(xy) + o0;
+    } else {
+        FARM_TRY(s->d_xy_in.ensure(side_total * sizeof(float2) + 16));
+        FARM_CUDA(cudaMemcpyAsync(s->d_xy_in.p, xy + 2 * o0, side_total * sizeof(float2), cudaMemcpyHostToDevice,
+                                  s->stream));
+        src = s->d_xy_in.as<float2>();
+    }
+    FARM_TRY(s->d_off.ensure((n0 + n1 + 1) * 8));
+    FARM_CUDA(cudaMemcpyAsync(s->d_off.p, cat.data(), (n0 + n1 + 1) * 8, cudaMemcpyHostToDevice, s->stream));
+    uint64_t first_poly = side == 0 ? 0 : n0;
+    if (n) {
+        unsigned blocks = grid_for(side_total, 256);
+        unsigned cap = 32u * (unsigned)sm_count();
+        if (blocks > cap) blocks = cap;
+        k_pad_rings<<<blocks, 256, 0, s->stream>>>(src, s->d_off.as<uint64_t>() + first_poly, (uint32_t)n,
+                                                   first_poly, nr.as<float2>());
+        FARM_CUDA(cudaGetLastError());
+        s->launches++;
+    }
+    FARM_CUDA(cudaStreamSynchronize(s->stream));  // the host offset vector dies here
+    s->d_ring.release();
+    s->d_ring = nr;
+    nr.p = nullptr;
+    s->n_poly = n0 + n1;
+    s->n_edges = total;
+    return FARM_OK;
+}
+
+int farm_raster_fetch(farm_store *s, int side, uint64_t index, farm_raster_view *v, uint8_t *status,
+                      uint32_t *offset, uint32_t *seq, uint32_t *hoff, double *hnodes, uint32_t *voff, double *vnodes,
+                      double *areas, double *layer_info) {
+    if (!s || !v || side < 0 || side > 1 || index >= s->n_side[side]) {
+        set_error("invalid arguments to farm_raster_fetch");
+        return FARM_EINVAL;
+    }
+    if (!s->rasterized) {
+        set_error("store is not rasterized");
+        return FARM_EINVAL;
+    }
+    uint64_t p = (side == 0 ? 0 : s->n_side[0]) + index;
+    PolyHdr h;
+    FARM_CUDA(cudaMemcpy(&h, s->d_hdr.as<PolyHdr>() + p, sizeof h, cudaMemcpyDeviceToHost));
+    memcpy(v->mbr, h.mbr, sizeof h.mbr);
+    v->dimx = h.dimx;
+    v->dimy = h.dimy;
+    v->step_x = h.step_x;
+    v->step_y = h.step_y;
+    v->nv = h.nv;
+    v->status_size = h.status_size;
+    v->n_seq = h.n_seq;
+    v->n_hnodes = h.n_hnodes;
+    v->n_vnodes = h.n_vnodes;
+    v->num_layers = h.num_layers;
+    v->err = h.err;
+    if (status) FARM_CUDA(cudaMemcpy(status, s->d_status.as<uint8_t>() + h.st, h.status_size, cudaMemcpyDeviceToHost));
+    if (offset)
+        FARM_CUDA(cudaMemcpy(offset, s->d_offset.as<uint32_t>() + h.off, 4ull * (h.P + 1), cudaMemcpyDeviceToHost));
+    if (seq) FARM_CUDA(cudaMemcpy(seq, s->d_seq.as<uint2>() + h.seq, 8ull * h.n_seq, cudaMemcpyDeviceToHost));
+    if (hoff)
+        FARM_CUDA(cudaMemcpy(hoff, s->d_hoff.as<uint32_t>() + h.hline, 4ull * (h.dimy + 2), cudaMemcpyDeviceToHost));
+    if (hnodes && h.n_hnodes)
+        FARM_CUDA(cudaMemcpy(hnodes, s->d_hnodes.as<double>() + h.hnode, 8ull * h.n_hnodes, cudaMemcpyDeviceToHost));
+    if (voff)
+        FARM_CUDA(cudaMemcpy(voff, s->d_voff.as<uint32_t>() + h.vline, 4ull * (h.dimx + 2), cudaMemcpyDeviceToHost));
+    if (vnodes && h.n_vnodes)
+        FARM_CUDA(cudaMemcpy(vnodes, s->d_vnodes.as<double>() + h.vnode, 8ull * h.n_vnodes, cudaMemcpyDeviceToHost));
+    if (areas) FARM_CUDA(cudaMemcpy(areas, s->d_areas.as<double>() + h.pix, 8ull * h.P, cudaMemcpyDeviceToHost));
+    if (layer_info) {
+        for (uint32_t i = 0; i < h.num_layers; i++) {
+            LayerGeom g;
+            layer_geom(h, i, g);
+            double *o = layer_info + 7 * i;
+            o[0] = g.mbr[0];
+            o[1] = g.mbr[1];
+            o[2] = g.mbr[2];
+            o[3] = g.mbr[3];
+            o[4] = g.step_x;
+            o[5] = g.step_y;
+            o[6] = (double)g.dimx * 65536.0 * 65536.0 + (double)g.dimy;  // packed dims
+            (void)o;
+        }
+    }
+    return FARM_OK;
+}
+
+}  // extern "C"

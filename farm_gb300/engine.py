@@ -1,0 +1,194 @@
+"""Host-side mirror of the reference's query interface for the polygon-join path.
+
+The reference's GPU entry points take a ``query_context`` (src/include/Ideal.h:205-213);
+here a :class:`Store` owns the device-resident polygons and rasters and each
+query mirrors one of them:
+
+==========================  ==================================================
+reference                   here
+==========================  ==================================================
+preprocess + rasterization  ``Store.load(...)`` + ``Store.rasterize(vpr, ...)``
+``Ideal::intersect``         ``Store.intersect(pairs)``
+``Ideal::within``            ``Store.within(pairs, distance)``
+``Ideal::intersection``      ``Store.intersection_area(pairs)``
+==========================  ==================================================
+
+Every call goes through the C ABI of ``libfarm_gpu.so`` (include/farm_gpu.h);
+there is no CPU path behind it. Pair arrays are ``uint32 [n, 2]`` of
+(source index, target index). Arrays may be numpy (host) or torch CUDA tensors
+(device-resident; no copy).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native
+from ._gpu_sig import RasterOpts, RasterView, Stats
+from ._native import check_gpu, gpu
+
+MODE_EXACT = 0
+MODE_LEARNED = 2
+MEM_HOST = 0
+MEM_DEVICE = 1
+
+
+def _addr(a):
+    """(pointer, mem) of a numpy array or a CUDA tensor."""
+    if isinstance(a, np.ndarray):
+        if not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("array must be C-contiguous")
+        return C.c_void_p(a.ctypes.data), MEM_HOST
+    if hasattr(a, "data_ptr") and getattr(a, "is_cuda", False):
+        if not a.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return C.c_void_p(a.data_ptr()), MEM_DEVICE
+    raise TypeError(f"unsupported array type {type(a)!r}")
+
+
+def stats_dict(st: Stats) -> dict:
+    return {"pairs": st.pairs, "found": st.found, "in_hits": st.in_hits, "border_pairs": st.border_pairs,
+            "segment_tests": st.segment_tests, "fp64_rechecks": st.fp64_rechecks, "ms_total": st.ms_total,
+            "ms_stage": list(st.ms_stage), "kernel_launches": st.kernel_launches}
+
+
+class Store:
+    """Device-resident source/target polygon tables with their rasters."""
+
+    def __init__(self):
+        self._lib = gpu()
+        self._h = C.c_void_p()
+        check_gpu(self._lib.farm_store_create(C.byref(self._h)))
+        self.n_source = 0
+        self.n_target = 0
+        self.last_stats: dict = {}
+
+    def close(self):
+        if self._h:
+            self._lib.farm_store_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def load(self, side: int, off, xy) -> None:
+        """Load rings (host layout, closing vertex included) for side 0 (source) or 1 (target)."""
+        po, mo = _addr(off)
+        px, mx = _addr(xy)
+        if mo != mx:
+            raise ValueError("offsets and vertices must live in the same memory")
+        n = (off.shape[0] if hasattr(off, "shape") else len(off)) - 1
+        check_gpu(self._lib.farm_store_load(self._h, side, n, po, px, mo))
+        if side == 0:
+            self.n_source, self.n_target = n, 0
+        else:
+            self.n_target = n
+
+    def load_sets(self, source, target=None) -> None:
+        self.load(0, source.off, source.xy)
+        if target is not None:
+            self.load(1, target.off, target.xy)
+
+    def rasterize(self, vpr: int = 10, category_count: int = 16, hierarchy: bool = False) -> None:
+        o = RasterOpts(vpr, category_count, int(hierarchy), 0)
+        check_gpu(self._lib.farm_rasterize(self._h, C.byref(o)))
+
+    def intersect(self, pairs, mode: int = MODE_EXACT, out=None):
+        """Per-pair 0/1 results (same memory kind as ``pairs``) and the found count."""
+        n = pairs.shape[0]
+        pp, mem = _addr(pairs)
+        if out is None:
+            out = np.zeros(n, dtype=np.uint8) if mem == MEM_HOST else _torch_empty_u8(n, pairs.device)
+        po, mo = _addr(out)
+        if mo != mem:
+            raise ValueError("pairs and out must live in the same memory")
+        found = C.c_uint64(0)
+        st = Stats()
+        check_gpu(self._lib.farm_intersect(self._h, pp, n, mode, mem, po, C.byref(found), C.byref(st)))
+        self.last_stats = stats_dict(st)
+        return out, found.value
+
+    def within(self, pairs, distance: float = 10.0, geography: bool = True, self_join: bool = False, out=None):
+        n = pairs.shape[0]
+        pp, mem = _addr(pairs)
+        if out is None:
+            out = np.zeros(n, dtype=np.uint8) if mem == MEM_HOST else _torch_empty_u8(n, pairs.device)
+        po, mo = _addr(out)
+        found = C.c_uint64(0)
+        st = Stats()
+        check_gpu(self._lib.farm_within(self._h, pp, n, float(distance), int(geography), int(self_join), mem, po,
+                                        C.byref(found), C.byref(st)))
+        self.last_stats = stats_dict(st)
+        return out, found.value
+
+    def intersection_area(self, pairs, out=None):
+        n = pairs.shape[0]
+        pp, mem = _addr(pairs)
+        if out is None:
+            out = np.zeros(n, dtype=np.float64) if mem == MEM_HOST else _torch_empty_f64(n, pairs.device)
+        po, _ = _addr(out)
+        st = Stats()
+        check_gpu(self._lib.farm_intersection_area(self._h, pp, n, mem, po, C.byref(st)))
+        self.last_stats = stats_dict(st)
+        return out
+
+    def fetch_raster(self, side: int, index: int) -> dict:
+        """One polygon's raster arrays (for parity tests)."""
+        v = RasterView()
+        lib = self._lib
+        check_gpu(lib.farm_raster_fetch(self._h, side, index, C.byref(v), None, None, None, None, None, None, None,
+                                        None, None))
+        P = v.dimx * v.dimy
+        status = np.zeros(v.status_size, np.uint8)
+        offset = np.zeros(P + 1, np.uint32)
+        seq = np.zeros((v.n_seq, 2), np.uint32)
+        hoff = np.zeros(v.dimy + 2, np.uint32)
+        hnodes = np.zeros(v.n_hnodes, np.float64)
+        voff = np.zeros(v.dimx + 2, np.uint32)
+        vnodes = np.zeros(v.n_vnodes, np.float64)
+        areas = np.zeros(P, np.float64)
+        layers = np.zeros((max(v.num_layers, 1), 7), np.float64)
+
+        def p(a, t):
+            return a.ctypes.data_as(C.POINTER(t))
+
+        check_gpu(lib.farm_raster_fetch(self._h, side, index, C.byref(v), p(status, C.c_uint8),
+                                        p(offset, C.c_uint32), p(seq, C.c_uint32), p(hoff, C.c_uint32),
+                                        p(hnodes, C.c_double), p(voff, C.c_uint32), p(vnodes, C.c_double),
+                                        p(areas, C.c_double), p(layers, C.c_double)))
+        out_layers = []
+        for i in range(v.num_layers):
+            L = layers[i]
+            packed = int(L[6])
+            out_layers.append((tuple(L[:4]), packed >> 32, packed & 0xFFFFFFFF, float(L[4]), float(L[5])))
+        return {"mbr": np.array(v.mbr[:]), "dimx": v.dimx, "dimy": v.dimy, "step": np.array([v.step_x, v.step_y]),
+                "nv": v.nv, "status": status, "offset": offset, "seq": seq, "hoff": hoff, "hnodes": hnodes,
+                "voff": voff, "vnodes": vnodes, "areas": areas, "num_layers": v.num_layers, "layers": out_layers,
+                "err": v.err}
+
+
+def _torch_empty_u8(n, device):
+    import torch
+    return torch.empty(n, dtype=torch.uint8, device=device)
+
+
+def _torch_empty_f64(n, device):
+    import torch
+    return torch.empty(n, dtype=torch.float64, device=device)
+
+
+def device_name() -> str:
+    buf = C.create_string_buffer(256)
+    ordn = C.c_int(0)
+    check_gpu(gpu().farm_device_info(C.byref(ordn), buf, 256))
+    return buf.value.decode()

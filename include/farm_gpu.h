@@ -1,0 +1,142 @@
+/*
+ * farm_gpu.h — C ABI of the GB300 (sm_103a) engine for FARM's polygon-join
+ * hot path. No CUDA or torch types: plain pointers, sizes and status codes.
+ *
+ * It replaces the reference's GPU offload entry points (src/include/Ideal.h:205-213):
+ *   cuda_create_buffer / preprocess_for_gpu  -> farm_store_create + farm_store_load + farm_rasterize
+ *   cuda_intersect                           -> farm_intersect
+ *   cuda_within_polygon                      -> farm_within
+ *   cuda_intersection                        -> farm_intersection_area
+ *   ResetDevice                              -> (none: results are written to caller buffers)
+ * and, for the CPU path it must agree with, Ideal::rasterization / Ideal::intersect /
+ * Ideal::within (src/geometry/Ideal.cpp:936, 1329, 2475).
+ *
+ * Semantics differ from the reference's god-object API in three deliberate ways:
+ * pair ids are (source index, target index) into two separate polygon tables
+ * (as intersect_cpu.cpp:45-50 uses them); results are written to a caller
+ * buffer (one byte per pair) besides the count; errors are returned, never
+ * exit()ed. Every call is thread-compatible per store (one store per host thread).
+ */
+#ifndef FARM_GPU_H
+#define FARM_GPU_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes (shared with farm_host.h). */
+#ifndef FARM_OK
+#define FARM_OK 0
+#define FARM_EINVAL (-1)
+#define FARM_EIO (-2)
+#define FARM_ENOMEM (-3)
+#define FARM_EOVERFLOW (-4)
+#define FARM_ECUDA (-5)
+#define FARM_ETIMEOUT (-6)
+#define FARM_EFORMAT (-7)
+#define FARM_EINTERNAL (-8)
+#endif
+/* a condition the reference asserts on (and aborts) was met while rasterizing */
+#define FARM_EASSERT (-10)
+
+typedef struct farm_store farm_store;
+
+/* Query modes for farm_intersect. */
+#define FARM_MODE_EXACT 0   /* the reference's decision procedure, bit-exact */
+#define FARM_MODE_LEARNED 2 /* MLP scorer; abstentions refined exactly */
+
+/* Pointer locations for pair lists and result buffers. */
+#define FARM_MEM_HOST 0
+#define FARM_MEM_DEVICE 1
+
+typedef struct farm_raster_opts {
+    int32_t vpr;            /* -v: vertices per pixel (reference default 10) */
+    int32_t category_count; /* -w: fill classes 4/16/256 (reference fixes 16) */
+    int32_t hierarchy;      /* -h: layered rasters (needed by within) */
+    int32_t reserved;
+} farm_raster_opts;
+
+typedef struct farm_stats {
+    uint64_t pairs;          /* pairs decided */
+    uint64_t found;          /* pairs whose result is true */
+    uint64_t in_hits;        /* decided by an IN pixel overlap (intersect) */
+    uint64_t border_pairs;   /* BORDER x BORDER pixel pairs examined */
+    uint64_t segment_tests;  /* segment-pair (or point-segment) evaluations */
+    uint64_t fp64_rechecks;  /* within: distances re-evaluated in FP64 */
+    double ms_total;         /* device time of the call (CUDA events) */
+    double ms_stage[4];      /* raster, filter, refine, other */
+    int32_t kernel_launches; /* engine kernels launched by the call */
+    int32_t reserved;
+} farm_stats;
+
+const char *farm_last_error(void);
+/* Device ordinal and name the library runs on; returns FARM_ECUDA without a GPU. */
+int farm_device_info(int *ordinal, char *name, size_t name_len);
+
+int farm_store_create(farm_store **out);
+void farm_store_destroy(farm_store *s);
+
+/* Load one side's rings (side 0 = source, 1 = target). Rings in the host
+ * layout of farm_host.h: off[n+1] (vertex offsets), xy float32 pairs with the
+ * closing copy included, exactly as a .dt record stores them. mem says where
+ * off/xy live (FARM_MEM_HOST or FARM_MEM_DEVICE). Replaces both sides' data.
+ * For a self-join load side 0 only and pass target_is_source to the queries. */
+int farm_store_load(farm_store *s, int side, uint64_t n, const uint64_t *off, const float *xy, int mem);
+
+/* Rasterize every loaded polygon (reference: preprocessing.cpp:4-29,
+ * Ideal.cpp:920-955). Must precede the queries. */
+int farm_rasterize(farm_store *s, const farm_raster_opts *o);
+
+/* Decide Ideal::intersect(source[p.s], target[p.t]) for n pairs. pairs: 2n
+ * uint32 (s, t). out: n bytes (0/1), may be NULL. found: count of true. */
+int farm_intersect(farm_store *s, const uint32_t *pairs, uint64_t n, int mode, int mem, uint8_t *out,
+                   uint64_t *found, farm_stats *st);
+
+/* Decide Ideal::within(source[p.s], target[p.t]) (hierarchical rasters required).
+ * distance in km with geography (the reference: 10 km, degree coordinates),
+ * in coordinate units without (planar mode for projected coordinates). */
+int farm_within(farm_store *s, const uint32_t *pairs, uint64_t n, double distance, int geography,
+                int target_is_source, int mem, uint8_t *out, uint64_t *found, farm_stats *st);
+
+/* FP64 area of source[p.s] ∩ target[p.t] for n pairs (out: n doubles). The
+ * reference stops before computing it (Ideal.cpp:1683); this is the project's
+ * boundary-integral formulation. */
+int farm_intersection_area(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, double *out,
+                           farm_stats *st);
+
+/* Copy one rasterized polygon back for inspection (tests): sizes first with
+ * NULL buffers, then the arrays. side/index select the polygon. */
+typedef struct farm_raster_view {
+    double mbr[4];
+    int32_t dimx, dimy;
+    double step_x, step_y;
+    uint32_t nv, status_size, n_seq, n_hnodes, n_vnodes, num_layers;
+    int32_t err;
+    uint32_t reserved;
+} farm_raster_view;
+int farm_raster_fetch(farm_store *s, int side, uint64_t index, farm_raster_view *v, uint8_t *status,
+                      uint32_t *offset, uint32_t *seq, uint32_t *hoff, double *hnodes, uint32_t *voff,
+                      double *vnodes, double *areas, double *layer_info /* 7 doubles per layer */);
+
+/* Wait for outstanding work of the store's stream. */
+int farm_sync(farm_store *s);
+
+/* CUDA-event timing on the store's stream (8 slots): record, then elapsed ms a -> b. */
+int farm_event_record(farm_store *s, int slot);
+int farm_event_elapsed(farm_store *s, int a, int b, double *ms);
+/* Engine kernels launched through this store so far. */
+uint64_t farm_store_launches(farm_store *s);
+
+/* Seeded star polygons generated on the device (benchmark inputs): d_off
+ * (count + 1 entries, device memory) holds the offsets of farm_gen_counts()'s
+ * counts, d_xy receives the rings. Same recipe as farm_gen_fill() on the host;
+ * the device libm may round a coordinate differently in its last bit. */
+int farm_gen_device(double dom_lo, double dom_hi, double r_lo, double r_hi, double sigma, uint64_t seed,
+                    uint64_t first, uint64_t count, const uint64_t *d_off, float *d_xy);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

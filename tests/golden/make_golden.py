@@ -1,0 +1,112 @@
+"""Generate the golden fixtures from the reference's own CPU code.
+
+Runs where the reference sources are present: it builds oracle/_ref (the
+reference's unmodified CPU sources + the harness, see oracle/ref/Makefile),
+generates seeded star polygons with the engine's generator, writes them as .dt
+files, and records what the reference computes for them:
+
+* ``<case>.rast.bin.gz`` — every polygon's raster (status, edge-sequence CSR,
+  grid-line nodes, FP64 fill areas, hierarchy layers), dumped by
+  ``ref_harness raster``;
+* ``<case>.pairs.bin.gz`` — every MBR-candidate pair with the reference's
+  decision, from ``ref_harness intersect|within``;
+* ``degree_table.json`` — the reference's longitude degree table (util.h:73) as
+  a SHA-256 of its printed values, which the regenerated table must match.
+
+The .dt inputs are committed next to the outputs, so the tests never need the
+reference or the generator's libm to reproduce them. Usage:
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import gzip
+import hashlib
+import json
+import re
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+sys.path.insert(0, str(ROOT))
+
+from farm_gb300 import build  # noqa: E402
+from farm_gb300.polygons import StarParams, generate  # noqa: E402
+
+REF_SRC = build.REF_SRC
+
+# (name, params, seed, count, vpr, hierarchy)
+RASTER_CASES = [
+    ("r_cfg1_v10", StarParams(dom_hi=20.0), 101, 80, 10, 0),
+    ("r_cfg1_v4_h", StarParams(dom_hi=20.0), 102, 60, 4, 1),
+    ("r_cfg1_v64", StarParams(dom_hi=20.0), 103, 60, 64, 0),
+    ("r_small_v1", StarParams(dom_hi=5.0, r_lo=0.01, r_hi=0.5, n_lo=16, n_hi=200), 104, 60, 1, 1),
+]
+# (name, params, seed, n_source, n_target (0 = self-join), vpr, mode)
+PAIR_CASES = [
+    ("p_intersect_v10", StarParams(dom_hi=20.0), 201, 60, 240, 10, "intersect"),
+    ("p_intersect_v4", StarParams(dom_hi=20.0), 202, 50, 200, 4, "intersect"),
+    ("p_within_v10", StarParams(dom_hi=20.0), 203, 260, 0, 10, "within"),
+    ("p_within_v64", StarParams(dom_hi=30.0), 204, 260, 0, 64, "within"),
+]
+
+
+def gz(src: Path, dst: Path) -> None:
+    with open(src, "rb") as f, gzip.open(dst, "wb", compresslevel=9) as g:
+        shutil.copyfileobj(f, g)
+
+
+def sha(p: Path) -> str:
+    return hashlib.sha256(p.read_bytes()).hexdigest()
+
+
+def main() -> None:
+    harness = build.build_ref()
+    if harness is None:
+        raise SystemExit(f"reference sources not found at {REF_SRC}")
+    build.build_host()
+    manifest = {"raster": [], "pairs": []}
+    tmp = Path("/tmp/farm_golden")
+    tmp.mkdir(exist_ok=True)
+    for name, prm, seed, n, vpr, hier in RASTER_CASES:
+        ps = generate(prm, seed, n)
+        dt = HERE / f"{name}.dt"
+        ps.write_dt(str(dt))
+        out = tmp / f"{name}.rast.bin"
+        subprocess.run([str(harness), "raster", str(dt), str(vpr), str(hier), str(out)], check=True,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL, env={"FARM_REF_THREADS": "4"})
+        gz(out, HERE / f"{name}.rast.bin.gz")
+        manifest["raster"].append({"name": name, "vpr": vpr, "hierarchy": hier, "seed": seed, "count": n,
+                                   "params": prm.__dict__, "dt_sha256": sha(dt)})
+    for name, prm, seed, ns, nt, vpr, mode in PAIR_CASES:
+        S = generate(prm, seed, ns)
+        sdt = HERE / f"{name}_S.dt"
+        S.write_dt(str(sdt))
+        if nt:
+            T = generate(prm, seed + 5000, nt)
+            tdt = HERE / f"{name}_T.dt"
+            T.write_dt(str(tdt))
+            targ = str(tdt)
+        else:
+            targ = "-"
+        out = tmp / f"{name}.pairs.bin"
+        subprocess.run([str(harness), mode, str(sdt), targ, str(vpr), str(out)], check=True,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL, env={"FARM_REF_THREADS": "4"})
+        gz(out, HERE / f"{name}.pairs.bin.gz")
+        manifest["pairs"].append({"name": name, "mode": mode, "vpr": vpr, "seed": seed, "n_source": ns,
+                                  "n_target": nt, "self_join": nt == 0, "params": prm.__dict__})
+    # the reference's longitude table, as printed in util.h
+    util = (REF_SRC / "include" / "util.h").read_text()
+    m = re.search(r"degree_per_kilometer_longitude_arr\[\] = \{([^}]*)\}", util)
+    vals = [v.strip() for v in m.group(1).split(",")]
+    manifest["degree_table"] = {"count": len(vals), "sha256_of_6_decimal_text": hashlib.sha256(
+        ",".join(vals).encode()).hexdigest()}
+    (HERE / "manifest.json").write_text(json.dumps(manifest, indent=1))
+    print("wrote", len(RASTER_CASES), "raster and", len(PAIR_CASES), "pair fixtures")
+
+
+if __name__ == "__main__":
+    main()

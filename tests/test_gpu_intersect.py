@@ -1,0 +1,61 @@
+"""GPU intersect (stages b + c) gives the reference's pair set, bit for bit."""
+import numpy as np
+import pytest
+
+from fixtures import manifest, pair_case
+from farm_gb300 import polygons as P
+from farm_gb300.engine import Store
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+M = manifest()
+
+
+def run(S, T, pairs, vpr, cc=16):
+    st = Store()
+    st.load_sets(S, T)
+    st.rasterize(vpr=vpr, category_count=cc)
+    out, found = st.intersect(np.ascontiguousarray(pairs, dtype=np.uint32))
+    stats = st.last_stats
+    st.close()
+    return out, found, stats
+
+
+@pytest.mark.parametrize("case", [c for c in M["pairs"] if c["mode"] == "intersect"],
+                         ids=[c["name"] for c in M["pairs"] if c["mode"] == "intersect"])
+def test_gpu_intersect_matches_reference_fixture(gpu_lib, case):
+    S, T, ref = pair_case(case)
+    pairs = ref[:, :2].astype(np.uint32)
+    out, found, _ = run(S, T, pairs, case["vpr"])
+    assert np.array_equal(out.astype(np.int64), ref[:, 2])
+    assert found == int(ref[:, 2].sum())
+
+
+@pytest.mark.parametrize("vpr,cc,seed", [(10, 16, 11), (4, 16, 12), (64, 4, 13), (1, 256, 14)])
+def test_gpu_intersect_matches_oracle(gpu_lib, vpr, cc, seed):
+    prm = P.StarParams(dom_hi=25.0, n_hi=1500)
+    S, T = P.generate(prm, seed, 150), P.generate(prm, seed + 100, 500)
+    pairs = P.mbr_join(S.mbrs(), T.mbrs())
+    out, found, stats = run(S, T, pairs, vpr, cc)
+    RS, RT = O.rasterize_set(S, vpr), O.rasterize_set(T, vpr)
+    exp = np.array([O.intersect(RS[s], RT[t]) for s, t in pairs], np.uint8)
+    assert np.array_equal(out, exp), f"{int((out != exp).sum())} of {len(exp)} differ"
+    assert stats["pairs"] == len(pairs)
+
+
+def test_gpu_intersect_edge_cases(gpu_lib):
+    sq = np.array([[0, 0], [2, 0], [2, 2], [0, 2], [0, 0]], np.float32)
+    rings_s = [sq, sq + 5, sq * 0.25 + 0.8]
+    rings_t = [sq, sq + np.float32(1), sq + np.float32(2), sq * 0.1 + 0.9, sq + 5.5]
+    mk = lambda rs: P.PolygonSet(np.concatenate([[0], np.cumsum([len(r) for r in rs])]).astype(np.uint64),
+                                 np.ascontiguousarray(np.concatenate(rs), dtype=np.float32))
+    S, T = mk(rings_s), mk(rings_t)
+    pairs = np.array([[s, t] for s in range(S.n) for t in range(T.n)], np.uint32)
+    for vpr in (1, 2, 10):
+        out, found, _ = run(S, T, pairs, vpr)
+        RS, RT = O.rasterize_set(S, vpr), O.rasterize_set(T, vpr)
+        exp = np.array([O.intersect(RS[s], RT[t]) for s, t in pairs], np.uint8)
+        assert np.array_equal(out, exp), vpr
+    # empty pair list
+    out, found, _ = run(S, T, np.zeros((0, 2), np.uint32), 10)
+    assert found == 0 and len(out) == 0
