@@ -1,0 +1,410 @@
+"""Benchmark of the polygon-join hot path: exact intersect pairs/sec on one GB300.
+
+Workload (BASELINE configuration 2): seeded star polygons, 100,000 sources x
+1,000,000 targets, vertex count log-uniform 16..100,000, mean radius
+log-uniform 0.05..2.0, per-vertex radius x lognormal(0, 0.3); the domain side
+is calibrated so the MBR join yields ~20M candidate pairs. The job runs in
+target batches (all sources + 1/B of the targets, ~20M/B candidates each): one
+"step" is one batch through the whole hot path — ring upload into the store's
+layout, rasterization of every polygon of the batch (stage a), pixel-pair
+filter + border refinement of every candidate (stages b, c), result bytes.
+Inputs are GBs (far larger than the 129 MB L2), so no L2 flush is needed.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun each rank takes its own target batches (weak scaling, no
+collective on the data path); value = all ranks' pairs / max rank time.
+--impl reference times the reference's CPU algorithm (the oracle port under
+oracle/, all host cores) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "polygon-pair tests/sec on 1 GB300: exact vs learned-approx at 99.9% P/R"
+UNIT = "pairs/s"
+
+# configuration 2
+N_SRC, N_TGT = 100_000, 1_000_000
+TARGET_PAIRS = 20_000_000
+
+
+def star_params(dom_hi):
+    from farm_gb300.polygons import StarParams
+    return StarParams(dom_lo=0.0, dom_hi=dom_hi, r_lo=0.05, r_hi=2.0, n_lo=16, n_hi=100_000, sigma=0.3)
+
+
+def calibrate_domain(seed: int) -> float:
+    """Domain side L giving ~20M expected MBR-overlap pairs for 100k x 1M polygons.
+
+    For centres uniform in [0, L]^2, P(overlap) ~ E[(w_s + w_t)(h_s + h_t)] / L^2;
+    the expectation is estimated from the MBRs of 4,000 polygons per side of a
+    unit-domain sample (sizes do not depend on the domain)."""
+    from farm_gb300 import polygons as P
+    prm = star_params(1.0)
+    prm.n_hi = 100_000
+    a = P.generate(prm, seed + 7, 4000).mbrs()
+    b = P.generate(prm, seed + 8, 4000).mbrs()
+    wa, ha = a[:, 2] - a[:, 0], a[:, 3] - a[:, 1]
+    wb, hb = b[:, 2] - b[:, 0], b[:, 3] - b[:, 1]
+    e = float(np.mean((wa[:, None] + wb[None, :2000]) * (ha[:, None] + hb[None, :2000])))
+    return math.sqrt(N_SRC * N_TGT * e / TARGET_PAIRS)
+
+
+class Clocks:
+    """Samples nvidia-smi clocks/throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def log(msg: str) -> None:
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
+def build_workload(seed: int, batch: int, n_batches: int, vpr: int):
+    """Host (pinned) rings of all sources and of target batch `batch`, and its candidates."""
+    import torch
+    from farm_gb300 import polygons as P
+
+    L = calibrate_domain(seed)
+    prm = star_params(L)
+    tb = N_TGT // n_batches
+    t_first = batch * tb
+
+    def gen_pinned(seed_, count, first):
+        from farm_gb300._native import check_host, host, ptr, u32p, u64p, f32p
+        import ctypes as C
+        gp = prm.c()
+        counts = np.zeros(count, np.uint32)
+        check_host(host().farm_gen_counts(C.byref(gp), seed_, first, count, ptr(counts, u32p)))
+        off = torch.zeros(count + 1, dtype=torch.int64).pin_memory()
+        offn = off.numpy().view(np.uint64)
+        np.cumsum(counts, dtype=np.uint64, out=offn[1:])
+        xy = torch.empty((int(offn[-1]), 2), dtype=torch.float32).pin_memory()
+        xyn = xy.numpy()
+        check_host(host().farm_gen_fill(C.byref(gp), seed_, first, count, ptr(offn, u64p), ptr(xyn, f32p), 0))
+        return P.PolygonSet(offn, xyn), off, xy
+
+    log(f"domain side {L:.2f}")
+    S, S_off_t, S_xy_t = gen_pinned(seed, N_SRC, 0)
+    log(f"sources generated: {S.total} vertices")
+    T, T_off_t, T_xy_t = gen_pinned(seed + 1, tb, t_first)
+    log(f"targets generated: {T.total} vertices")
+    ms, mt = S.mbrs(), T.mbrs()
+    pairs = P.mbr_join(ms, mt)
+    log(f"candidates: {len(pairs)}")
+    return {"L": L, "S": S, "T": T, "pairs": pairs, "tb": tb, "t_first": t_first,
+            "pinned": (S_off_t, S_xy_t, T_off_t, T_xy_t)}
+
+
+def filter_bytes(stats: dict, n_pairs: int, bits: int) -> float:
+    """Algorithmic bytes of the filter+refine kernel for one launch: per pair 8
+    (pair ids) + 2 x 64 (raster headers) + w/8 per source window pixel and per
+    target pixel visited + 1/8 (result bit)."""
+    return n_pairs * (8 + 128 + 0.125) + bits / 8.0 * (stats["src_window_pixels"] + stats["tgt_window_pixels"])
+
+
+def run_ours(args) -> dict:
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from farm_gb300.engine import Store
+
+    n_batches = args.batches
+    W = build_workload(args.seed, rank % n_batches, n_batches, args.vpr)
+    S, T, pairs = W["S"], W["T"], W["pairs"]
+    S_off_t, S_xy_t, T_off_t, T_xy_t = W["pinned"]
+    dev = torch.device("cuda", local)
+    d = {k: v.to(dev) for k, v in (("so", S_off_t), ("sx", S_xy_t), ("to", T_off_t), ("tx", T_xy_t))}
+    d_pairs = torch.from_numpy(pairs.view(np.int32)).to(dev)
+    d_out = torch.empty(len(pairs), dtype=torch.uint8, device=dev)
+    h_out = torch.empty(len(pairs), dtype=torch.uint8).pin_memory()
+    h_pairs = torch.from_numpy(pairs.view(np.int32)).pin_memory()
+    store = Store()
+
+    def step_device():
+        store.load(0, d["so"], d["sx"])
+        store.load(1, d["to"], d["tx"])
+        store.rasterize(vpr=args.vpr, category_count=16, strict=False)
+        _, found = store.intersect(d_pairs.view(len(pairs), 2), out=d_out)
+        return found
+
+    def step_e2e():
+        store.load(0, S_off_t.numpy().view(np.uint64), S_xy_t.numpy())
+        store.load(1, T_off_t.numpy().view(np.uint64), T_xy_t.numpy())
+        store.rasterize(vpr=args.vpr, category_count=16, strict=False)
+        _, found = store.intersect(h_pairs.numpy().view(np.uint32).reshape(-1, 2), out=h_out.numpy())
+        return found
+
+    for i in range(args.warmup):
+        t = time.time()
+        step_device()
+        log(f"warmup step {i}: {time.time() - t:.2f}s, stats {store.last_stats}")
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    launches0 = store.launches
+    store.event_record(0)
+    founds = []
+    stage = {"filter_ms": 0.0}
+    for _ in range(args.steps):
+        founds.append(step_device())
+        stage["filter_ms"] += store.last_stats["ms_stage"][1]
+    store.event_record(1)
+    ms = store.event_elapsed(0, 1)
+    torch.cuda.synchronize()
+    launches = store.launches - launches0
+    last = dict(store.last_stats)
+    if world > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    t_dev = ms / 1000.0
+    # end to end through the C ABI with host buffers
+    step_e2e()
+    torch.cuda.synchronize()
+    store.event_record(2)
+    for _ in range(args.steps):
+        step_e2e()
+    store.event_record(3)
+    ms_e2e = store.event_elapsed(2, 3)
+    t_e2e = ms_e2e / 1000.0
+    if world > 1:
+        tt = torch.tensor([t_dev, t_e2e], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_dev, t_e2e = tt.tolist()
+        npairs = torch.tensor([len(pairs)], device=dev, dtype=torch.float64)
+        dist.all_reduce(npairs)
+        total_pairs = float(npairs.item())
+    else:
+        total_pairs = float(len(pairs))
+    value = total_pairs * args.steps / t_dev
+    e2e_value = total_pairs * args.steps / t_e2e
+    bits = 4
+    fb = filter_bytes(last, len(pairs), bits)
+    kernel_ms = stage["filter_ms"] / args.steps
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = fb / (kernel_ms / 1000.0) / 1e9 if kernel_ms > 0 else None
+    h2d = int(S_xy_t.numel() * 4 + T_xy_t.numel() * 4 + S_off_t.numel() * 8 + T_off_t.numel() * 8 + pairs.nbytes)
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64", "data": "synthetic (seeded star polygons, configuration 2 generator)",
+        "config": {"workload": "intersect, configuration 2: 100k sources x 1M targets, nv log-uniform 16..100000, "
+                               f"~20M MBR candidates, -v {args.vpr}, -w 16, target batch {W['tb']} of "
+                               f"{N_TGT} (batch {rank % n_batches})",
+                   "domain_side": W["L"], "vpr": args.vpr, "category_count": 16, "n_source": N_SRC,
+                   "n_target_batch": W["tb"], "candidate_pairs_per_step": len(pairs), "found_per_step": founds[-1],
+                   "vertices_per_step": int(S.total + T.total), "l2": "inputs larger than L2 (no flush needed)",
+                   "seed": args.seed, "parallelism": f"weak-dp{world}"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": int(len(pairs))},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "kernel": "k_intersect (filter + refine)", "kernel_ms": kernel_ms,
+                     "algorithmic_bytes": fb, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+        "stage_ms": {"filter_refine": kernel_ms, "step": ms / args.steps},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(W, args, budget_s=args.cpu_seconds, threads=1, gpu_out=h_out.numpy())
+    store.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return result if rank == 0 else None
+
+
+def _oracle_chunk(job):
+    """Worker: oracle rasterization + intersect over a list of sampled pairs."""
+    import time as _t
+    sys.path.insert(0, str(ROOT))
+    from oracle import oracle as O
+    rings_s, rings_t, pairs, vpr = job
+
+    def ras(r):
+        try:
+            return O.Raster(r, vpr)
+        except RuntimeError:  # the reference aborts on this polygon
+            return None
+
+    t0 = _t.perf_counter()
+    rs = {k: ras(r) for k, r in rings_s.items()}
+    rt = {k: ras(r) for k, r in rings_t.items()}
+    t1 = _t.perf_counter()
+    res = [2 if rs[s] is None or rt[t] is None else int(O.intersect(rs[s], rt[t])) for s, t in pairs]
+    t2 = _t.perf_counter()
+    verts = sum(len(r) for r in rings_s.values()) + sum(len(r) for r in rings_t.values())
+    return t1 - t0, t2 - t1, verts, len(pairs), sum(v == 1 for v in res), [(s, t, int(v)) for (s, t), v in zip(pairs, res)]
+
+
+def cpu_baseline(W, args, budget_s: float, threads: int, gpu_out=None) -> dict:
+    """The CPU oracle (a port of the reference's algorithm) on a bounded uniform
+    sample of the step's candidate pairs. Raster time is charged per vertex and
+    query time per pair, then scaled to the whole step."""
+    import multiprocessing as mp
+    S, T, pairs = W["S"], W["T"], W["pairs"]
+    rng = np.random.default_rng(args.seed + 99)
+    order = rng.permutation(len(pairs))
+    chunk = 8
+
+    def job(k):
+        sel = pairs[order[k:k + chunk]]
+        rs = {int(s): np.ascontiguousarray(S.ring(int(s))) for s in set(sel[:, 0].tolist())}
+        rt = {int(t): np.ascontiguousarray(T.ring(int(t))) for t in set(sel[:, 1].tolist())}
+        return (rs, rt, [(int(a), int(b)) for a, b in sel], args.vpr)
+
+    t_r = t_q = 0.0
+    verts = npairs = found = 0
+    checked = []
+    t0 = time.perf_counter()
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(threads) as pool:
+        pending, k = [], 0
+        while True:
+            while len(pending) < 2 * threads and k < len(order) and time.perf_counter() - t0 < budget_s:
+                pending.append(pool.apply_async(_oracle_chunk, (job(k),)))
+                k += chunk
+            if not pending:
+                break
+            r = pending.pop(0).get()
+            t_r += r[0]
+            t_q += r[1]
+            verts += r[2]
+            npairs += r[3]
+            found += r[4]
+            checked.extend(r[5])
+    total_verts = S.total + T.total
+    raster_s = t_r / max(verts, 1) * total_verts
+    query_s = t_q / max(npairs, 1) * len(pairs)
+    value = len(pairs) / (raster_s + query_s) * 1.0
+    extra = {}
+    if gpu_out is not None and checked:
+        # the same oracle doubles as a full-size parity spot check of the GPU results
+        index = {(int(a), int(b)): i for i, (a, b) in enumerate(pairs)}
+        bad = sum(1 for s_, t_, v in checked if int(gpu_out[index[(s_, t_)]]) != v)
+        extra = {"parity_sample_pairs": len(checked), "parity_sample_mismatches": bad}
+    return {**extra, "value": value, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{npairs} uniformly sampled candidate pairs of the step ({verts} vertices rasterized), "
+                      f"{time.perf_counter() - t0:.1f} s wall on {threads} core(s); raster time scaled per vertex "
+                      f"to the step's {total_verts} vertices, query time per pair to its {len(pairs)} pairs",
+            "raster_s_per_step": raster_s, "query_s_per_step": query_s}
+
+
+def run_reference(args) -> dict:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return None
+    W = build_workload(args.seed, 0, args.batches, args.vpr)
+    threads = os.cpu_count() or 1
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.warmup + args.steps):
+        vals.append(cpu_baseline(W, args, budget_s=args.ref_step_seconds, threads=threads))
+    wall = time.perf_counter() - t0
+    v = statistics.median([x["value"] for x in vals[args.warmup:]])
+    cb = dict(vals[-1])
+    cb["value"] = v
+    cb["kind"] = "port"
+    return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1000 / (args.warmup + args.steps),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic (seeded star polygons, configuration 2 generator)", "impl": "reference",
+            "config": {"workload": "intersect, configuration 2 (see ours); CPU oracle port of the reference, "
+                                   f"-v {args.vpr}", "vpr": args.vpr, "seed": args.seed},
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--vpr", type=int, default=64)
+    ap.add_argument("--batches", type=int, default=10, help="target batches the 1M targets are split into")
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--ref-step-seconds", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    res = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if res is not None:
+        print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()

@@ -11,7 +11,7 @@ class Stats(C.Structure):
     _fields_ = [("pairs", C.c_uint64), ("found", C.c_uint64), ("in_hits", C.c_uint64),
                 ("border_pairs", C.c_uint64), ("segment_tests", C.c_uint64), ("fp64_rechecks", C.c_uint64),
                 ("ms_total", C.c_double), ("ms_stage", C.c_double * 4), ("kernel_launches", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("reserved", C.c_int32), ("src_window_pixels", C.c_uint64), ("tgt_window_pixels", C.c_uint64)]
 
 
 class RasterView(C.Structure):
@@ -48,6 +48,7 @@ def declare(lib):
     lib.farm_raster_fetch.argtypes = [vp, C.c_int, C.c_uint64, C.POINTER(RasterView), u8p, u32p, u32p, u32p, f64p,
                                       u32p, f64p, f64p, f64p]
     lib.farm_sync.argtypes = [vp]
+    lib.farm_raster_errors.argtypes = [vp, C.c_int, vp, C.c_uint64]
     lib.farm_event_record.argtypes = [vp, C.c_int]
     lib.farm_event_elapsed.argtypes = [vp, C.c_int, C.c_int, f64p]
     lib.farm_store_launches.argtypes = [vp]

@@ -200,7 +200,7 @@ struct farm_store {
     farm::DevBuf d_hdr, d_status, d_offset, d_seq, d_hoff, d_hnodes, d_voff, d_vnodes, d_areas;
     uint64_t tot_P = 0, tot_status = 0, tot_seq = 0;
     // scratch for the rasterizer and the queries
-    farm::DevBuf s[24];
+    farm::DevBuf s[32];
     farm::DevBuf cub_tmp;
     farm::DevBuf d_pairs, d_out, d_counters;
     cudaEvent_t ev[8] = {};

@@ -120,9 +120,10 @@ int farm_gen_device(double dom_lo, double dom_hi, double r_lo, double r_hi, doub
     return FARM_OK;
 }
 
-/* CUDA-event timing on the store's own stream: record slot, elapsed a -> b. */
+/* CUDA-event timing on the store's own stream: record slot, elapsed a -> b.
+ * Slots 0-5 belong to the caller; the queries time themselves with 6 and 7. */
 int farm_event_record(farm_store *s, int slot) {
-    if (!s || slot < 0 || slot >= 8) {
+    if (!s || slot < 0 || slot >= 6) {
         set_error("invalid event slot");
         return FARM_EINVAL;
     }
@@ -131,7 +132,7 @@ int farm_event_record(farm_store *s, int slot) {
 }
 
 int farm_event_elapsed(farm_store *s, int a, int b, double *ms) {
-    if (!s || !ms || a < 0 || a >= 8 || b < 0 || b >= 8) {
+    if (!s || !ms || a < 0 || a >= 6 || b < 0 || b >= 6) {
         set_error("invalid event slot");
         return FARM_EINVAL;
     }

@@ -65,7 +65,7 @@ __device__ __forceinline__ Window retrieve(const double *mbr, double stx, double
 }
 
 struct IxCounters {
-    unsigned long long found, in_hits, border_pairs, segment_tests;
+    unsigned long long found, in_hits, border_pairs, segment_tests, src_window, tgt_window;
 };
 
 // Refine one BORDER x BORDER pixel pair: any edge-sequence pair with an
@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     uint2 *q = queue[wib];
     const int cc = sv.category_count;
-    unsigned long long my_found = 0, my_in = 0, my_bb = 0, my_tests = 0;
+    unsigned long long my_found = 0, my_in = 0, my_bb = 0, my_tests = 0, my_ws = 0, my_wt = 0;
     for (;;) {
         unsigned long long pid = 0;
         if (lane == 0) pid = atomicAdd(next, 1ull);
@@ -108,6 +108,10 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         const uint32_t s = pv.pairs[2 * pid], t = pv.pairs[2 * pid + 1];
         const PolyHdr &S = sv.hdr[s];
         const PolyHdr &T = sv.hdr[pv.tgt_base + t];
+        if (S.err || T.err) {  // the reference aborts on one of the two polygons
+            if (lane == 0 && out) out[pid] = 2;
+            continue;
+        }
         const uint8_t *sst = sv.status + S.st, *tst = sv.status + T.st;
         Window w = retrieve(S.mbr, S.step_x, S.step_y, S.dimx, S.dimy, T.mbr[0], T.mbr[1], T.mbr[2], T.mbr[3]);
         const int wh = w.ey - w.sy + 1;
@@ -156,6 +160,10 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
             }
             uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
             uint32_t excl = incl - cnt;
+            if (lane == 0) {
+                my_ws += (unsigned long long)min((long)32, nw - base);
+                my_wt += total;
+            }
             for (uint32_t f = 0; f < total && !decided; f += 32) {
                 uint32_t item = f + lane;
                 bool valid = item < total;
@@ -225,6 +233,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         atomicAdd(&ctr->in_hits, my_in);
         atomicAdd(&ctr->border_pairs, my_bb);
         atomicAdd(&ctr->segment_tests, my_tests);
+        atomicAdd(&ctr->src_window, my_ws);
+        atomicAdd(&ctr->tgt_window, my_wt);
     }
 }
 
@@ -241,10 +251,7 @@ int intersect(farm_store *s, const uint32_t *pairs, uint64_t n, int mode, int me
         set_error("farm_intersect: no target side loaded");
         return FARM_EINVAL;
     }
-    if (s->raster_err) {
-        set_error("farm_intersect: a polygon failed rasterization (a reference assert); see farm_raster_fetch");
-        return s->raster_err;
-    }
+
     cudaStream_t stream = s->stream;
     const uint32_t *dpairs = pairs;
     if (mem == FARM_MEM_HOST && n) {
@@ -263,12 +270,12 @@ int intersect(farm_store *s, const uint32_t *pairs, uint64_t n, int mode, int me
     FARM_CUDA(cudaMemsetAsync(next, 0, 8 + sizeof(IxCounters), stream));
     PairView pv{dpairs, n, s->n_side[0]};
     StoreView sv = s->view();
-    FARM_CUDA(cudaEventRecord(s->ev[0], stream));
+    FARM_CUDA(cudaEventRecord(s->ev[6], stream));
     int blocks = sm_count() * 8;
     k_intersect<<<blocks, kWarpsPerBlock * 32, 0, stream>>>(sv, pv, next, dout, ctr);
     s->launches++;
     FARM_CUDA(cudaGetLastError());
-    FARM_CUDA(cudaEventRecord(s->ev[1], stream));
+    FARM_CUDA(cudaEventRecord(s->ev[7], stream));
     IxCounters h{};
     FARM_CUDA(cudaMemcpyAsync(&h, ctr, sizeof h, cudaMemcpyDeviceToHost, stream));
     if (mem == FARM_MEM_HOST && out && n) FARM_CUDA(cudaMemcpyAsync(out, dout, n, cudaMemcpyDeviceToHost, stream));
@@ -281,8 +288,10 @@ int intersect(farm_store *s, const uint32_t *pairs, uint64_t n, int mode, int me
         st->in_hits = h.in_hits;
         st->border_pairs = h.border_pairs;
         st->segment_tests = h.segment_tests;
+        st->src_window_pixels = h.src_window;
+        st->tgt_window_pixels = h.tgt_window;
         float ms = 0;
-        cudaEventElapsedTime(&ms, s->ev[0], s->ev[1]);
+        cudaEventElapsedTime(&ms, s->ev[6], s->ev[7]);
         st->ms_total = ms;
         st->ms_stage[1] = ms;
         st->kernel_launches = 1;

@@ -17,6 +17,7 @@
 #include <cub/cub.cuh>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "common.cuh"
@@ -54,6 +55,8 @@ enum Scratch {
     S_ROWY,
     S_TMP_A,
     S_TMP_B,
+    S_CPOLY,  // column polygons of the fill sweep
+    S_SMALL,  // small-point flags / scan / index
 };
 
 // ------------------------------------------------------------ headers ----
@@ -462,231 +465,6 @@ struct FillSink {
     __device__ bool failed() const { return bad; }
 };
 
-__global__ void k_walk_count(const StoreView sv, PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off,
-                             uint32_t npoly, uint64_t nedges, uint32_t *__restrict__ cnt) {
-    uint64_t n1 = nedges + 1;
-    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nedges;
-         e += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t p = find_segment(off, npoly, e);
-        const PolyHdr &h = hdr[p];
-        uint32_t i = (uint32_t)(e - h.edge);
-        const float2 *r = sv.ring + h.ring;
-        CountSink s;
-        s.status = sv.status + h.st;
-        s.dimx = h.dimx;
-        s.dimy = h.dimy;
-        if (h.err == 0) walk_edge(h, r[i], r[i + 1], s);
-        if (s.bad) atomicMin(&hdr[p].err, FARM_EASSERT);
-        cnt[e] = s.nc;
-        cnt[n1 + e] = s.nh;
-        cnt[2 * n1 + e] = s.nv;
-    }
-}
-
-__global__ void k_walk_fill(const StoreView sv, const PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off,
-                            uint32_t npoly, uint64_t nedges, const uint64_t *__restrict__ scan, uint32_t *from,
-                            uint32_t *to, uint32_t *cedge, uint64_t *hkey, double *hval, uint64_t *vkey,
-                            double *vval) {
-    uint64_t n1 = nedges + 1;
-    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nedges;
-         e += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t p = find_segment(off, npoly, e);
-        const PolyHdr &h = hdr[p];
-        uint32_t i = (uint32_t)(e - h.edge);
-        const float2 *r = sv.ring + h.ring;
-        // walk exactly the edges the count pass walked (those with output)
-        if (scan[e + 1] == scan[e] && scan[n1 + e + 1] == scan[n1 + e] && scan[2 * n1 + e + 1] == scan[2 * n1 + e])
-            continue;
-        FillSink s;
-        s.dimx = h.dimx;
-        s.dimy = h.dimy;
-        s.edge = i;
-        s.c = scan[e];
-        s.hn = scan[n1 + e];
-        s.vn = scan[2 * n1 + e];
-        s.from = from;
-        s.to = to;
-        s.cedge = cedge;
-        s.hkey = hkey;
-        s.hval = hval;
-        s.vkey = vkey;
-        s.vval = vval;
-        s.hline = h.hline;
-        s.vline = h.vline;
-        walk_edge(h, r[i], r[i + 1], s);
-    }
-}
-
-// per polygon crossing base and sequence count
-__global__ void k_cross_base(PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off, uint32_t npoly,
-                             const uint64_t *__restrict__ escan, uint64_t *__restrict__ cbase,
-                             uint64_t *__restrict__ nseq) {
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p <= npoly; p += gridDim.x * blockDim.x) {
-        uint64_t cb = escan[off[p]];
-        cbase[p] = cb;
-        if (p < npoly) {
-            uint64_t ce = escan[off[p + 1]];
-            uint64_t c = ce - cb;
-            hdr[p].cross = cb;
-            nseq[p] = c ? c + 1 : 1;
-            if (!c && hdr[p].P != 1) hdr[p].err = FARM_EASSERT;
-        } else {
-            nseq[p] = 0;
-        }
-    }
-}
-
-// Visits: crossing c enters pixel to[c]; the visit ends at the next crossing
-// (which must leave that pixel). The ring's last crossing closes the visit to
-// the start pixel that the first crossing left; it is placed first so that,
-// after a stable sort by pixel, its two sequences lead that pixel's list, as
-// the LEAVE-first case of Ideal.cpp:158-165 orders them.
-__global__ void k_visits(PolyHdr *__restrict__ hdr, uint32_t npoly, const uint64_t *__restrict__ cbase,
-                         uint64_t ncross, const uint32_t *__restrict__ from, const uint32_t *__restrict__ to,
-                         const uint32_t *__restrict__ cedge, uint64_t *__restrict__ vkey,
-                         uint64_t *__restrict__ vval) {
-    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncross;
-         c += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t p = find_segment(cbase, npoly, c);
-        uint64_t cb = cbase[p], ce = cbase[p + 1];
-        const PolyHdr &h = hdr[p];
-        uint64_t pos;
-        uint32_t ein = cedge[c], eout;
-        bool wrap = (c == ce - 1);
-        uint64_t nxt = wrap ? cb : c + 1;
-        eout = cedge[nxt];
-        if (from[nxt] != to[c]) atomicMin(&hdr[p].err, FARM_EASSERT);
-        pos = wrap ? cb : c + 1;
-        vkey[pos] = h.pix + to[c];
-        vval[pos] = ((uint64_t)ein << 32) | (uint64_t)eout | (wrap ? (1ull << 63) : 0ull);
-    }
-}
-
-__global__ void k_seq_width(const uint64_t *__restrict__ vkey, const uint64_t *__restrict__ vval, uint64_t n,
-                            uint64_t *__restrict__ w, uint32_t *__restrict__ pixcnt) {
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t wd = (vval[k] >> 63) ? 2u : 1u;
-        w[k] = wd;
-        atomicAdd(&pixcnt[vkey[k]], wd);
-    }
-}
-
-__global__ void k_seq_fill(PolyHdr *__restrict__ hdr, uint32_t npoly, const uint64_t *__restrict__ cbase,
-                           const uint64_t *__restrict__ seqbase, const uint64_t *__restrict__ vval,
-                           const uint64_t *__restrict__ wscan, uint64_t n, uint2 *__restrict__ seq) {
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t p = find_segment(cbase, npoly, k);
-        uint64_t cb = cbase[p];
-        uint64_t at = seqbase[p] + (wscan[k] - wscan[cb]);
-        uint64_t v = vval[k];
-        uint32_t ein = (uint32_t)((v >> 32) & 0x7FFFFFFFu), eout = (uint32_t)(v & 0xFFFFFFFFu);
-        uint32_t nv = hdr[p].nv;
-        if (v >> 63) {
-            // add_edge(0, first leave) and add_edge(last enter, nv - 2)
-            seq[at] = make_uint2(0u, eout + 1u);
-            seq[at + 1] = make_uint2(ein, nv - 2u - ein + 1u);
-        } else {
-            if (eout < ein) atomicMin(&hdr[p].err, FARM_EASSERT);
-            seq[at] = make_uint2(ein, eout - ein + 1u);
-        }
-    }
-}
-
-// Polygons without crossings: one sequence covering the ring (Ideal.cpp:523-529).
-__global__ void k_seq_single(PolyHdr *__restrict__ hdr, uint32_t npoly, const uint64_t *__restrict__ seqbase,
-                             const uint64_t *__restrict__ cbase, uint2 *__restrict__ seq, uint32_t *__restrict__ pixcnt) {
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npoly; p += gridDim.x * blockDim.x) {
-        PolyHdr &h = hdr[p];
-        h.seq = seqbase[p];
-        h.n_seq = (uint32_t)(seqbase[p + 1] - seqbase[p]);
-        if (cbase[p + 1] == cbase[p]) {
-            seq[h.seq] = make_uint2(0u, h.nv);
-            pixcnt[h.pix] += 1;
-        }
-    }
-}
-
-// CSR offsets: offset[i] = sequences in pixels before i (Ideal.cpp:35-45 makes
-// non-BORDER pixels repeat the next start, which is the same prefix).
-__global__ void k_offsets(const PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ pixbase, uint32_t npoly,
-                          uint64_t totP, const uint64_t *__restrict__ pscan, uint32_t *__restrict__ offset) {
-    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < totP; g += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t p = find_segment(pixbase, npoly, g);
-        const PolyHdr &h = hdr[p];
-        uint32_t i = (uint32_t)(g - h.pix);
-        offset[h.off + i] = (uint32_t)(pscan[g] - pscan[h.pix]);
-        if (i == 0) offset[h.off + h.P] = h.n_seq;
-    }
-}
-
-__global__ void k_line_count(const uint64_t *__restrict__ key, uint64_t n, uint32_t *__restrict__ cnt) {
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
-        atomicAdd(&cnt[key[k]], 1u);
-}
-
-__global__ void k_line_scatter(const uint64_t *__restrict__ key, const double *__restrict__ val, uint64_t n,
-                               const uint64_t *__restrict__ start, uint32_t *__restrict__ fillc,
-                               double *__restrict__ out) {
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t l = key[k];
-        uint32_t r = atomicAdd(&fillc[l], 1u);
-        out[start[l] + r] = val[k];
-    }
-}
-
-// Grid-line offsets (Ideal.cpp:185-238): lines with nodes get their start,
-// others keep 0; the end entries get the node count.
-__global__ void k_line_offsets(PolyHdr *__restrict__ hdr, uint32_t npoly, int vertical,
-                               const uint32_t *__restrict__ cnt, const uint64_t *__restrict__ start,
-                               uint32_t *__restrict__ loff) {
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npoly; p += gridDim.x * blockDim.x) {
-        PolyHdr &h = hdr[p];
-        uint64_t lb = vertical ? h.vline : h.hline;
-        int dim = vertical ? h.dimx : h.dimy;
-        uint64_t nb = start[lb];
-        uint32_t total = (uint32_t)(start[lb + dim + 2] - nb);
-        for (int l = 0; l < dim + 2; l++) loff[lb + l] = cnt[lb + l] ? (uint32_t)(start[lb + l] - nb) : 0u;
-        loff[lb + dim] = total;
-        if (vertical) {
-            loff[lb + dim + 1] = total;
-            h.vnode = nb;
-            h.n_vnodes = total;
-        } else {
-            h.hnode = nb;
-            h.n_hnodes = total;
-        }
-    }
-}
-
-// Ideal.cpp:540-573, one thread per row.
-__global__ void k_scanline(const PolyHdr *__restrict__ hdr, uint32_t npoly, const uint64_t *__restrict__ rowbase,
-                           uint64_t nrows, uint8_t *__restrict__ status, const uint32_t *__restrict__ hoff,
-                           const double *__restrict__ hnodes, int cc) {
-    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < nrows; g += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t p = find_segment(rowbase, npoly, g);
-        const PolyHdr &h = hdr[p];
-        int y = (int)(g - rowbase[p]);
-        if (y < 1 || y >= h.dimy || h.err) continue;
-        const double start_x = h.mbr[0];
-        bool isin = false;
-        uint32_t i = hoff[h.hline + y], j = hoff[h.hline + y + 1];
-        const double *nodes = hnodes + h.hnode;
-        uint8_t *st = status + h.st + (uint64_t)y * h.dimx;
-        for (int x = 0; x < h.dimx; x++) {
-            if (show_status(st[x], cc) != 1) {
-                st[x] = isin ? 2 : 0;
-                continue;
-            }
-            int pass = 0;
-            while (i < j && nodes[i] <= start_x + h.step_x * (x + 1)) {
-                pass++;
-                i++;
-            }
-            if (pass % 2 == 1) isin = !isin;
-        }
-    }
-}
-
 // ------------------------------------------------------------ fill ----
 
 __device__ inline bool in_rng(double lo, double hi, double v) { return !(v < lo || v > hi); }
@@ -792,16 +570,308 @@ __device__ int first_line(const double *lines, int n, double step, double v) {
 // margin covering the float rounding of a clip line coordinate
 __device__ inline double fmargin(double a, double b) { return (fabs(a) + fabs(b)) * 1.2e-7 + 1e-30; }
 
-// Per edge: points contributed to every column (count pass or emit pass).
-__global__ void k_clipx(const StoreView sv, const PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off,
-                        uint32_t npoly, uint64_t nedges, const double *__restrict__ colx, uint32_t *__restrict__ cnt,
-                        const uint64_t *__restrict__ scan, uint64_t *__restrict__ okey, float2 *__restrict__ opt) {
+// "Small" points: a coordinate below 2^-5 in magnitude, where two distinct
+// floats can be closer than the 1e-9 of Point::operator==. Elsewhere that
+// equality is bit equality (float spacing there exceeds 1e-9).
+__device__ inline bool small_pt(float2 q) { return fabsf(q.x) < 0.03125f || fabsf(q.y) < 0.03125f; }
+
+__device__ inline uint64_t pt_bits(float2 q) {
+    return ((uint64_t)__float_as_uint(q.x) << 32) | (uint64_t)__float_as_uint(q.y);
+}
+
+// ======================================================= chunked pipeline ==
+// Phase 1 covers every polygon at once and only accumulates per-polygon
+// totals (crossings, grid-line nodes), which size the persistent outputs.
+// Phase 2 runs the full pipeline over chunks of polygons whose scratch fits a
+// fixed budget, writing into those outputs at each polygon's base.
+
+struct Chunk {
+    uint32_t p0, np;  // polygons
+    uint64_t e0, ne;  // edges
+    uint64_t pix0, npix;
+    uint64_t h0, nh;     // horizontal grid lines
+    uint64_t v0, nvl;    // vertical grid lines
+    uint64_t col0, ncol; // fill sweep columns
+    uint64_t row0, nrow; // scanline rows
+    uint64_t hn0, vn0;   // global node bases of the chunk's first polygon
+};
+
+__global__ void k_walk_tot(const StoreView sv, PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off,
+                           uint32_t npoly, uint64_t nedges, unsigned long long *__restrict__ tot) {
     for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nedges;
          e += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t p = find_segment(off, npoly, e);
         const PolyHdr &h = hdr[p];
+        if (h.err) continue;
+        uint32_t i = (uint32_t)(e - h.edge);
+        const float2 *r = sv.ring + h.ring;
+        CountSink s;
+        s.status = sv.status + h.st;
+        s.dimx = h.dimx;
+        s.dimy = h.dimy;
+        walk_edge(h, r[i], r[i + 1], s);
+        if (s.bad) atomicMin(&hdr[p].err, FARM_EASSERT);
+        if (s.nc) atomicAdd(&tot[3ull * p], (unsigned long long)s.nc);
+        if (s.nh) atomicAdd(&tot[3ull * p + 1], (unsigned long long)s.nh);
+        if (s.nv) atomicAdd(&tot[3ull * p + 2], (unsigned long long)s.nv);
+    }
+}
+
+__global__ void k_tot_sizes(const unsigned long long *__restrict__ tot, const PolyHdr *__restrict__ hdr,
+                            uint32_t npoly, uint64_t *__restrict__ sz) {
+    uint64_t n1 = (uint64_t)npoly + 1;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p <= npoly; p += gridDim.x * blockDim.x) {
+        if (p == npoly) {
+            sz[p] = sz[n1 + p] = sz[2 * n1 + p] = 0;
+            continue;
+        }
+        uint64_t c = tot[3ull * p];
+        sz[p] = hdr[p].err ? 0 : (c ? c + 1 : 1);
+        sz[n1 + p] = hdr[p].err ? 0 : tot[3ull * p + 1];
+        sz[2 * n1 + p] = hdr[p].err ? 0 : tot[3ull * p + 2];
+    }
+}
+
+__global__ void k_set_node_bases(PolyHdr *__restrict__ hdr, uint32_t npoly, const uint64_t *__restrict__ sz,
+                                 const uint64_t *__restrict__ sc) {
+    uint64_t n1 = (uint64_t)npoly + 1;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npoly; p += gridDim.x * blockDim.x) {
+        PolyHdr &h = hdr[p];
+        h.seq = sc[p];
+        h.n_seq = (uint32_t)sz[p];
+        h.hnode = sc[n1 + p];
+        h.n_hnodes = (uint32_t)sz[n1 + p];
+        h.vnode = sc[2 * n1 + p];
+        h.n_vnodes = (uint32_t)sz[2 * n1 + p];
+    }
+}
+
+__global__ void k_walk_count(const StoreView sv, PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off,
+                             Chunk ch, uint32_t *__restrict__ cnt) {
+    uint64_t n1 = ch.ne + 1;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < ch.ne;
+         k += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t e = ch.e0 + k;
+        uint32_t p = ch.p0 + find_segment(off + ch.p0, ch.np, e);
+        const PolyHdr &h = hdr[p];
+        CountSink s;
+        s.status = sv.status + h.st;
+        s.dimx = h.dimx;
+        s.dimy = h.dimy;
+        if (h.err == 0) {
+            uint32_t i = (uint32_t)(e - h.edge);
+            const float2 *r = sv.ring + h.ring;
+            walk_edge(h, r[i], r[i + 1], s);
+        }
+        if (s.bad) atomicMin(&hdr[p].err, FARM_EASSERT);
+        cnt[k] = s.nc;
+        cnt[n1 + k] = s.nh;
+        cnt[2 * n1 + k] = s.nv;
+    }
+}
+
+__global__ void k_walk_fill(const StoreView sv, const PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off,
+                            Chunk ch, const uint64_t *__restrict__ scan, uint32_t *from, uint32_t *to,
+                            uint32_t *cedge, uint64_t *hkey, double *hval, uint64_t *vkey, double *vval) {
+    uint64_t n1 = ch.ne + 1;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < ch.ne;
+         k += (uint64_t)gridDim.x * blockDim.x) {
+        // walk exactly the edges the count pass walked (those with output)
+        if (scan[k + 1] == scan[k] && scan[n1 + k + 1] == scan[n1 + k] && scan[2 * n1 + k + 1] == scan[2 * n1 + k])
+            continue;
+        uint64_t e = ch.e0 + k;
+        uint32_t p = ch.p0 + find_segment(off + ch.p0, ch.np, e);
+        const PolyHdr &h = hdr[p];
+        uint32_t i = (uint32_t)(e - h.edge);
+        const float2 *r = sv.ring + h.ring;
+        FillSink s;
+        s.dimx = h.dimx;
+        s.dimy = h.dimy;
+        s.edge = i;
+        s.c = scan[k];
+        s.hn = scan[n1 + k];
+        s.vn = scan[2 * n1 + k];
+        s.from = from;
+        s.to = to;
+        s.cedge = cedge;
+        s.hkey = hkey;
+        s.hval = hval;
+        s.vkey = vkey;
+        s.vval = vval;
+        s.hline = h.hline - ch.h0;
+        s.vline = h.vline - ch.v0;
+        walk_edge(h, r[i], r[i + 1], s);
+    }
+}
+
+// per polygon (chunk-local) crossing base
+__global__ void k_cross_base(const uint64_t *__restrict__ off, Chunk ch, const uint64_t *__restrict__ escan,
+                             uint64_t *__restrict__ cbase) {
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q <= ch.np; q += gridDim.x * blockDim.x)
+        cbase[q] = escan[off[ch.p0 + q] - ch.e0];
+}
+
+// Visits: crossing c enters pixel to[c]; the visit ends at the next crossing
+// (which must leave that pixel). The ring's last crossing closes the visit to
+// the start pixel that the first crossing left; it is placed first so that,
+// after a stable sort by pixel, its two sequences lead that pixel's list, as
+// the LEAVE-first case of Ideal.cpp:158-165 orders them.
+__global__ void k_visits(PolyHdr *__restrict__ hdr, Chunk ch, const uint64_t *__restrict__ cbase, uint64_t ncross,
+                         const uint32_t *__restrict__ from, const uint32_t *__restrict__ to,
+                         const uint32_t *__restrict__ cedge, uint64_t *__restrict__ vkey,
+                         uint64_t *__restrict__ vval) {
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncross;
+         c += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t q = find_segment(cbase, ch.np, c);
+        uint64_t cb = cbase[q], ce = cbase[q + 1];
+        const PolyHdr &h = hdr[ch.p0 + q];
+        bool wrap = (c == ce - 1);
+        uint64_t nxt = wrap ? cb : c + 1;
+        if (from[nxt] != to[c]) atomicMin(&hdr[ch.p0 + q].err, FARM_EASSERT);
+        uint64_t pos = wrap ? cb : c + 1;
+        vkey[pos] = (h.pix - ch.pix0) + to[c];
+        vval[pos] = ((uint64_t)cedge[c] << 32) | (uint64_t)cedge[nxt] | (wrap ? (1ull << 63) : 0ull);
+    }
+}
+
+__global__ void k_seq_width(const uint64_t *__restrict__ vkey, const uint64_t *__restrict__ vval, uint64_t n,
+                            uint64_t *__restrict__ w, uint32_t *__restrict__ pixcnt) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t wd = (vval[k] >> 63) ? 2u : 1u;
+        w[k] = wd;
+        atomicAdd(&pixcnt[vkey[k]], wd);
+    }
+}
+
+__global__ void k_seq_fill(PolyHdr *__restrict__ hdr, Chunk ch, const uint64_t *__restrict__ cbase,
+                           const uint64_t *__restrict__ vval, const uint64_t *__restrict__ wscan, uint64_t n,
+                           uint2 *__restrict__ seq) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t q = find_segment(cbase, ch.np, k);
+        PolyHdr &h = hdr[ch.p0 + q];
+        uint64_t rel = wscan[k] - wscan[cbase[q]];
+        uint64_t v = vval[k];
+        uint32_t ein = (uint32_t)((v >> 32) & 0x7FFFFFFFu), eout = (uint32_t)(v & 0xFFFFFFFFu);
+        uint32_t wd = (v >> 63) ? 2u : 1u;
+        if (rel + wd > h.n_seq) {  // sizes disagree with the first pass
+            atomicMin(&h.err, FARM_EINTERNAL);
+            continue;
+        }
+        uint64_t at = h.seq + rel;
+        if (v >> 63) {
+            // add_edge(0, first leave) and add_edge(last enter, nv - 2)
+            seq[at] = make_uint2(0u, eout + 1u);
+            seq[at + 1] = make_uint2(ein, h.nv - 2u - ein + 1u);
+        } else {
+            if (eout < ein) atomicMin(&h.err, FARM_EASSERT);
+            seq[at] = make_uint2(ein, eout - ein + 1u);
+        }
+    }
+}
+
+// Polygons without crossings: one sequence covering the ring (Ideal.cpp:523-529).
+__global__ void k_seq_single(const PolyHdr *__restrict__ hdr, Chunk ch, const uint64_t *__restrict__ cbase,
+                             uint2 *__restrict__ seq, uint32_t *__restrict__ pixcnt) {
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < ch.np; q += gridDim.x * blockDim.x) {
+        const PolyHdr &h = hdr[ch.p0 + q];
+        if (h.err == 0 && cbase[q + 1] == cbase[q]) {
+            seq[h.seq] = make_uint2(0u, h.nv);
+            pixcnt[h.pix - ch.pix0] += 1;
+        }
+    }
+}
+
+// CSR offsets: offset[i] = sequences in pixels before i (Ideal.cpp:35-45 makes
+// non-BORDER pixels repeat the next start, which is the same prefix).
+__global__ void k_offsets(const PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ pixbase, Chunk ch,
+                          const uint64_t *__restrict__ pscan, uint32_t *__restrict__ offset) {
+    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ch.npix;
+         g += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t p = ch.p0 + find_segment(pixbase + ch.p0, ch.np, g + ch.pix0);
+        const PolyHdr &h = hdr[p];
+        uint64_t lb = h.pix - ch.pix0;
+        uint32_t i = (uint32_t)(g - lb);
+        offset[h.off + i] = (uint32_t)(pscan[g] - pscan[lb]);
+        if (i == 0) offset[h.off + h.P] = h.n_seq;
+    }
+}
+
+__global__ void k_line_count(const uint64_t *__restrict__ key, uint64_t n, uint32_t *__restrict__ cnt) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
+        atomicAdd(&cnt[key[k]], 1u);
+}
+
+__global__ void k_line_scatter(const uint64_t *__restrict__ key, const double *__restrict__ val, uint64_t n,
+                               const uint64_t *__restrict__ start, uint32_t *__restrict__ fillc,
+                               double *__restrict__ out) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t l = key[k];
+        uint32_t r = atomicAdd(&fillc[l], 1u);
+        out[start[l] + r] = val[k];
+    }
+}
+
+// Grid-line offsets (Ideal.cpp:185-238): lines with nodes get their start,
+// others keep 0; the end entries get the node count.
+__global__ void k_line_offsets(PolyHdr *__restrict__ hdr, Chunk ch, int vertical, const uint32_t *__restrict__ cnt,
+                               const uint64_t *__restrict__ start, uint32_t *__restrict__ loff) {
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < ch.np; q += gridDim.x * blockDim.x) {
+        PolyHdr &h = hdr[ch.p0 + q];
+        uint64_t gl = vertical ? h.vline : h.hline;
+        uint64_t lb = gl - (vertical ? ch.v0 : ch.h0);
+        int dim = vertical ? h.dimx : h.dimy;
+        uint64_t nb = start[lb];
+        uint32_t total = (uint32_t)(start[lb + dim + 2] - nb);
+        uint64_t gnode = (vertical ? ch.vn0 : ch.hn0) + nb;
+        if (total != (vertical ? h.n_vnodes : h.n_hnodes) || gnode != (vertical ? h.vnode : h.hnode))
+            atomicMin(&h.err, FARM_EINTERNAL);
+        for (int l = 0; l < dim + 2; l++) loff[gl + l] = cnt[lb + l] ? (uint32_t)(start[lb + l] - nb) : 0u;
+        loff[gl + dim] = total;
+        if (vertical) loff[gl + dim + 1] = total;
+    }
+}
+
+// Ideal.cpp:540-573, one thread per row.
+__global__ void k_scanline(const PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ rowbase, Chunk ch,
+                           uint8_t *__restrict__ status, const uint32_t *__restrict__ hoff,
+                           const double *__restrict__ hnodes, int cc) {
+    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ch.nrow;
+         g += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t p = ch.p0 + find_segment(rowbase + ch.p0, ch.np, g + ch.row0);
+        const PolyHdr &h = hdr[p];
+        int y = (int)(g + ch.row0 - rowbase[p]);
+        if (y < 1 || y >= h.dimy || h.err) continue;
+        const double start_x = h.mbr[0];
+        bool isin = false;
+        uint32_t i = hoff[h.hline + y], j = hoff[h.hline + y + 1];
+        const double *nodes = hnodes + h.hnode;
+        uint8_t *st = status + h.st + (uint64_t)y * h.dimx;
+        for (int x = 0; x < h.dimx; x++) {
+            if (show_status(st[x], cc) != 1) {
+                st[x] = isin ? 2 : 0;
+                continue;
+            }
+            int pass = 0;
+            while (i < j && nodes[i] <= start_x + h.step_x * (x + 1)) {
+                pass++;
+                i++;
+            }
+            if (pass % 2 == 1) isin = !isin;
+        }
+    }
+}
+
+// Per edge: points contributed to every column (count pass or emit pass).
+__global__ void k_clipx(const StoreView sv, const PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off,
+                        Chunk ch, const double *__restrict__ colx, uint32_t *__restrict__ cnt,
+                        const uint64_t *__restrict__ scan, uint64_t *__restrict__ okey, float2 *__restrict__ opt) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < ch.ne;
+         k += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t e = ch.e0 + k;
+        uint32_t p = ch.p0 + find_segment(off + ch.p0, ch.np, e);
+        const PolyHdr &h = hdr[p];
         if (h.err) {
-            if (cnt) cnt[e] = 0;
+            if (cnt) cnt[k] = 0;
             continue;
         }
         uint32_t i = (uint32_t)(e - h.edge);
@@ -812,31 +882,22 @@ __global__ void k_clipx(const StoreView sv, const PolyHdr *__restrict__ hdr, con
         const double *lines = colx + h.col;
         int c = first_line(lines, h.ncols, h.step_x, mnx - mg);
         uint32_t total = 0;
-        uint64_t at = scan ? scan[e] : 0;
+        uint64_t at = scan ? scan[k] : 0;
         float2 buf[4];
         for (; c < h.ncols && lines[c] <= mxx + mg; c++) {
             double Xi = lines[c], Xi1 = Xi + h.step_x;
-            int k = clip_x_points(A, B, Xi, Xi1, okey ? buf : nullptr);
+            int m = clip_x_points(A, B, Xi, Xi1, okey ? buf : nullptr);
             if (okey) {
-                for (int q = 0; q < k; q++) {
-                    okey[at] = h.col + (uint64_t)c;
+                for (int q = 0; q < m; q++) {
+                    okey[at] = (h.col - ch.col0) + (uint64_t)c;
                     opt[at] = buf[q];
                     at++;
                 }
             }
-            total += (uint32_t)k;
+            total += (uint32_t)m;
         }
-        if (cnt) cnt[e] = total;
+        if (cnt) cnt[k] = total;
     }
-}
-
-// "Small" points: a coordinate below 2^-5 in magnitude, where two distinct
-// floats can be closer than the 1e-9 of Point::operator==. Elsewhere that
-// equality is bit equality (float spacing there exceeds 1e-9).
-__device__ inline bool small_pt(float2 q) { return fabsf(q.x) < 0.03125f || fabsf(q.y) < 0.03125f; }
-
-__device__ inline uint64_t pt_bits(float2 q) {
-    return ((uint64_t)__float_as_uint(q.x) << 32) | (uint64_t)__float_as_uint(q.y);
 }
 
 __global__ void k_ptbits(const float2 *__restrict__ pt, uint64_t n, uint64_t *__restrict__ bits,
@@ -850,8 +911,7 @@ __global__ void k_ptbits(const float2 *__restrict__ pt, uint64_t n, uint64_t *__
 // After sorting by (column, bits, position): a non-first element of a run of
 // identical large points is a later duplicate (MyPolygon.h:49-58 drops it).
 __global__ void k_dup_large(const uint64_t *__restrict__ col, const uint32_t *__restrict__ pos,
-                            const float2 *__restrict__ pt, uint64_t n, uint8_t *__restrict__ drop,
-                            uint8_t *__restrict__ colsmall_flag_unused) {
+                            const float2 *__restrict__ pt, uint64_t n, uint8_t *__restrict__ drop) {
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t me = pos[k];
         float2 q = pt[me];
@@ -872,20 +932,59 @@ __global__ void k_col_count(const uint64_t *__restrict__ colkey, const float2 *_
 }
 
 // Columns holding small points: the reference's sequential rule, restricted to
-// the small points (a small point never equals a large one).
+// the small points (a small point never equals a large one). One warp per
+// column walks the column's small points (compacted, in order) in chunks of
+// 32: each lane first compares its point with every kept point of earlier
+// chunks, then the chunk resolves its own order with one ballot per lane.
+__global__ void k_small_flags(const float2 *__restrict__ pt, uint64_t n, uint64_t *__restrict__ flag) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
+        flag[k] = small_pt(pt[k]) ? 1 : 0;
+}
+
+__global__ void k_small_compact(const float2 *__restrict__ pt, uint64_t n, const uint64_t *__restrict__ sscan,
+                                uint32_t *__restrict__ sidx) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
+        if (sscan[k + 1] != sscan[k]) sidx[sscan[k]] = (uint32_t)k;
+}
+
 __global__ void k_dup_small(const uint64_t *__restrict__ colstart, uint64_t ncol, const uint8_t *__restrict__ colsmall,
+                            const uint64_t *__restrict__ sscan, const uint32_t *__restrict__ sidx,
                             const float2 *__restrict__ pt, uint8_t *__restrict__ drop) {
-    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncol; c += (uint64_t)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t c = w; c < ncol; c += nw) {
         if (!colsmall[c]) continue;
-        uint64_t b = colstart[c], e = colstart[c + 1];
-        for (uint64_t k = b; k < e; k++) {
-            float2 q = pt[k];
-            if (!small_pt(q)) continue;
+        uint64_t b = sscan[colstart[c]], e = sscan[colstart[c + 1]];  // this column's small points
+        for (uint64_t base = b; base < e; base += 32) {
+            uint64_t k = base + lane;
+            bool have = k < e;
+            float2 q = have ? pt[sidx[k]] : make_float2(0.f, 0.f);
             bool dup = false;
-            for (uint64_t j = b; j < k && !dup; j++)
-                if (!drop[j] && small_pt(pt[j]) && pt_eq(pt[j], q)) dup = true;
-            if (dup) drop[k] = 1;
+            // against kept points of earlier chunks (already resolved)
+            for (uint64_t j = b; have && j < base && !dup; j++) {
+                uint32_t pj = sidx[j];
+                if (!drop[pj] && pt_eq(pt[pj], q)) dup = true;
+            }
+            // within the chunk, in order
+            for (int i = 0; i < 32; i++) {
+                bool di = __shfl_sync(0xffffffffu, dup, i);
+                float2 qi = make_float2(__shfl_sync(0xffffffffu, q.x, i), __shfl_sync(0xffffffffu, q.y, i));
+                bool hi = __shfl_sync(0xffffffffu, have, i);
+                // a kept point i knocks out later equal points of the chunk
+                if (hi && !di && lane > i && have && !dup && pt_eq(qi, q)) dup = true;
+            }
+            if (have && dup) drop[sidx[k]] = 1;
+            __syncwarp();
         }
+    }
+}
+
+__global__ void k_cp_sizes(const uint64_t *__restrict__ colstart, const uint64_t *__restrict__ keptscan, uint64_t ncol,
+                           uint64_t *__restrict__ cpsize) {
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncol; c += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t nk = keptscan[colstart[c + 1]] - keptscan[colstart[c]];
+        cpsize[c] = nk ? nk + 1 : 0;
     }
 }
 
@@ -906,27 +1005,18 @@ __global__ void k_col_polys(const uint64_t *__restrict__ colkey, const float2 *_
     }
 }
 
-__global__ void k_cp_sizes(const uint64_t *__restrict__ colstart, const uint8_t *__restrict__ drop_unused,
-                           const uint64_t *__restrict__ keptscan, uint64_t ncol, uint64_t *__restrict__ cpsize) {
-    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncol; c += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t nk = keptscan[colstart[c + 1]] - keptscan[colstart[c]];
-        cpsize[c] = nk ? nk + 1 : 0;
-    }
-}
-
 // Per column-polygon edge: points contributed to each row (count or emit).
-__global__ void k_clipy(const PolyHdr *__restrict__ hdr, uint32_t npoly, const uint64_t *__restrict__ colbase,
-                        const uint64_t *__restrict__ cpstart, uint64_t ncol, const float2 *__restrict__ cpoly,
-                        uint64_t ncp, const double *__restrict__ rowy, uint32_t *__restrict__ cnt,
-                        const uint64_t *__restrict__ scan, uint64_t *__restrict__ okey, float2 *__restrict__ opt,
-                        uint32_t *__restrict__ cellcnt) {
+__global__ void k_clipy(const PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ colbase, Chunk ch,
+                        const uint64_t *__restrict__ cpstart, const float2 *__restrict__ cpoly, uint64_t ncp,
+                        const double *__restrict__ rowy, uint32_t *__restrict__ cnt, const uint64_t *__restrict__ scan,
+                        uint64_t *__restrict__ okey, float2 *__restrict__ opt, uint32_t *__restrict__ cellcnt) {
     for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < ncp; j += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t c = find_segment(cpstart, (uint32_t)ncol, j);
+        uint64_t c = find_segment(cpstart, (uint32_t)ch.ncol, j);
         uint32_t total = 0;
         if (j + 1 < cpstart[c + 1]) {
-            uint32_t p = find_segment(colbase, npoly, c);
+            uint32_t p = ch.p0 + find_segment(colbase + ch.p0, ch.np, c + ch.col0);
             const PolyHdr &h = hdr[p];
-            int x = (int)(c - h.col);
+            int x = (int)(c + ch.col0 - h.col);
             float2 A = cpoly[j], B = cpoly[j + 1];
             double mny = A.y < B.y ? A.y : B.y, mxy = A.y < B.y ? B.y : A.y;
             double mg = fmargin(mny, mxy);
@@ -938,7 +1028,7 @@ __global__ void k_clipy(const PolyHdr *__restrict__ hdr, uint32_t npoly, const u
                 double Yi = lines[r], Yi1 = Yi + h.step_y;
                 int k = clip_y_points(A, B, Yi, Yi1, okey ? buf : nullptr);
                 if (okey && k) {
-                    uint64_t cell = h.pix + (uint64_t)r * h.dimx + x;
+                    uint64_t cell = (h.pix - ch.pix0) + (uint64_t)r * h.dimx + x;
                     for (int q = 0; q < k; q++) {
                         okey[at] = cell;
                         opt[at] = buf[q];
@@ -955,18 +1045,19 @@ __global__ void k_clipy(const PolyHdr *__restrict__ hdr, uint32_t npoly, const u
 
 // Per pixel: cell area (geometry_computation.h:275-297 over the cell's clip,
 // closed as Ideal.cpp:805-808 does) and the fill class (Ideal.cpp:880-914).
-__global__ void k_cells(PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ pixbase, uint32_t npoly, uint64_t totP,
+__global__ void k_cells(PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ pixbase, Chunk ch,
                         const uint64_t *__restrict__ cellstart, const float2 *__restrict__ cpt,
                         const uint64_t *__restrict__ cpstart, uint8_t *__restrict__ status,
                         double *__restrict__ areas, int cc) {
-    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < totP; g += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t p = find_segment(pixbase, npoly, g);
+    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ch.npix;
+         g += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t p = ch.p0 + find_segment(pixbase + ch.p0, ch.np, g + ch.pix0);
         const PolyHdr &h = hdr[p];
         if (h.err) continue;
-        uint32_t id = (uint32_t)(g - h.pix);
+        uint32_t id = (uint32_t)(g + ch.pix0 - h.pix);
         int x = (int)(id % (uint32_t)h.dimx), y = (int)(id / (uint32_t)h.dimx);
         if (x >= h.ncols || y >= h.nrows) continue;
-        uint64_t cidx = h.col + (uint64_t)x;
+        uint64_t cidx = h.col - ch.col0 + (uint64_t)x;
         if (cpstart[cidx + 1] == cpstart[cidx]) continue;  // empty column: not visited
         uint64_t b = cellstart[g], e = cellstart[g + 1];
         uint64_t n = e - b;
@@ -988,13 +1079,13 @@ __global__ void k_cells(PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ 
         if (raw == 1) {
             int t = type < cc - 2 ? type : cc - 2;
             *st = (uint8_t)(t > 1 ? t : 1);
-            areas[g] = area;
+            areas[h.pix + id] = area;
         } else if (raw == 2) {
             *st = (uint8_t)(cc - 1);
-            areas[g] = pa;
+            areas[h.pix + id] = pa;
         } else {
             *st = 0;
-            areas[g] = 0.0;
+            areas[h.pix + id] = 0.0;
         }
     }
 }
@@ -1003,21 +1094,20 @@ __global__ void k_cells(PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ 
 // Ideal.cpp:1008-1059: each coarse pixel sums the finest areas under it. The
 // reference leaves merge_area's status argument uninitialised; compiled, it
 // carries over from the previous coarse pixel (x outer, y inner), so once a
-// BORDER is seen the rest of the layer is classified as BORDER. Pass 1 finds
-// the first such pixel per layer; pass 2 classifies.
-__global__ void k_merge(const PolyHdr *__restrict__ hdr, uint32_t npoly, uint8_t *__restrict__ status,
-                        const double *__restrict__ areas, int cc, int pass, uint32_t *__restrict__ firstb,
-                        const uint64_t *__restrict__ lbase) {
+// BORDER is seen the rest of the layer is classified as BORDER. Pass 0 finds
+// the first such pixel per layer; pass 1 classifies.
+__global__ void k_merge(const PolyHdr *__restrict__ hdr, Chunk ch, uint8_t *__restrict__ status,
+                        const double *__restrict__ areas, int cc, int pass, uint32_t *__restrict__ firstb) {
     uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t p = warp; p < npoly; p += nw) {
-        const PolyHdr &h = hdr[p];
+    for (uint32_t q = warp; q < ch.np; q += nw) {
+        const PolyHdr &h = hdr[ch.p0 + q];
         if (h.err || h.num_layers < 2) continue;
         for (int li = (int)h.num_layers - 2; li >= 0; li--) {
             LayerGeom g;
             layer_geom(h, (uint32_t)li, g);
-            uint32_t *fb = firstb + lbase[p] + li;
+            uint32_t *fb = firstb + 32ull * q + li;
             uint32_t np = (uint32_t)(g.dimx * g.dimy);
             for (uint32_t k = lane; k < np; k += 32) {
                 int x = (int)(k / (uint32_t)g.dimy), y = (int)(k % (uint32_t)g.dimy);  // x outer
@@ -1051,11 +1141,6 @@ __global__ void k_merge(const PolyHdr *__restrict__ hdr, uint32_t npoly, uint8_t
     }
 }
 
-__global__ void k_layer_count(const PolyHdr *__restrict__ hdr, uint32_t npoly, uint64_t *__restrict__ cnt) {
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npoly; p += gridDim.x * blockDim.x)
-        cnt[p] = hdr[p].num_layers;
-}
-
 __global__ void k_fill_u32(uint32_t *a, uint64_t n, uint32_t v) {
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
         a[k] = v;
@@ -1083,12 +1168,6 @@ __global__ void k_gather_u64(const uint64_t *src, const uint32_t *idx, uint64_t 
 
 // ------------------------------------------------------------ host ----
 
-struct Launch {
-    cudaStream_t st;
-    int blocks_cap;
-    int count = 0;
-};
-
 template <typename F>
 static int cub_call(farm_store *s, F f) {
     size_t bytes = 0;
@@ -1098,7 +1177,6 @@ static int cub_call(farm_store *s, F f) {
     return FARM_OK;
 }
 
-// exclusive scan of n u64 values into out (n entries); returns total via host copy of out[n-1]+in[n-1]
 static int excl_scan(farm_store *s, const uint64_t *in, uint64_t *out, uint64_t n) {
     if (n == 0) return FARM_OK;
     return cub_call(s, [&](void *t, size_t &b) {
@@ -1106,8 +1184,8 @@ static int excl_scan(farm_store *s, const uint64_t *in, uint64_t *out, uint64_t 
     });
 }
 
-static int d2h_u64(farm_store *s, const uint64_t *d, uint64_t &v) {
-    FARM_CUDA(cudaMemcpyAsync(&v, d, 8, cudaMemcpyDeviceToHost, s->stream));
+static int d2h(farm_store *s, void *h, const void *d, size_t bytes) {
+    FARM_CUDA(cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, s->stream));
     FARM_CUDA(cudaStreamSynchronize(s->stream));
     return FARM_OK;
 }
@@ -1133,8 +1211,307 @@ static unsigned gb(uint64_t n) {
     return (unsigned)(g ? g : 1);
 }
 
+// scratch budget per chunk (crossings and edges bound the sizes of every
+// intermediate array)
+// (FARM_CHUNK_EDGES / FARM_CHUNK_CROSS / FARM_CHUNK_PIX override them, e.g. to
+// exercise many small chunks in tests)
+static uint64_t env_u64(const char *name, uint64_t dflt) {
+    const char *v = getenv(name);
+    if (!v || !*v) return dflt;
+    unsigned long long x = strtoull(v, nullptr, 10);
+    return x ? (uint64_t)x : dflt;
+}
+
+struct RasterCtx {
+    farm_store *s;
+    uint32_t np;
+    uint64_t n1;
+    PolyHdr *hdr;
+    const uint64_t *doff;
+    const uint64_t *scan;  // per polygon bases (pix, st, off, hline, vline, col, row, scanrow)
+    double *colx, *rowy;
+    int cc;
+    int launches = 0;
+};
+
+static int raster_chunk(RasterCtx &R, const Chunk &ch) {
+    farm_store *s = R.s;
+    cudaStream_t st = s->stream;
+    int &L = R.launches;
+    StoreView sv = s->view();
+    sv.category_count = R.cc;
+    const uint64_t *pixbase = R.scan + 0 * R.n1, *colbase = R.scan + 5 * R.n1, *rowbase = R.scan + 7 * R.n1;
+    const uint64_t ne = ch.ne, ne1 = ne + 1;
+
+    // ---- edge walk: count, scan, fill
+    FARM_TRY(s->s[S_CNT_E].ensure(3 * ne1 * 4 + 16));
+    FARM_TRY(s->s[S_TMP_A].ensure(3 * ne1 * 8 + 16));
+    FARM_TRY(s->s[S_SCAN_E].ensure(3 * ne1 * 8 + 16));
+    uint32_t *ecnt = s->s[S_CNT_E].as<uint32_t>();
+    FARM_CUDA(cudaMemsetAsync(ecnt, 0, 3 * ne1 * 4, st));
+    k_walk_count<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, ecnt);
+    uint64_t *ecnt64 = s->s[S_TMP_A].as<uint64_t>(), *escan = s->s[S_SCAN_E].as<uint64_t>();
+    k_u32_to_u64<<<gb(3 * ne1), 256, 0, st>>>(ecnt, 3 * ne1, ecnt64);
+    L += 2;
+    for (int t = 0; t < 3; t++) FARM_TRY(excl_scan(s, ecnt64 + t * ne1, escan + t * ne1, ne1));
+    uint64_t nC, nH, nV;
+    FARM_TRY(d2h(s, &nC, escan + ne, 8));
+    FARM_TRY(d2h(s, &nH, escan + ne1 + ne, 8));
+    FARM_TRY(d2h(s, &nV, escan + 2 * ne1 + ne, 8));
+    FARM_TRY(s->s[S_CFROM].ensure(4 * nC + 16));
+    FARM_TRY(s->s[S_CTO].ensure(4 * nC + 16));
+    FARM_TRY(s->s[S_CEDGE].ensure(4 * nC + 16));
+    FARM_TRY(s->s[S_HKEY].ensure(8 * nH + 16));
+    FARM_TRY(s->s[S_HVAL].ensure(8 * nH + 16));
+    FARM_TRY(s->s[S_VNKEY].ensure(8 * nV + 16));
+    FARM_TRY(s->s[S_VNVAL].ensure(8 * nV + 16));
+    uint32_t *cfrom = s->s[S_CFROM].as<uint32_t>(), *cto = s->s[S_CTO].as<uint32_t>(),
+             *cedge = s->s[S_CEDGE].as<uint32_t>();
+    k_walk_fill<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, escan, cfrom, cto, cedge, s->s[S_HKEY].as<uint64_t>(),
+                                        s->s[S_HVAL].as<double>(), s->s[S_VNKEY].as<uint64_t>(),
+                                        s->s[S_VNVAL].as<double>());
+    L++;
+
+    // ---- visits -> edge sequences (process_crosses)
+    const uint64_t cn1 = (uint64_t)ch.np + 1;
+    FARM_TRY(s->s[S_TMP_B].ensure(cn1 * 8 + 16));
+    uint64_t *cbase = s->s[S_TMP_B].as<uint64_t>();
+    k_cross_base<<<gb(cn1), 256, 0, st>>>(R.doff, ch, escan, cbase);
+    L++;
+    FARM_TRY(s->s[S_VKEY].ensure(8 * nC + 16));
+    FARM_TRY(s->s[S_VVAL].ensure(8 * nC + 16));
+    FARM_TRY(s->s[S_VKEY2].ensure(8 * nC + 16));
+    FARM_TRY(s->s[S_VVAL2].ensure(8 * nC + 16));
+    uint64_t *vkey = s->s[S_VKEY].as<uint64_t>(), *vval = s->s[S_VVAL].as<uint64_t>();
+    uint64_t *vkey2 = s->s[S_VKEY2].as<uint64_t>(), *vval2 = s->s[S_VVAL2].as<uint64_t>();
+    if (nC) {
+        k_visits<<<gb(nC), 256, 0, st>>>(R.hdr, ch, cbase, nC, cfrom, cto, cedge, vkey, vval);
+        L++;
+        FARM_TRY(sort_pairs(s, vkey, vkey2, vval, vval2, nC, key_bits(ch.npix)));
+    }
+    FARM_TRY(s->s[S_PIXCNT].ensure(4 * (ch.npix + 1) + 16));
+    uint32_t *pixcnt = s->s[S_PIXCNT].as<uint32_t>();
+    FARM_CUDA(cudaMemsetAsync(pixcnt, 0, 4 * (ch.npix + 1), st));
+    FARM_TRY(s->s[S_SEQW].ensure(2 * 8 * (nC + 1) + 16));
+    uint64_t *w = s->s[S_SEQW].as<uint64_t>(), *wscan = w + nC + 1;
+    uint2 *seq = s->d_seq.as<uint2>();
+    if (nC) {
+        k_seq_width<<<gb(nC), 256, 0, st>>>(vkey2, vval2, nC, w, pixcnt);
+        FARM_TRY(excl_scan(s, w, wscan, nC + 1));
+        k_seq_fill<<<gb(nC), 256, 0, st>>>(R.hdr, ch, cbase, vval2, wscan, nC, seq);
+        L += 2;
+    }
+    k_seq_single<<<gb(ch.np), 256, 0, st>>>(R.hdr, ch, cbase, seq, pixcnt);
+    L++;
+    {
+        FARM_TRY(s->s[S_TMP_A].ensure(8 * (ch.npix + 1) + 16));
+        uint64_t *p64 = s->s[S_TMP_A].as<uint64_t>();
+        k_u32_to_u64<<<gb(ch.npix + 1), 256, 0, st>>>(pixcnt, ch.npix + 1, p64);
+        FARM_TRY(s->s[S_PIXSCAN].ensure(8 * (ch.npix + 1) + 16));
+        uint64_t *pscan = s->s[S_PIXSCAN].as<uint64_t>();
+        FARM_TRY(excl_scan(s, p64, pscan, ch.npix + 1));
+        k_offsets<<<gb(ch.npix), 256, 0, st>>>(R.hdr, pixbase, ch, pscan, s->d_offset.as<uint32_t>());
+        L += 2;
+    }
+
+    // ---- grid lines (process_intersection)
+    for (int vert = 0; vert < 2; vert++) {
+        uint64_t nn = vert ? nV : nH;
+        uint64_t nl = vert ? ch.nvl : ch.nh;
+        const uint64_t *key = vert ? s->s[S_VNKEY].as<uint64_t>() : s->s[S_HKEY].as<uint64_t>();
+        const double *val = vert ? s->s[S_VNVAL].as<double>() : s->s[S_HVAL].as<double>();
+        double *nodes_out = (vert ? s->d_vnodes.as<double>() : s->d_hnodes.as<double>()) + (vert ? ch.vn0 : ch.hn0);
+        FARM_TRY(s->s[S_LINECNT].ensure(2 * 4 * (nl + 1) + 16));
+        FARM_TRY(s->s[S_LINESCAN].ensure(2 * 8 * (nl + 1) + 16));
+        uint32_t *lcnt = s->s[S_LINECNT].as<uint32_t>(), *lfill = lcnt + (nl + 1);
+        uint64_t *lc64 = s->s[S_LINESCAN].as<uint64_t>(), *lstart = lc64 + (nl + 1);
+        FARM_CUDA(cudaMemsetAsync(lcnt, 0, 2 * 4 * (nl + 1), st));
+        if (nn) {
+            k_line_count<<<gb(nn), 256, 0, st>>>(key, nn, lcnt);
+            L++;
+        }
+        k_u32_to_u64<<<gb(nl + 1), 256, 0, st>>>(lcnt, nl + 1, lc64);
+        L++;
+        FARM_TRY(excl_scan(s, lc64, lstart, nl + 1));
+        FARM_TRY(s->s[S_TMP_B].ensure(8 * nn + 16));
+        double *unsorted = s->s[S_TMP_B].as<double>();
+        if (nn) {
+            k_line_scatter<<<gb(nn), 256, 0, st>>>(key, val, nn, lstart, lfill, unsorted);
+            L++;
+            FARM_TRY(cub_call(s, [&](void *t, size_t &b) {
+                return cub::DeviceSegmentedSort::SortKeys(t, b, unsorted, nodes_out, (int64_t)nn, (int64_t)nl, lstart,
+                                                          lstart + 1, st);
+            }));
+        }
+        k_line_offsets<<<gb(ch.np), 256, 0, st>>>(R.hdr, ch, vert, lcnt, lstart,
+                                                  vert ? s->d_voff.as<uint32_t>() : s->d_hoff.as<uint32_t>());
+        L++;
+    }
+
+    // ---- scanline
+    k_scanline<<<gb(ch.nrow), 256, 0, st>>>(R.hdr, rowbase, ch, s->d_status.as<uint8_t>(), s->d_hoff.as<uint32_t>(),
+                                            s->d_hnodes.as<double>(), R.cc);
+    L++;
+
+    // ---- fill: strip clip per column
+    FARM_TRY(s->s[S_CNT_E].ensure(4 * ne1 + 16));
+    uint32_t *xcnt = s->s[S_CNT_E].as<uint32_t>();
+    FARM_CUDA(cudaMemsetAsync(xcnt, 0, 4 * ne1, st));
+    k_clipx<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, R.colx, xcnt, nullptr, nullptr, nullptr);
+    FARM_TRY(s->s[S_TMP_A].ensure(8 * ne1 + 16));
+    uint64_t *x64 = s->s[S_TMP_A].as<uint64_t>();
+    k_u32_to_u64<<<gb(ne1), 256, 0, st>>>(xcnt, ne1, x64);
+    L += 2;
+    FARM_TRY(s->s[S_SCAN_E].ensure(8 * ne1 + 16));
+    uint64_t *xscan = s->s[S_SCAN_E].as<uint64_t>();
+    FARM_TRY(excl_scan(s, x64, xscan, ne1));
+    uint64_t nX;
+    FARM_TRY(d2h(s, &nX, xscan + ne, 8));
+    FARM_TRY(s->s[S_VKEY].ensure(8 * nX + 16));
+    FARM_TRY(s->s[S_VVAL].ensure(8 * nX + 16));
+    FARM_TRY(s->s[S_VKEY2].ensure(8 * nX + 16));
+    FARM_TRY(s->s[S_VVAL2].ensure(8 * nX + 16));
+    uint64_t *xkey = s->s[S_VKEY].as<uint64_t>(), *xkey_s = s->s[S_VKEY2].as<uint64_t>();
+    float2 *xpt = s->s[S_VVAL].as<float2>(), *xpt_s = s->s[S_VVAL2].as<float2>();
+    const int colbits = key_bits(ch.ncol);
+    if (nX) {
+        k_clipx<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, R.colx, nullptr, xscan, xkey, xpt);
+        L++;
+        FARM_TRY(sort_pairs(s, xkey, xkey_s, reinterpret_cast<uint64_t *>(xpt), reinterpret_cast<uint64_t *>(xpt_s),
+                            nX, colbits));
+    }
+    // duplicates: sort (bits, position), then stable by column
+    FARM_TRY(s->s[S_HKEY].ensure(8 * nX + 16));
+    FARM_TRY(s->s[S_HVAL].ensure(8 * nX + 16));
+    FARM_TRY(s->s[S_VNKEY].ensure(8 * nX + 16));
+    FARM_TRY(s->s[S_VNVAL].ensure(8 * nX + 16));
+    FARM_TRY(s->s[S_CFROM].ensure(4 * nX + 16));
+    FARM_TRY(s->s[S_CTO].ensure(4 * nX + 16));
+    FARM_TRY(s->s[S_CEDGE].ensure(4 * nX + 16));
+    FARM_TRY(s->s[S_SEQW].ensure(nX + 32 + 8 * (nX + 1) * 2));
+    uint64_t *bits = s->s[S_HKEY].as<uint64_t>(), *bits_s = s->s[S_HVAL].as<uint64_t>();
+    uint64_t *ck = s->s[S_VNKEY].as<uint64_t>(), *ck_s = s->s[S_VNVAL].as<uint64_t>();
+    uint32_t *pos = s->s[S_CFROM].as<uint32_t>(), *pos_s = s->s[S_CTO].as<uint32_t>();
+    uint32_t *pos2 = s->s[S_CEDGE].as<uint32_t>();
+    uint8_t *drop = s->s[S_SEQW].as<uint8_t>();
+    uint64_t *keptscan = reinterpret_cast<uint64_t *>(drop + ((nX + 16 + 7) & ~7ull));
+    uint64_t *kept64 = keptscan + (nX + 1);
+    FARM_CUDA(cudaMemsetAsync(drop, 0, nX + 1, st));
+    if (nX) {
+        k_ptbits<<<gb(nX), 256, 0, st>>>(xpt_s, nX, bits, pos);
+        L++;
+        FARM_TRY(sort_pairs(s, bits, bits_s, pos, pos_s, nX, 64));
+        k_gather_u64<<<gb(nX), 256, 0, st>>>(xkey_s, pos_s, nX, ck);
+        L++;
+        FARM_TRY(sort_pairs(s, ck, ck_s, pos_s, pos2, nX, colbits));
+        k_dup_large<<<gb(nX), 256, 0, st>>>(ck_s, pos2, xpt_s, nX, drop);
+        L++;
+    }
+    // column starts and small-point columns
+    const uint64_t ncol = ch.ncol;
+    FARM_TRY(s->s[S_LINECNT].ensure(4 * (ncol + 1) + (ncol + 1) + 16));
+    FARM_TRY(s->s[S_LINESCAN].ensure(8 * (ncol + 1) * 2 + 16));
+    uint32_t *colcnt = s->s[S_LINECNT].as<uint32_t>();
+    uint8_t *colsmall = reinterpret_cast<uint8_t *>(colcnt + (ncol + 1));
+    uint64_t *cc64 = s->s[S_LINESCAN].as<uint64_t>(), *colstart = cc64 + (ncol + 1);
+    FARM_CUDA(cudaMemsetAsync(colcnt, 0, 4 * (ncol + 1) + (ncol + 1), st));
+    if (nX) {
+        k_col_count<<<gb(nX), 256, 0, st>>>(xkey_s, xpt_s, nX, colcnt, colsmall);
+        L++;
+    }
+    k_u32_to_u64<<<gb(ncol + 1), 256, 0, st>>>(colcnt, ncol + 1, cc64);
+    L++;
+    FARM_TRY(excl_scan(s, cc64, colstart, ncol + 1));
+    {
+        // small points: flag, compact (column order), then one warp per column
+        FARM_TRY(s->s[S_SMALL].ensure(8 * (nX + 1) * 2 + 4 * nX + 32));
+        uint64_t *sflag = s->s[S_SMALL].as<uint64_t>(), *sscan = sflag + (nX + 1);
+        uint32_t *sidx = reinterpret_cast<uint32_t *>(sscan + (nX + 1));
+        FARM_CUDA(cudaMemsetAsync(sflag + nX, 0, 8, st));
+        k_small_flags<<<gb(nX), 256, 0, st>>>(xpt_s, nX, sflag);
+        L++;
+        FARM_TRY(excl_scan(s, sflag, sscan, nX + 1));
+        k_small_compact<<<gb(nX), 256, 0, st>>>(xpt_s, nX, sscan, sidx);
+        k_dup_small<<<gb(32ull * ncol), 256, 0, st>>>(colstart, ncol, colsmall, sscan, sidx, xpt_s, drop);
+        L += 2;
+    }
+    k_not_u8<<<gb(nX + 1), 256, 0, st>>>(drop, nX + 1, kept64);
+    L++;
+    FARM_TRY(excl_scan(s, kept64, keptscan, nX + 1));
+    FARM_TRY(s->s[S_PIXSCAN].ensure(8 * (ncol + 1) * 2 + 16));
+    uint64_t *cpsize = s->s[S_PIXSCAN].as<uint64_t>(), *cpstart = cpsize + (ncol + 1);
+    FARM_CUDA(cudaMemsetAsync(cpsize, 0, 8 * (ncol + 1), st));
+    k_cp_sizes<<<gb(ncol), 256, 0, st>>>(colstart, keptscan, ncol, cpsize);
+    L++;
+    FARM_TRY(excl_scan(s, cpsize, cpstart, ncol + 1));
+    uint64_t nCP;
+    FARM_TRY(d2h(s, &nCP, cpstart + ncol, 8));
+    FARM_TRY(s->s[S_CPOLY].ensure(8 * nCP + 16));
+    float2 *cpoly = s->s[S_CPOLY].as<float2>();
+    if (nX) {
+        k_col_polys<<<gb(nX), 256, 0, st>>>(xkey_s, xpt_s, drop, keptscan, nX, colstart, cpstart, cpoly);
+        L++;
+    }
+
+    // ---- fill: cell clip per row
+    FARM_TRY(s->s[S_CNT_E].ensure(4 * (nCP + 1) + 16));
+    uint32_t *ycnt = s->s[S_CNT_E].as<uint32_t>();
+    FARM_CUDA(cudaMemsetAsync(ycnt, 0, 4 * (nCP + 1), st));
+    FARM_TRY(s->s[S_PIXCNT].ensure(4 * (ch.npix + 1) + 16));
+    uint32_t *cellcnt = s->s[S_PIXCNT].as<uint32_t>();
+    FARM_CUDA(cudaMemsetAsync(cellcnt, 0, 4 * (ch.npix + 1), st));
+    if (nCP) {
+        k_clipy<<<gb(nCP), 256, 0, st>>>(R.hdr, colbase, ch, cpstart, cpoly, nCP, R.rowy, ycnt, nullptr, nullptr,
+                                         nullptr, nullptr);
+        L++;
+    }
+    FARM_TRY(s->s[S_TMP_A].ensure(8 * (nCP + 1) + 16));
+    uint64_t *y64 = s->s[S_TMP_A].as<uint64_t>();
+    k_u32_to_u64<<<gb(nCP + 1), 256, 0, st>>>(ycnt, nCP + 1, y64);
+    L++;
+    FARM_TRY(s->s[S_SCAN_E].ensure(8 * (nCP + 1) + 16));
+    uint64_t *yscan = s->s[S_SCAN_E].as<uint64_t>();
+    FARM_TRY(excl_scan(s, y64, yscan, nCP + 1));
+    uint64_t nY;
+    FARM_TRY(d2h(s, &nY, yscan + nCP, 8));
+    FARM_TRY(s->s[S_VKEY].ensure(8 * nY + 16));
+    FARM_TRY(s->s[S_VVAL].ensure(8 * nY + 16));
+    FARM_TRY(s->s[S_HKEY].ensure(8 * nY + 16));
+    FARM_TRY(s->s[S_HVAL].ensure(8 * nY + 16));
+    uint64_t *ykb = s->s[S_VKEY].as<uint64_t>(), *yks = s->s[S_HKEY].as<uint64_t>();
+    float2 *ypb = s->s[S_VVAL].as<float2>(), *yps = s->s[S_HVAL].as<float2>();
+    if (nY) {
+        k_clipy<<<gb(nCP), 256, 0, st>>>(R.hdr, colbase, ch, cpstart, cpoly, nCP, R.rowy, nullptr, yscan, ykb, ypb,
+                                         cellcnt);
+        L++;
+        FARM_TRY(sort_pairs(s, ykb, yks, reinterpret_cast<uint64_t *>(ypb), reinterpret_cast<uint64_t *>(yps), nY,
+                            key_bits(ch.npix)));
+    }
+    FARM_TRY(s->s[S_TMP_A].ensure(8 * (ch.npix + 1) * 2 + 16));
+    uint64_t *c64 = s->s[S_TMP_A].as<uint64_t>(), *cellstart = c64 + (ch.npix + 1);
+    k_u32_to_u64<<<gb(ch.npix + 1), 256, 0, st>>>(cellcnt, ch.npix + 1, c64);
+    L++;
+    FARM_TRY(excl_scan(s, c64, cellstart, ch.npix + 1));
+    k_cells<<<gb(ch.npix), 256, 0, st>>>(R.hdr, pixbase, ch, cellstart, yps, cpstart, s->d_status.as<uint8_t>(),
+                                         s->d_areas.as<double>(), R.cc);
+    L++;
+
+    // ---- hierarchy
+    if (s->ropts.hierarchy) {
+        FARM_TRY(s->s[S_TMP_B].ensure(4ull * 32 * ch.np + 16));
+        uint32_t *fb = s->s[S_TMP_B].as<uint32_t>();
+        k_fill_u32<<<gb(32ull * ch.np), 256, 0, st>>>(fb, 32ull * ch.np, 0xFFFFFFFFu);
+        k_merge<<<gb(32ull * ch.np), 256, 0, st>>>(R.hdr, ch, s->d_status.as<uint8_t>(), s->d_areas.as<double>(), R.cc,
+                                                  0, fb);
+        k_merge<<<gb(32ull * ch.np), 256, 0, st>>>(R.hdr, ch, s->d_status.as<uint8_t>(), s->d_areas.as<double>(), R.cc,
+                                                  1, fb);
+        L += 3;
+    }
+    FARM_CUDA(cudaGetLastError());
+    return FARM_OK;
+}
+
 int rasterize(farm_store *s, const farm_raster_opts *o, int *launches) {
-    int L = 0;
     uint32_t np = (uint32_t)s->n_poly;
     uint64_t ne = s->n_edges;
     if (np == 0) {
@@ -1153,26 +1530,31 @@ int rasterize(farm_store *s, const farm_raster_opts *o, int *launches) {
         int power = 2 - (int)d;
         double magnitude = pow(10.0, power);
         rp.gstep = round(num * magnitude) / magnitude;
-        for (int k = 0; k < 40; k++) rp.pow2_ceil[k] = (int)ceil(log((double)(1ull << (k < 62 ? k : 62))) / log(2.0));
+        for (int k = 0; k < 40; k++) rp.pow2_ceil[k] = (int)ceil(log((double)(1ull << k)) / log(2.0));
     }
     cudaStream_t st = s->stream;
-    const uint64_t *doff = s->d_off.as<uint64_t>();
-    uint64_t n1 = (uint64_t)np + 1;
+    RasterCtx R;
+    R.s = s;
+    R.np = np;
+    R.n1 = (uint64_t)np + 1;
+    R.cc = o->category_count;
+    R.doff = s->d_off.as<uint64_t>();
+    const uint64_t n1 = R.n1;
     FARM_TRY(s->d_hdr.ensure(sizeof(PolyHdr) * np));
     FARM_TRY(s->s[S_SIZES].ensure(9 * n1 * 8));
     FARM_TRY(s->s[S_SCAN].ensure(9 * n1 * 8));
     FARM_CUDA(cudaMemsetAsync(s->s[S_SIZES].p, 0, 9 * n1 * 8, st));
-    PolyHdr *hdr = s->d_hdr.as<PolyHdr>();
+    R.hdr = s->d_hdr.as<PolyHdr>();
     uint64_t *sizes = s->s[S_SIZES].as<uint64_t>(), *scan = s->s[S_SCAN].as<uint64_t>();
-    k_header<<<gb(32ull * np), 256, 0, st>>>(s->d_ring.as<float2>(), doff, np, rp, hdr, sizes);
-    L++;
+    R.scan = scan;
+    k_header<<<gb(32ull * np), 256, 0, st>>>(s->d_ring.as<float2>(), R.doff, np, rp, R.hdr, sizes);
+    R.launches++;
     for (int t = 0; t < 8; t++) FARM_TRY(excl_scan(s, sizes + t * n1, scan + t * n1, n1));
     uint64_t tot[8];
-    FARM_CUDA(cudaMemcpyAsync(tot, scan, 8, cudaMemcpyDeviceToHost, st));
     for (int t = 0; t < 8; t++) FARM_CUDA(cudaMemcpyAsync(&tot[t], scan + t * n1 + np, 8, cudaMemcpyDeviceToHost, st));
     FARM_CUDA(cudaStreamSynchronize(st));
     const uint64_t totP = tot[0], totStatus = tot[1], totOff = tot[2], totH = tot[3], totV = tot[4], totCol = tot[5],
-                   totRow = tot[6], totScanRows = tot[7];
+                   totRow = tot[6];
     FARM_TRY(s->d_status.ensure(totStatus + 16));
     FARM_TRY(s->d_offset.ensure(4 * totOff + 16));
     FARM_TRY(s->d_areas.ensure(8 * totP + 16));
@@ -1182,317 +1564,98 @@ int rasterize(farm_store *s, const farm_raster_opts *o, int *launches) {
     FARM_TRY(s->s[S_ROWY].ensure(8 * totRow + 16));
     FARM_CUDA(cudaMemsetAsync(s->d_status.p, 0, totStatus + 16, st));
     FARM_CUDA(cudaMemsetAsync(s->d_areas.p, 0, 8 * totP + 16, st));
-    double *colx = s->s[S_COLX].as<double>(), *rowy = s->s[S_ROWY].as<double>();
-    k_bases<<<gb(np), 256, 0, st>>>(hdr, np, scan, colx, rowy);
-    L++;
-    StoreView sv = s->view();
-    sv.category_count = o->category_count;
+    FARM_CUDA(cudaMemsetAsync(s->d_offset.p, 0, 4 * totOff + 16, st));
+    FARM_CUDA(cudaMemsetAsync(s->d_hoff.p, 0, 4 * totH + 16, st));
+    FARM_CUDA(cudaMemsetAsync(s->d_voff.p, 0, 4 * totV + 16, st));
+    R.colx = s->s[S_COLX].as<double>();
+    R.rowy = s->s[S_ROWY].as<double>();
+    k_bases<<<gb(np), 256, 0, st>>>(R.hdr, np, scan, R.colx, R.rowy);
+    R.launches++;
 
-    // ---- edge walk: count, scan, fill
-    uint64_t ne1 = ne + 1;
-    FARM_TRY(s->s[S_CNT_E].ensure(3 * ne1 * 4 + 16));
-    FARM_TRY(s->s[S_TMP_A].ensure(3 * ne1 * 8 + 16));
-    FARM_TRY(s->s[S_SCAN_E].ensure(3 * ne1 * 8 + 16));
-    uint32_t *ecnt = s->s[S_CNT_E].as<uint32_t>();
-    FARM_CUDA(cudaMemsetAsync(ecnt, 0, 3 * ne1 * 4, st));
-    k_walk_count<<<gb(ne), 256, 0, st>>>(sv, hdr, doff, np, ne, ecnt);
-    L++;
-    uint64_t *ecnt64 = s->s[S_TMP_A].as<uint64_t>(), *escan = s->s[S_SCAN_E].as<uint64_t>();
-    k_u32_to_u64<<<gb(3 * ne1), 256, 0, st>>>(ecnt, 3 * ne1, ecnt64);
-    L++;
-    for (int t = 0; t < 3; t++) FARM_TRY(excl_scan(s, ecnt64 + t * ne1, escan + t * ne1, ne1));
-    uint64_t nC, nH, nV;
-    FARM_TRY(d2h_u64(s, escan + ne, nC));
-    FARM_TRY(d2h_u64(s, escan + ne1 + ne, nH));
-    FARM_TRY(d2h_u64(s, escan + 2 * ne1 + ne, nV));
-    FARM_TRY(s->s[S_CFROM].ensure(4 * nC + 16));
-    FARM_TRY(s->s[S_CTO].ensure(4 * nC + 16));
-    FARM_TRY(s->s[S_CEDGE].ensure(4 * nC + 16));
-    FARM_TRY(s->s[S_HKEY].ensure(8 * nH + 16));
-    FARM_TRY(s->s[S_HVAL].ensure(8 * nH + 16));
-    FARM_TRY(s->s[S_VNKEY].ensure(8 * nV + 16));
-    FARM_TRY(s->s[S_VNVAL].ensure(8 * nV + 16));
-    uint32_t *cfrom = s->s[S_CFROM].as<uint32_t>(), *cto = s->s[S_CTO].as<uint32_t>(),
-             *cedge = s->s[S_CEDGE].as<uint32_t>();
-    k_walk_fill<<<gb(ne), 256, 0, st>>>(sv, hdr, doff, np, ne, escan, cfrom, cto, cedge, s->s[S_HKEY].as<uint64_t>(),
-                                        s->s[S_HVAL].as<double>(), s->s[S_VNKEY].as<uint64_t>(),
-                                        s->s[S_VNVAL].as<double>());
-    L++;
-
-    // ---- visits -> edge sequences (process_crosses)
-    FARM_TRY(s->s[S_TMP_B].ensure(2 * n1 * 8 + 16));
-    uint64_t *cbase = s->s[S_TMP_B].as<uint64_t>(), *nseq = cbase + n1;
-    k_cross_base<<<gb(n1), 256, 0, st>>>(hdr, doff, np, escan, cbase, nseq);
-    L++;
-    FARM_TRY(s->s[S_VKEY].ensure(8 * nC + 16));
-    FARM_TRY(s->s[S_VVAL].ensure(8 * nC + 16));
-    FARM_TRY(s->s[S_VKEY2].ensure(8 * nC + 16));
-    FARM_TRY(s->s[S_VVAL2].ensure(8 * nC + 16));
-    uint64_t *vkey = s->s[S_VKEY].as<uint64_t>(), *vval = s->s[S_VVAL].as<uint64_t>();
-    uint64_t *vkey2 = s->s[S_VKEY2].as<uint64_t>(), *vval2 = s->s[S_VVAL2].as<uint64_t>();
-    if (nC) {
-        k_visits<<<gb(nC), 256, 0, st>>>(hdr, np, cbase, nC, cfrom, cto, cedge, vkey, vval);
-        L++;
-        FARM_TRY(sort_pairs(s, vkey, vkey2, vval, vval2, nC, key_bits(totP)));
-    }
-    FARM_TRY(s->s[S_PIXCNT].ensure(4 * (totP + 1) + 16));
-    uint32_t *pixcnt = s->s[S_PIXCNT].as<uint32_t>();
-    FARM_CUDA(cudaMemsetAsync(pixcnt, 0, 4 * (totP + 1), st));
-    FARM_TRY(s->s[S_SEQW].ensure(2 * 8 * (nC + 1) + 16));
-    uint64_t *w = s->s[S_SEQW].as<uint64_t>(), *wscan = w + nC + 1;
-    // per polygon sequence bases
-    FARM_TRY(s->s[S_PIXSCAN].ensure(8 * (totP + 1) + 8 * n1 + 16));
-    uint64_t *seqbase = s->s[S_PIXSCAN].as<uint64_t>() + (totP + 1);
-    FARM_TRY(excl_scan(s, nseq, seqbase, n1));
-    uint64_t totSeq;
-    FARM_TRY(d2h_u64(s, seqbase + np, totSeq));
-    FARM_TRY(s->d_seq.ensure(8 * totSeq + 16));
-    uint2 *seq = s->d_seq.as<uint2>();
-    if (nC) {
-        k_seq_width<<<gb(nC), 256, 0, st>>>(vkey2, vval2, nC, w, pixcnt);
-        L++;
-        FARM_TRY(excl_scan(s, w, wscan, nC + 1));
-        k_seq_fill<<<gb(nC), 256, 0, st>>>(hdr, np, cbase, seqbase, vval2, wscan, nC, seq);
-        L++;
-    }
-    k_seq_single<<<gb(np), 256, 0, st>>>(hdr, np, seqbase, cbase, seq, pixcnt);
-    L++;
-    // offsets
+    // ---- phase 1: per-polygon totals size the sequence and node arrays
     {
-        uint64_t *p64 = s->s[S_TMP_A].as<uint64_t>();  // reuse: totP+1 u64 needed
-        FARM_TRY(s->s[S_TMP_A].ensure(8 * (totP + 1) + 16));
-        p64 = s->s[S_TMP_A].as<uint64_t>();
-        k_u32_to_u64<<<gb(totP + 1), 256, 0, st>>>(pixcnt, totP + 1, p64);
-        L++;
-        uint64_t *pscan = s->s[S_PIXSCAN].as<uint64_t>();
-        FARM_TRY(excl_scan(s, p64, pscan, totP + 1));
-        k_offsets<<<gb(totP), 256, 0, st>>>(hdr, scan + 0 * n1, np, totP, pscan, s->d_offset.as<uint32_t>());
-        L++;
+        StoreView sv = s->view();
+        FARM_TRY(s->s[S_TMP_B].ensure(3 * 8 * n1 + 16));
+        unsigned long long *tot3 = s->s[S_TMP_B].as<unsigned long long>();
+        FARM_CUDA(cudaMemsetAsync(tot3, 0, 3 * 8 * n1, st));
+        k_walk_tot<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, np, ne, tot3);
+        FARM_TRY(s->s[S_TMP_A].ensure(2 * 3 * 8 * n1 + 16));
+        uint64_t *sz = s->s[S_TMP_A].as<uint64_t>(), *sc = sz + 3 * n1;
+        k_tot_sizes<<<gb(n1), 256, 0, st>>>(tot3, R.hdr, np, sz);
+        R.launches += 2;
+        for (int t = 0; t < 3; t++) FARM_TRY(excl_scan(s, sz + t * n1, sc + t * n1, n1));
+        k_set_node_bases<<<gb(np), 256, 0, st>>>(R.hdr, np, sz, sc);
+        R.launches++;
+        uint64_t tseq, th, tv;
+        FARM_TRY(d2h(s, &tseq, sc + np, 8));
+        FARM_TRY(d2h(s, &th, sc + n1 + np, 8));
+        FARM_TRY(d2h(s, &tv, sc + 2 * n1 + np, 8));
+        FARM_TRY(s->d_seq.ensure(8 * tseq + 16));
+        FARM_TRY(s->d_hnodes.ensure(8 * th + 16));
+        FARM_TRY(s->d_vnodes.ensure(8 * tv + 16));
+        s->tot_seq = tseq;
     }
 
-    // ---- grid lines (process_intersection)
-    for (int vert = 0; vert < 2; vert++) {
-        uint64_t nn = vert ? nV : nH;
-        uint64_t nl = vert ? totV : totH;
-        const uint64_t *key = vert ? s->s[S_VNKEY].as<uint64_t>() : s->s[S_HKEY].as<uint64_t>();
-        const double *val = vert ? s->s[S_VNVAL].as<double>() : s->s[S_HVAL].as<double>();
-        DevBuf &nodes = vert ? s->d_vnodes : s->d_hnodes;
-        FARM_TRY(nodes.ensure(8 * nn + 16));
-        FARM_TRY(s->s[S_LINECNT].ensure(2 * 4 * (nl + 1) + 16));
-        FARM_TRY(s->s[S_LINESCAN].ensure(2 * 8 * (nl + 1) + 16));
-        uint32_t *lcnt = s->s[S_LINECNT].as<uint32_t>(), *lfill = lcnt + (nl + 1);
-        uint64_t *lc64 = s->s[S_LINESCAN].as<uint64_t>(), *lstart = lc64 + (nl + 1);
-        FARM_CUDA(cudaMemsetAsync(lcnt, 0, 2 * 4 * (nl + 1), st));
-        if (nn) {
-            k_line_count<<<gb(nn), 256, 0, st>>>(key, nn, lcnt);
-            L++;
-        }
-        k_u32_to_u64<<<gb(nl + 1), 256, 0, st>>>(lcnt, nl + 1, lc64);
-        L++;
-        FARM_TRY(excl_scan(s, lc64, lstart, nl + 1));
-        FARM_TRY(s->s[S_TMP_B].ensure(2 * n1 * 8 + 8 * nn + 16));
-        cbase = s->s[S_TMP_B].as<uint64_t>();  // (re-fetched: buffer may have moved)
-        double *unsorted = reinterpret_cast<double *>(cbase + 2 * n1);
-        if (nn) {
-            k_line_scatter<<<gb(nn), 256, 0, st>>>(key, val, nn, lstart, lfill, unsorted);
-            L++;
-            FARM_TRY(cub_call(s, [&](void *t, size_t &b) {
-                return cub::DeviceSegmentedSort::SortKeys(t, b, unsorted, nodes.as<double>(), (int64_t)nn, (int64_t)nl,
-                                                          lstart, lstart + 1, st);
-            }));
-        }
-        k_line_offsets<<<gb(np), 256, 0, st>>>(hdr, np, vert, lcnt, lstart,
-                                               vert ? s->d_voff.as<uint32_t>() : s->d_hoff.as<uint32_t>());
-        L++;
+    // ---- phase 2: chunks
+    std::vector<uint64_t> hscan(8 * n1);
+    std::vector<PolyHdr> hh(np);
+    FARM_CUDA(cudaMemcpyAsync(hscan.data(), scan, 8 * 8 * n1, cudaMemcpyDeviceToHost, st));
+    FARM_CUDA(cudaMemcpyAsync(hh.data(), R.hdr, sizeof(PolyHdr) * np, cudaMemcpyDeviceToHost, st));
+    FARM_CUDA(cudaStreamSynchronize(st));
+    std::vector<uint64_t> hoff(np + 1);
+    FARM_CUDA(cudaMemcpy(hoff.data(), R.doff, 8 * (np + 1), cudaMemcpyDeviceToHost));
+    const uint64_t kChunkEdges = env_u64("FARM_CHUNK_EDGES", 1ull << 25);
+    const uint64_t kChunkCross = env_u64("FARM_CHUNK_CROSS", 1ull << 25);
+    const uint64_t kChunkPix = env_u64("FARM_CHUNK_PIX", 1ull << 26);
+    uint32_t p = 0;
+    while (p < np) {
+        uint32_t q = p;
+        uint64_t ce = 0, cc = 0, cp = 0;
+        do {
+            ce += hoff[q + 1] - hoff[q];
+            cc += hh[q].n_seq;
+            cp += hh[q].P;
+            q++;
+        } while (q < np && ce + (hoff[q + 1] - hoff[q]) <= kChunkEdges && cc + hh[q].n_seq <= kChunkCross &&
+                 cp + hh[q].P <= kChunkPix);
+        Chunk ch;
+        ch.p0 = p;
+        ch.np = q - p;
+        ch.e0 = hoff[p];
+        ch.ne = hoff[q] - hoff[p];
+        ch.pix0 = hscan[0 * n1 + p];
+        ch.npix = hscan[0 * n1 + q] - ch.pix0;
+        ch.h0 = hscan[3 * n1 + p];
+        ch.nh = hscan[3 * n1 + q] - ch.h0;
+        ch.v0 = hscan[4 * n1 + p];
+        ch.nvl = hscan[4 * n1 + q] - ch.v0;
+        ch.col0 = hscan[5 * n1 + p];
+        ch.ncol = hscan[5 * n1 + q] - ch.col0;
+        ch.row0 = hscan[7 * n1 + p];
+        ch.nrow = hscan[7 * n1 + q] - ch.row0;
+        ch.hn0 = hh[p].hnode;
+        ch.vn0 = hh[p].vnode;
+        FARM_TRY(raster_chunk(R, ch));
+        p = q;
     }
+    (void)totRow;
 
-    // ---- scanline
-    sv = s->view();
-    sv.category_count = o->category_count;
-    k_scanline<<<gb(totScanRows), 256, 0, st>>>(hdr, np, scan + 7 * n1, totScanRows, s->d_status.as<uint8_t>(),
-                                                s->d_hoff.as<uint32_t>(), s->d_hnodes.as<double>(), o->category_count);
-    L++;
-
-    // ---- fill: strip clip per column
-    uint32_t *xcnt = s->s[S_CNT_E].as<uint32_t>();
-    k_clipx<<<gb(ne), 256, 0, st>>>(sv, hdr, doff, np, ne, colx, xcnt, nullptr, nullptr, nullptr);
-    L++;
-    uint64_t *x64 = s->s[S_TMP_A].as<uint64_t>();
-    FARM_TRY(s->s[S_TMP_A].ensure(8 * ne1 + 16));
-    x64 = s->s[S_TMP_A].as<uint64_t>();
-    FARM_CUDA(cudaMemsetAsync(xcnt + ne, 0, 4, st));
-    k_u32_to_u64<<<gb(ne1), 256, 0, st>>>(xcnt, ne1, x64);
-    L++;
-    uint64_t *xscan = s->s[S_SCAN_E].as<uint64_t>();
-    FARM_TRY(excl_scan(s, x64, xscan, ne1));
-    uint64_t nX;
-    FARM_TRY(d2h_u64(s, xscan + ne, nX));
-    // buffers: keys/points (emit order), then sorted by column
-    FARM_TRY(s->s[S_VKEY].ensure(8 * nX + 16));
-    FARM_TRY(s->s[S_VVAL].ensure(8 * nX + 16));
-    FARM_TRY(s->s[S_VKEY2].ensure(8 * nX + 16));
-    FARM_TRY(s->s[S_VVAL2].ensure(8 * nX + 16));
-    uint64_t *xkey = s->s[S_VKEY].as<uint64_t>(), *xkey_s = s->s[S_VKEY2].as<uint64_t>();
-    float2 *xpt = s->s[S_VVAL].as<float2>(), *xpt_s = s->s[S_VVAL2].as<float2>();
-    if (nX) {
-        k_clipx<<<gb(ne), 256, 0, st>>>(sv, hdr, doff, np, ne, colx, nullptr, xscan, xkey, xpt);
-        L++;
-        FARM_TRY(sort_pairs(s, xkey, xkey_s, reinterpret_cast<uint64_t *>(xpt), reinterpret_cast<uint64_t *>(xpt_s),
-                            nX, key_bits(totCol)));
-    }
-    // duplicates: sort (bits, position) then stable by column
-    FARM_TRY(s->s[S_HKEY].ensure(8 * nX + 16));
-    FARM_TRY(s->s[S_HVAL].ensure(8 * nX + 16));
-    FARM_TRY(s->s[S_VNKEY].ensure(8 * nX + 16));
-    FARM_TRY(s->s[S_VNVAL].ensure(8 * nX + 16));
-    FARM_TRY(s->s[S_CFROM].ensure(4 * nX + 16));
-    FARM_TRY(s->s[S_CTO].ensure(4 * nX + 16));
-    FARM_TRY(s->s[S_SEQW].ensure(nX + 32 + 8 * (nX + 1) * 2));
-    uint64_t *bits = s->s[S_HKEY].as<uint64_t>(), *bits_s = s->s[S_HVAL].as<uint64_t>();
-    uint64_t *ck = s->s[S_VNKEY].as<uint64_t>(), *ck_s = s->s[S_VNVAL].as<uint64_t>();
-    uint32_t *pos = s->s[S_CFROM].as<uint32_t>(), *pos_s = s->s[S_CTO].as<uint32_t>();
-    uint8_t *drop = s->s[S_SEQW].as<uint8_t>();
-    uint64_t *keptscan = reinterpret_cast<uint64_t *>(s->s[S_SEQW].as<uint8_t>() + ((nX + 16 + 7) & ~7ull));
-    uint64_t *kept64 = keptscan + (nX + 1);
-    FARM_CUDA(cudaMemsetAsync(drop, 0, nX + 1, st));
-    if (nX) {
-        k_ptbits<<<gb(nX), 256, 0, st>>>(xpt_s, nX, bits, pos);
-        L++;
-        FARM_TRY(sort_pairs(s, bits, bits_s, pos, pos_s, nX, 64));
-        // column of each element in (bits) order, then stable sort by column
-        FARM_TRY(s->s[S_CEDGE].ensure(4 * nX + 16));
-        // gather column keys for pos_s
-        uint32_t *pos2 = s->s[S_CEDGE].as<uint32_t>();
-        // ck[k] = column of the k-th element in bit order
-        k_gather_u64<<<gb(nX), 256, 0, st>>>(xkey_s, pos_s, nX, ck);
-        L++;
-        FARM_TRY(sort_pairs(s, ck, ck_s, pos_s, pos2, nX, key_bits(totCol)));
-        k_dup_large<<<gb(nX), 256, 0, st>>>(ck_s, pos2, xpt_s, nX, drop, nullptr);
-        L++;
-    }
-    // column starts and small-point columns
-    FARM_TRY(s->s[S_LINECNT].ensure(4 * (totCol + 1) + (totCol + 1) + 16));
-    FARM_TRY(s->s[S_LINESCAN].ensure(8 * (totCol + 1) * 2 + 16));
-    uint32_t *colcnt = s->s[S_LINECNT].as<uint32_t>();
-    uint8_t *colsmall = reinterpret_cast<uint8_t *>(colcnt + (totCol + 1));
-    uint64_t *cc64 = s->s[S_LINESCAN].as<uint64_t>(), *colstart = cc64 + (totCol + 1);
-    FARM_CUDA(cudaMemsetAsync(colcnt, 0, 4 * (totCol + 1) + (totCol + 1), st));
-    if (nX) {
-        k_col_count<<<gb(nX), 256, 0, st>>>(xkey_s, xpt_s, nX, colcnt, colsmall);
-        L++;
-    }
-    k_u32_to_u64<<<gb(totCol + 1), 256, 0, st>>>(colcnt, totCol + 1, cc64);
-    L++;
-    FARM_TRY(excl_scan(s, cc64, colstart, totCol + 1));
-    k_dup_small<<<gb(totCol), 256, 0, st>>>(colstart, totCol, colsmall, xpt_s, drop);
-    L++;
-    // kept scan and column polygons
-    k_not_u8<<<gb(nX + 1), 256, 0, st>>>(drop, nX + 1, kept64);
-    L++;
-    FARM_TRY(excl_scan(s, kept64, keptscan, nX + 1));
-    FARM_TRY(s->s[S_PIXSCAN].ensure(8 * (totCol + 1) * 2 + 16));
-    uint64_t *cpsize = s->s[S_PIXSCAN].as<uint64_t>(), *cpstart = cpsize + (totCol + 1);
-    FARM_CUDA(cudaMemsetAsync(cpsize, 0, 8 * (totCol + 1), st));
-    k_cp_sizes<<<gb(totCol), 256, 0, st>>>(colstart, drop, keptscan, totCol, cpsize);
-    L++;
-    FARM_TRY(excl_scan(s, cpsize, cpstart, totCol + 1));
-    uint64_t nCP;
-    FARM_TRY(d2h_u64(s, cpstart + totCol, nCP));
-    DevBuf cpbuf;
-    FARM_TRY(cpbuf.ensure(8 * nCP + 16));
-    float2 *cpoly = cpbuf.as<float2>();
-    if (nX) {
-        k_col_polys<<<gb(nX), 256, 0, st>>>(xkey_s, xpt_s, drop, keptscan, nX, colstart, cpstart, cpoly);
-        L++;
-    }
-
-    // ---- fill: cell clip per row
-    FARM_TRY(s->s[S_CNT_E].ensure(4 * (nCP + 1) + 16));
-    uint32_t *ycnt = s->s[S_CNT_E].as<uint32_t>();
-    FARM_CUDA(cudaMemsetAsync(ycnt, 0, 4 * (nCP + 1), st));
-    FARM_TRY(s->s[S_PIXCNT].ensure(4 * (totP + 1) + 16));
-    uint32_t *cellcnt = s->s[S_PIXCNT].as<uint32_t>();
-    FARM_CUDA(cudaMemsetAsync(cellcnt, 0, 4 * (totP + 1), st));
-    const uint64_t *colbase = scan + 5 * n1;
-    if (nCP) {
-        k_clipy<<<gb(nCP), 256, 0, st>>>(hdr, np, colbase, cpstart, totCol, cpoly, nCP, rowy, ycnt, nullptr, nullptr,
-                                         nullptr, nullptr);
-        L++;
-    }
-    FARM_TRY(s->s[S_TMP_A].ensure(8 * (nCP + 1) + 16));
-    uint64_t *y64 = s->s[S_TMP_A].as<uint64_t>();
-    k_u32_to_u64<<<gb(nCP + 1), 256, 0, st>>>(ycnt, nCP + 1, y64);
-    L++;
-    FARM_TRY(s->s[S_SCAN_E].ensure(8 * (nCP + 1) + 16));
-    uint64_t *yscan = s->s[S_SCAN_E].as<uint64_t>();
-    FARM_TRY(excl_scan(s, y64, yscan, nCP + 1));
-    uint64_t nY;
-    FARM_TRY(d2h_u64(s, yscan + nCP, nY));
-    DevBuf ykb, ypb, yks, yps;
-    FARM_TRY(ykb.ensure(8 * nY + 16));
-    FARM_TRY(ypb.ensure(8 * nY + 16));
-    FARM_TRY(yks.ensure(8 * nY + 16));
-    FARM_TRY(yps.ensure(8 * nY + 16));
-    if (nY) {
-        k_clipy<<<gb(nCP), 256, 0, st>>>(hdr, np, colbase, cpstart, totCol, cpoly, nCP, rowy, nullptr, yscan,
-                                         ykb.as<uint64_t>(), ypb.as<float2>(), cellcnt);
-        L++;
-        FARM_TRY(sort_pairs(s, ykb.as<uint64_t>(), yks.as<uint64_t>(), ypb.as<uint64_t>(), yps.as<uint64_t>(), nY,
-                            key_bits(totP)));
-    }
-    FARM_TRY(s->s[S_TMP_A].ensure(8 * (totP + 1) * 2 + 16));
-    uint64_t *c64 = s->s[S_TMP_A].as<uint64_t>(), *cellstart = c64 + (totP + 1);
-    k_u32_to_u64<<<gb(totP + 1), 256, 0, st>>>(cellcnt, totP + 1, c64);
-    L++;
-    FARM_TRY(excl_scan(s, c64, cellstart, totP + 1));
-    k_cells<<<gb(totP), 256, 0, st>>>(hdr, scan + 0 * n1, np, totP, cellstart, yps.as<float2>(), cpstart,
-                                      s->d_status.as<uint8_t>(), s->d_areas.as<double>(), o->category_count);
-    L++;
-
-    // ---- hierarchy
-    if (o->hierarchy) {
-        FARM_TRY(s->s[S_TMP_B].ensure(2 * 8 * n1 + 16));
-        uint64_t *lc = s->s[S_TMP_B].as<uint64_t>(), *lb = lc + n1;
-        FARM_CUDA(cudaMemsetAsync(lc, 0, 8 * n1, st));
-        k_layer_count<<<gb(np), 256, 0, st>>>(hdr, np, lc);
-        L++;
-        FARM_TRY(excl_scan(s, lc, lb, n1));
-        uint64_t nl;
-        FARM_TRY(d2h_u64(s, lb + np, nl));
-        DevBuf fb;
-        FARM_TRY(fb.ensure(4 * nl + 16));
-        k_fill_u32<<<gb(nl), 256, 0, st>>>(fb.as<uint32_t>(), nl, 0xFFFFFFFFu);
-        L++;
-        k_merge<<<gb(32ull * np), 256, 0, st>>>(hdr, np, s->d_status.as<uint8_t>(), s->d_areas.as<double>(),
-                                               o->category_count, 0, fb.as<uint32_t>(), lb);
-        k_merge<<<gb(32ull * np), 256, 0, st>>>(hdr, np, s->d_status.as<uint8_t>(), s->d_areas.as<double>(),
-                                               o->category_count, 1, fb.as<uint32_t>(), lb);
-        L += 2;
-        FARM_CUDA(cudaStreamSynchronize(st));
-        fb.release();
-    }
-    FARM_CUDA(cudaGetLastError());
     // errors
-    int *derr;
     FARM_TRY(s->d_counters.ensure(64));
-    derr = s->d_counters.as<int>();
+    int *derr = s->d_counters.as<int>();
     FARM_CUDA(cudaMemsetAsync(derr, 0, 4, st));
-    k_err_reduce<<<gb(np), 256, 0, st>>>(hdr, np, derr);
-    L++;
+    k_err_reduce<<<gb(np), 256, 0, st>>>(R.hdr, np, derr);
+    R.launches++;
     int herr = 0;
     FARM_CUDA(cudaMemcpyAsync(&herr, derr, 4, cudaMemcpyDeviceToHost, st));
     FARM_CUDA(cudaStreamSynchronize(st));
-    cpbuf.release();
-    ykb.release();
-    ypb.release();
-    yks.release();
-    yps.release();
     s->tot_P = totP;
     s->tot_status = totStatus;
-    s->tot_seq = totSeq;
-    if (launches) *launches = L;
+    if (launches) *launches = R.launches;
     if (herr) {
-        set_error("a polygon violated a condition the reference asserts on (see farm_raster_fetch err)");
+        set_error(herr == FARM_EASSERT
+                      ? "a polygon violated a condition the reference asserts on (see farm_raster_fetch err)"
+                      : "internal inconsistency between the rasterizer's passes");
         return herr;
     }
     return FARM_OK;

@@ -208,12 +208,20 @@ int farm_store_load(farm_store *s, int side, uint64_t n, const uint64_t *off, co
     for (uint64_t k = 0; k <= n0; k++) cat[k] = s->h_off[0][k];
     for (uint64_t k = 1; k <= n1; k++) cat[n0 + k] = t0 + s->h_off[1][k];
     uint64_t total = t0 + t1;
-    // padded layout: polygon p's ring starts at cat[p] + 2p
-    DevBuf nr;
-    FARM_TRY(nr.ensure((total + 2 * (n0 + n1)) * sizeof(float2) + 64));
-    if (side == 1 && s->d_ring.p)
-        FARM_CUDA(cudaMemcpyAsync(nr.p, s->d_ring.p, (t0 + 2 * n0) * sizeof(float2), cudaMemcpyDeviceToDevice,
-                                  s->stream));
+    // padded layout: polygon p's ring starts at cat[p] + 2p. The source side
+    // sits first, so loading the target side appends in place when it fits.
+    size_t need = (total + 2 * (n0 + n1)) * sizeof(float2) + 64;
+    if (need > s->d_ring.cap) {
+        DevBuf nr;
+        FARM_TRY(nr.ensure(need + need / 8));
+        if (side == 1 && s->d_ring.p)
+            FARM_CUDA(cudaMemcpyAsync(nr.p, s->d_ring.p, (t0 + 2 * n0) * sizeof(float2), cudaMemcpyDeviceToDevice,
+                                      s->stream));
+        FARM_CUDA(cudaStreamSynchronize(s->stream));
+        s->d_ring.release();
+        s->d_ring = nr;
+        nr.p = nullptr;
+    }
     uint64_t side_total = side == 0 ? t0 : t1;
     const float2 *src;
     if (mem == FARM_MEM_DEVICE) {
@@ -232,16 +240,40 @@ int farm_store_load(farm_store *s, int side, uint64_t n, const uint64_t *off, co
         unsigned cap = 32u * (unsigned)sm_count();
         if (blocks > cap) blocks = cap;
         k_pad_rings<<<blocks, 256, 0, s->stream>>>(src, s->d_off.as<uint64_t>() + first_poly, (uint32_t)n,
-                                                   first_poly, nr.as<float2>());
+                                                   first_poly, s->d_ring.as<float2>());
         FARM_CUDA(cudaGetLastError());
         s->launches++;
     }
     FARM_CUDA(cudaStreamSynchronize(s->stream));  // the host offset vector dies here
-    s->d_ring.release();
-    s->d_ring = nr;
-    nr.p = nullptr;
     s->n_poly = n0 + n1;
     s->n_edges = total;
+    return FARM_OK;
+}
+
+__global__ void k_collect_err(const PolyHdr *__restrict__ hdr, uint64_t first, uint64_t n, int32_t *__restrict__ out) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
+        out[k] = hdr[first + k].err;
+}
+
+int farm_raster_errors(farm_store *s, int side, int32_t *err, uint64_t n) {
+    if (!s || side < 0 || side > 1 || n != s->n_side[side] || (n && !err)) {
+        set_error("invalid arguments to farm_raster_errors");
+        return FARM_EINVAL;
+    }
+    if (!s->rasterized) {
+        set_error("store is not rasterized");
+        return FARM_EINVAL;
+    }
+    if (!n) return FARM_OK;
+    int32_t *d = nullptr;
+    FARM_CUDA(cudaMalloc(&d, 4 * n));
+    uint64_t first = side == 0 ? 0 : s->n_side[0];
+    k_collect_err<<<grid_for(n, 256) > 4096 ? 4096 : grid_for(n, 256), 256, 0, s->stream>>>(
+        s->d_hdr.as<PolyHdr>(), first, n, d);
+    cudaError_t e = cudaMemcpyAsync(err, d, 4 * n, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(e, "farm_raster_errors");
     return FARM_OK;
 }
 

@@ -50,7 +50,8 @@ def _addr(a):
 def stats_dict(st: Stats) -> dict:
     return {"pairs": st.pairs, "found": st.found, "in_hits": st.in_hits, "border_pairs": st.border_pairs,
             "segment_tests": st.segment_tests, "fp64_rechecks": st.fp64_rechecks, "ms_total": st.ms_total,
-            "ms_stage": list(st.ms_stage), "kernel_launches": st.kernel_launches}
+            "ms_stage": list(st.ms_stage), "kernel_launches": st.kernel_launches,
+            "src_window_pixels": st.src_window_pixels, "tgt_window_pixels": st.tgt_window_pixels}
 
 
 class Store:
@@ -99,9 +100,17 @@ class Store:
         if target is not None:
             self.load(1, target.off, target.xy)
 
-    def rasterize(self, vpr: int = 10, category_count: int = 16, hierarchy: bool = False) -> None:
+    def rasterize(self, vpr: int = 10, category_count: int = 16, hierarchy: bool = False,
+                  strict: bool = True) -> int:
+        """Rasterize every loaded polygon. With strict=False, polygons on which
+        the reference asserts or never terminates (FARM_EASSERT) are reported
+        by count instead of raising; queries then return 2 for their pairs."""
         o = RasterOpts(vpr, category_count, int(hierarchy), 0)
-        check_gpu(self._lib.farm_rasterize(self._h, C.byref(o)))
+        rc = self._lib.farm_rasterize(self._h, C.byref(o))
+        if rc == -10 and not strict:
+            return int((self.raster_errors(0) != 0).sum() + (self.raster_errors(1) != 0).sum())
+        check_gpu(rc)
+        return 0
 
     def intersect(self, pairs, mode: int = MODE_EXACT, out=None):
         """Per-pair 0/1 results (same memory kind as ``pairs``) and the found count."""
@@ -141,6 +150,29 @@ class Store:
         check_gpu(self._lib.farm_intersection_area(self._h, pp, n, mem, po, C.byref(st)))
         self.last_stats = stats_dict(st)
         return out
+
+    @property
+    def launches(self) -> int:
+        """Engine kernels launched through this store so far."""
+        return int(self._lib.farm_store_launches(self._h))
+
+    def event_record(self, slot: int) -> None:
+        check_gpu(self._lib.farm_event_record(self._h, slot))
+
+    def event_elapsed(self, a: int, b: int) -> float:
+        ms = C.c_double(0)
+        check_gpu(self._lib.farm_event_elapsed(self._h, a, b, C.byref(ms)))
+        return ms.value
+
+    def raster_errors(self, side: int) -> np.ndarray:
+        """Per-polygon rasterization status (0 or FARM_EASSERT) of one side."""
+        n = self.n_source if side == 0 else self.n_target
+        out = np.zeros(n, np.int32)
+        check_gpu(self._lib.farm_raster_errors(self._h, side, C.c_void_p(out.ctypes.data), n))
+        return out
+
+    def sync(self) -> None:
+        check_gpu(self._lib.farm_sync(self._h))
 
     def fetch_raster(self, side: int, index: int) -> dict:
         """One polygon's raster arrays (for parity tests)."""

@@ -69,6 +69,8 @@ typedef struct farm_stats {
     double ms_stage[4];      /* raster, filter, refine, other */
     int32_t kernel_launches; /* engine kernels launched by the call */
     int32_t reserved;
+    uint64_t src_window_pixels; /* source pixels in the target-MBR windows */
+    uint64_t tgt_window_pixels; /* target pixels visited under non-OUT source pixels */
 } farm_stats;
 
 const char *farm_last_error(void);
@@ -90,7 +92,9 @@ int farm_store_load(farm_store *s, int side, uint64_t n, const uint64_t *off, co
 int farm_rasterize(farm_store *s, const farm_raster_opts *o);
 
 /* Decide Ideal::intersect(source[p.s], target[p.t]) for n pairs. pairs: 2n
- * uint32 (s, t). out: n bytes (0/1), may be NULL. found: count of true. */
+ * uint32 (s, t). out: n bytes, may be NULL: 0 / 1, or 2 when either polygon
+ * failed rasterization (farm_raster_errors: the reference aborts on it).
+ * found: count of 1s. */
 int farm_intersect(farm_store *s, const uint32_t *pairs, uint64_t n, int mode, int mem, uint8_t *out,
                    uint64_t *found, farm_stats *st);
 
@@ -120,10 +124,15 @@ int farm_raster_fetch(farm_store *s, int side, uint64_t index, farm_raster_view 
                       uint32_t *offset, uint32_t *seq, uint32_t *hoff, double *hnodes, uint32_t *voff,
                       double *vnodes, double *areas, double *layer_info /* 7 doubles per layer */);
 
+/* Per-polygon rasterization status of one side (n = that side's polygon
+ * count): 0, or FARM_EASSERT for a polygon on which the reference asserts or
+ * never terminates (such polygons are reported, not rasterized). */
+int farm_raster_errors(farm_store *s, int side, int32_t *err, uint64_t n);
+
 /* Wait for outstanding work of the store's stream. */
 int farm_sync(farm_store *s);
 
-/* CUDA-event timing on the store's stream (8 slots): record, then elapsed ms a -> b. */
+/* CUDA-event timing on the store's stream (slots 0-5): record, then elapsed ms a -> b. */
 int farm_event_record(farm_store *s, int slot);
 int farm_event_elapsed(farm_store *s, int a, int b, double *ms);
 /* Engine kernels launched through this store so far. */

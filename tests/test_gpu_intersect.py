@@ -59,3 +59,25 @@ def test_gpu_intersect_edge_cases(gpu_lib):
     # empty pair list
     out, found, _ = run(S, T, np.zeros((0, 2), np.uint32), 10)
     assert found == 0 and len(out) == 0
+
+
+def test_gpu_intersect_marks_pairs_of_unrasterizable_polygons(gpu_lib):
+    from farm_gb300._native import FarmError
+    # the diamond's edges pass exactly through grid corners at -v 1: the
+    # reference's edge walk never terminates on it; the engine flags it
+    diamond = np.array([[0, 0], [3, 3], [0, 6], [-3, 3], [0, 0]], np.float32)
+    sq = np.array([[-1, 1], [1, 1], [1, 5], [-1, 5], [-1, 1]], np.float32)
+    mk = lambda rs: P.PolygonSet(np.concatenate([[0], np.cumsum([len(r) for r in rs])]).astype(np.uint64),
+                                 np.ascontiguousarray(np.concatenate(rs), dtype=np.float32))
+    S, T = mk([diamond, sq]), mk([sq, diamond])
+    st = Store()
+    st.load_sets(S, T)
+    with pytest.raises(FarmError):
+        st.rasterize(vpr=1)
+    assert st.raster_errors(0).tolist() == [-10, 0] and st.raster_errors(1).tolist() == [0, -10]
+    pairs = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.uint32)
+    out, found = st.intersect(pairs)
+    RS, RT = O.Raster(sq, 1), O.Raster(sq, 1)
+    assert out.tolist() == [2, int(O.intersect(RS, RT)), 2, 2]
+    assert found == int(out[1] == 1)
+    st.close()

@@ -90,3 +90,17 @@ def test_gpu_raster_edge_cases(gpu_lib):
             else:
                 assert g["err"] == 0 and not raster_mismatches(g, exp[k]), (vpr, k)
         st.close()
+
+
+def test_gpu_raster_many_chunks(gpu_lib, monkeypatch):
+    # tiny scratch budgets force one or two polygons per chunk
+    monkeypatch.setenv("FARM_CHUNK_EDGES", "700")
+    monkeypatch.setenv("FARM_CHUNK_CROSS", "300")
+    monkeypatch.setenv("FARM_CHUNK_PIX", "64")
+    ps = P.generate(P.StarParams(dom_hi=30.0, n_hi=1200), 21, 120)
+    for hier in (False, True):
+        st, got = gpu_rasters(ps, 4, hier)
+        for k in range(ps.n):
+            r = O.Raster(ps.ring(k), 4, hier).arrays()
+            assert not raster_mismatches(got[k], r), (hier, k)
+        st.close()
