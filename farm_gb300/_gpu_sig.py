@@ -49,6 +49,7 @@ def declare(lib):
                                       u32p, f64p, f64p, f64p]
     lib.farm_sync.argtypes = [vp]
     lib.farm_raster_errors.argtypes = [vp, C.c_int, vp, C.c_uint64]
+    lib.farm_intersect_static.argtypes = [vp, vp, C.c_uint64, vp, u64p]
     lib.farm_event_record.argtypes = [vp, C.c_int]
     lib.farm_event_elapsed.argtypes = [vp, C.c_int, C.c_int, f64p]
     lib.farm_store_launches.argtypes = [vp]

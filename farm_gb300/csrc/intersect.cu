@@ -13,6 +13,10 @@
 // at the first decisive hit.
 #include <cub/cub.cuh>
 
+#include <cstring>
+#include <mutex>
+#include <string>
+
 #include "common.cuh"
 
 namespace farm {
@@ -311,4 +315,97 @@ extern "C" int farm_intersect(farm_store *s, const uint32_t *pairs, uint64_t n, 
     }
     if (mode != FARM_MODE_EXACT) return intersect_learned(s, pairs, n, mem, out, found, st);
     return intersect(s, pairs, n, mode, mem, out, found, st);
+}
+
+// ------------------------------------------------ allocation-free entry --
+// farm_intersect_static: the same filter + refine kernel, but every device
+// byte it needs beyond the store (the staged pair list, the result bytes and
+// the work/stat counters) lives in one file-scope __device__ array instead of
+// store buffers that farm_intersect grows with cudaMalloc. It is for callers
+// that must not allocate device memory at query time: code whose device memory
+// is owned by another allocator (a framework's caching allocator that has
+// reserved the HBM), and host threads that must not trigger the device-wide
+// synchronisation a cudaMalloc/cudaFree implies while other streams run.
+namespace farm {
+
+constexpr uint64_t kStaticMaxPairs = 1ull << 20;  // 1,048,576 pairs per call
+constexpr size_t kStaticCtrBytes = 256;
+constexpr size_t kStaticBytes = kStaticCtrBytes + 8 * kStaticMaxPairs + kStaticMaxPairs;  // ~9 MiB
+constexpr int kStaticMaxDevices = 64;
+
+// Shared by every call on a device and kept for the life of the process.
+static __device__ __align__(256) unsigned char g_intersect_static[kStaticBytes];
+
+static std::mutex g_static_mu;
+static unsigned char *g_static_addr[kStaticMaxDevices] = {};
+
+// Device address of the array on the current device, looked up once per device.
+static int static_scratch(int dev, unsigned char **p) {
+    if (dev < 0 || dev >= kStaticMaxDevices) {
+        set_error("farm_intersect_static: device ordinal out of range");
+        return FARM_EINVAL;
+    }
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_addr[dev]) {
+        void *q = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&q, g_intersect_static);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_intersect_static)");
+        g_static_addr[dev] = static_cast<unsigned char *>(q);
+    }
+    *p = g_static_addr[dev];
+    return FARM_OK;
+}
+
+}  // namespace farm
+
+extern "C" int farm_intersect_static(farm_store *s, const uint32_t *pairs, uint64_t n, uint8_t *out,
+                                     uint64_t *found) {
+    using namespace farm;
+    if (!s || (n && (!pairs || !out))) {
+        set_error("invalid arguments to farm_intersect_static");
+        return FARM_EINVAL;
+    }
+    if (n > kStaticMaxPairs) {
+        set_error("farm_intersect_static: " + std::to_string(n) + " pairs exceed its fixed scratch of " +
+                  std::to_string(kStaticMaxPairs) + " pairs; split the list or use farm_intersect");
+        return FARM_EINVAL;
+    }
+    if (!s->rasterized) {
+        set_error("farm_intersect_static: rasterize first");
+        return FARM_EINVAL;
+    }
+    if (s->n_side[1] == 0) {
+        set_error("farm_intersect_static: no target side loaded");
+        return FARM_EINVAL;
+    }
+    int cur = 0;
+    FARM_CUDA(cudaGetDevice(&cur));
+    if (cur != s->device) FARM_CUDA(cudaSetDevice(s->device));
+    unsigned char *base = nullptr;
+    int rc = static_scratch(s->device, &base);
+    if (rc == FARM_OK) {
+        cudaStream_t stream = s->stream;
+        unsigned long long *next = reinterpret_cast<unsigned long long *>(base);
+        IxCounters *ctr = reinterpret_cast<IxCounters *>(next + 1);
+        uint32_t *dpairs = reinterpret_cast<uint32_t *>(base + kStaticCtrBytes);
+        uint8_t *dout = base + kStaticCtrBytes + 8 * kStaticMaxPairs;
+        IxCounters h{};
+        cudaError_t e = cudaMemsetAsync(base, 0, kStaticCtrBytes, stream);  // counters start at zero
+        if (e == cudaSuccess && n) e = cudaMemcpyAsync(dpairs, pairs, 8 * n, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess && n) {
+            PairView pv{dpairs, n, s->n_side[0]};
+            k_intersect<<<sm_count() * 8, kWarpsPerBlock * 32, 0, stream>>>(s->view(), pv, next, dout, ctr);
+            e = cudaGetLastError();
+            if (e == cudaSuccess) s->launches++;
+        }
+        if (e == cudaSuccess && n) e = cudaMemcpyAsync(out, dout, n, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&h, ctr, sizeof h, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess)
+            rc = cuda_fail(e, "farm_intersect_static");
+        else if (found)
+            *found = h.found;
+    }
+    if (cur != s->device) cudaSetDevice(cur);
+    return rc;
 }

@@ -124,6 +124,23 @@ int farm_raster_fetch(farm_store *s, int side, uint64_t index, farm_raster_view 
                       uint32_t *offset, uint32_t *seq, uint32_t *hoff, double *hnodes, uint32_t *voff,
                       double *vnodes, double *areas, double *layer_info /* 7 doubles per layer */);
 
+/* Allocation-free variant of farm_intersect (no counterpart in the reference):
+ * for callers that cannot allocate device memory at query time — code whose
+ * device memory belongs to another allocator (e.g. a framework's caching
+ * allocator that has reserved the HBM), or threads that must not trigger the
+ * device-wide synchronisation of cudaMalloc/cudaFree while other streams run.
+ * pairs (2n uint32) and out (n bytes, same encoding as farm_intersect) are
+ * HOST buffers; the staged pairs, results and counters live in a fixed
+ * file-scope device array of about 9 MiB that every device which loads the
+ * library keeps until process exit. At most 1,048,576 pairs per call; larger
+ * n is rejected with FARM_EINVAL. The first call on a device looks the array's
+ * address up (cudaGetSymbolAddress) with that device current: make that first
+ * call before any stream capture. All calls share the array and it keeps the
+ * last call's contents, so calls that overlap on the GPU (from different host
+ * threads or stores) race; serialise them. The store itself must already be
+ * loaded and rasterized (those steps allocate). */
+int farm_intersect_static(farm_store *s, const uint32_t *pairs, uint64_t n, uint8_t *out, uint64_t *found);
+
 /* Per-polygon rasterization status of one side (n = that side's polygon
  * count): 0, or FARM_EASSERT for a polygon on which the reference asserts or
  * never terminates (such polygons are reported, not rasterized). */
