@@ -4,7 +4,7 @@ import ctypes as C
 
 class RasterOpts(C.Structure):
     _fields_ = [("vpr", C.c_int32), ("category_count", C.c_int32), ("hierarchy", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("reserved", C.c_int32), ("grid_extent", C.c_double)]
 
 
 class Stats(C.Structure):
@@ -54,5 +54,4 @@ def declare(lib):
     lib.farm_event_elapsed.argtypes = [vp, C.c_int, C.c_int, f64p]
     lib.farm_store_launches.argtypes = [vp]
     lib.farm_store_launches.restype = C.c_uint64
-    lib.farm_gen_device.argtypes = [C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_uint64,
-                                    C.c_uint64, C.c_uint64, vp, vp]
+

@@ -1525,7 +1525,7 @@ int rasterize(farm_store *s, const farm_raster_opts *o, int *launches) {
     rp.hier = o->hierarchy;
     {
         // UniversalGrid::configure(25) (UniversalGrid.h:29-35) with util.h:53-66
-        double num = 360.0 / pow(2, 25);
+        double num = (o->grid_extent > 0 ? o->grid_extent : 360.0) / pow(2, 25);
         double d = ceil(log10(num < 0 ? -num : num));
         int power = 2 - (int)d;
         double magnitude = pow(10.0, power);

@@ -1,0 +1,759 @@
+// Stages (b) + (c) for within-distance: hierarchical BORDER x BORDER descent,
+// candidate ordering and border refinement with point-segment distances.
+//
+// Reference decision procedure (Ideal::within, Ideal.cpp:2475-2643):
+//  * descend the two polygons' raster hierarchies together (the coarser side
+//    advances); at each level the BORDER children of the queued pixels form
+//    two sets, their cross product gives the smallest box max-distance (any
+//    max-distance <= d decides "true") and keeps the pairs whose box distance
+//    is <= d and below that smallest max-distance;
+//  * at the finest level the kept pairs are ordered by (approximate distance,
+//    low, high, ids) and refined in that order with the minimum point-segment
+//    distance of their edge sequences; "true" once the running minimum is
+//    below d, "false" once it is below every later pair's lower bound.
+// Below the finest level the queue only matters through the two sets of
+// pixels it holds (the children of its members), so each level here keeps
+// two pixel sets instead of an explicit pair queue.
+//
+// Kernels: k_within_descend (one warp per pair) writes the finest level's
+// candidate pairs; a merge sort orders them by pair and the reference's tuple;
+// k_within_refine (one warp per pair) runs the ordered refinement, with the
+// point-segment distances of each edge-sequence pair spread over the lanes.
+#include <cub/cub.cuh>
+
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace farm {
+
+// util.h:68 (float constants) and the 900-entry longitude table (util.h:73),
+// regenerated on the host from its defining formula.
+__constant__ float c_mean20[20];
+__constant__ double c_deg_lon[900];
+
+static std::mutex g_tab_mu;
+static bool g_tab_ready[64] = {};
+
+static int ensure_tables(int dev) {
+    std::lock_guard<std::mutex> lock(g_tab_mu);
+    if (dev >= 0 && dev < 64 && g_tab_ready[dev]) return FARM_OK;
+    const float mean20[20] = {0.0f,  0.7f,  0.62f, 0.55f, 0.52f, 0.45f, 0.42f, 0.4f,  0.38f, 0.34f,
+                              0.31f, 0.28f, 0.25f, 0.22f, 0.18f, 0.15f, 0.1f,  0.05f, 0.0f,  0.0f};
+    double deg[900];
+    const double PI = 3.14159265;
+    for (int i = 0; i < 900; i++) {
+        double lat = i / 10.0;
+        double v = 360.0 / (sin((90 - lat) * PI / 180) * 40076);
+        char buf[64];
+        snprintf(buf, sizeof buf, "%.6f", v);
+        deg[i] = strtod(buf, nullptr);
+    }
+    FARM_CUDA(cudaMemcpyToSymbol(c_mean20, mean20, sizeof mean20));
+    FARM_CUDA(cudaMemcpyToSymbol(c_deg_lon, deg, sizeof deg));
+    if (dev >= 0 && dev < 64) g_tab_ready[dev] = true;
+    return FARM_OK;
+}
+
+__device__ __forceinline__ double deg_lon(double lat) {
+    double a = fabs(lat);
+    if (a == 90) a = 89.9;
+    int idx = (int)(a * 10);
+    if (idx < 0 || idx >= 900) idx = 899;  // the reference indexes past the table here
+    return c_deg_lon[idx];
+}
+#define DEG_LAT (360.0 / 40076.0)
+
+struct Box {
+    double lo0, lo1, hi0, hi1;
+};
+
+__device__ __forceinline__ Box pixel_box(const LayerGeom &g, int id) {
+    int x = id % g.dimx, y = id / g.dimx;
+    Box b;
+    b.lo0 = g.mbr[0] + x * g.step_x;
+    b.lo1 = g.mbr[1] + y * g.step_y;
+    b.hi0 = g.mbr[0] + (x + 1) * g.step_x;
+    b.hi1 = g.mbr[1] + (y + 1) * g.step_y;
+    return b;
+}
+
+// Box.cpp:90-118
+__device__ double box_distance(const Box &a, const Box &t, bool geo) {
+    if (!(t.lo0 > a.hi0 || t.hi0 < a.lo0 || t.lo1 > a.hi1 || t.hi1 < a.lo1)) return 0;
+    double dx = 0, dy = 0;
+    if (t.lo1 > a.hi1)
+        dy = t.lo1 - a.hi1;
+    else if (t.hi1 < a.lo1)
+        dy = a.lo1 - t.hi1;
+    if (t.lo0 > a.hi0)
+        dx = t.lo0 - a.hi0;
+    else if (t.hi0 < a.lo0)
+        dx = a.lo0 - t.hi0;
+    if (geo) {
+        dy = dy / DEG_LAT;
+        dx = dx / deg_lon(a.lo1);
+    }
+    return sqrt(dx * dx + dy * dy);
+}
+
+// Box.cpp:120-149: the corners become float points first
+__device__ double box_max_distance(const Box &a, const Box &t, bool geo) {
+    float ax[2] = {(float)a.lo0, (float)a.hi0}, ay[2] = {(float)a.lo1, (float)a.hi1};
+    float tx[2] = {(float)t.lo0, (float)t.hi0}, ty[2] = {(float)t.lo1, (float)t.hi1};
+    double dlon = geo ? deg_lon(a.lo1) : 1.0;
+    double md = 0.0;
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) {
+            // vertices1[i] = (x, y) with x from {lo, lo, hi, hi}, y from {lo, hi, lo, hi}
+            float vx = ax[i >> 1], vy = ay[i & 1], wx = tx[j >> 1], wy = ty[j & 1];
+            double dx = __fsub_rn(vx, wx), dy = __fsub_rn(vy, wy);
+            if (geo) {
+                dy = dy / DEG_LAT;
+                dx = dx / dlon;
+            }
+            double d = sqrt(dx * dx + dy * dy);
+            md = md > d ? md : d;
+        }
+    return md;
+}
+
+// geometry_computation.h:49-89
+__device__ double pt_seg_dist(float2 p, float2 p1, float2 p2, bool geo) {
+    double A = __fsub_rn(p.x, p1.x), B = __fsub_rn(p.y, p1.y);
+    double C = __fsub_rn(p2.x, p1.x), D = __fsub_rn(p2.y, p1.y);
+    double dot = A * C + B * D;
+    double len_sq = C * C + D * D;
+    double param = -1;
+    if (len_sq != 0) param = dot / len_sq;
+    double xx, yy;
+    if (param < 0) {
+        xx = p1.x;
+        yy = p1.y;
+    } else if (param > 1) {
+        xx = p2.x;
+        yy = p2.y;
+    } else {
+        xx = p1.x + param * C;
+        yy = p1.y + param * D;
+    }
+    double dx = p.x - xx, dy = p.y - yy;
+    if (geo) {
+        dx = dx / deg_lon(p.y);
+        dy = dy / DEG_LAT;
+    }
+    return sqrt(dx * dx + dy * dy);
+}
+
+struct WCand {
+    double apx, lo, hi;
+    uint32_t pair;
+    int32_t id1, id2;
+    uint32_t pad;
+};
+
+struct WCandLess {
+    __device__ bool operator()(const WCand &a, const WCand &b) const {
+        if (a.pair != b.pair) return a.pair < b.pair;
+        if (a.apx != b.apx) return a.apx < b.apx;
+        if (a.lo != b.lo) return a.lo < b.lo;
+        if (a.hi != b.hi) return a.hi < b.hi;
+        if (a.id1 != b.id1) return a.id1 < b.id1;
+        return a.id2 < b.id2;
+    }
+};
+
+// out codes of the descent: 0 / 1 decided, 4 refine candidates, 2 polygon
+// failed rasterization, 3 did not fit the candidate buffer (retried)
+enum : uint8_t { W_FALSE = 0, W_TRUE = 1, W_BADPOLY = 2, W_RETRY = 3, W_REFINE = 4 };
+
+struct WithinArgs {
+    const uint32_t *pairs;
+    uint64_t n;
+    uint64_t tgt_base;
+    double thr;
+    int geo;
+    uint32_t cap_pix;  // per-side pixel capacity of a warp's scratch
+    uint32_t *scratch; // per warp: 2 sides x (bitmap words + 2 lists)
+    uint64_t scratch_words;
+    WCand *cand;
+    unsigned long long *ncand;
+    uint64_t cand_cap;
+    uint8_t *out;
+    unsigned long long *next;
+    unsigned long long *stats;  // candidates, box pairs
+};
+
+struct SideScratch {
+    uint32_t *bits;  // cap_pix/32 + 1 words
+    uint32_t *q;     // current queued set
+    uint32_t *p;     // next level set
+};
+
+// set bit, return whether newly set
+__device__ __forceinline__ void set_bit(uint32_t *bits, uint32_t id) { atomicOr(&bits[id >> 5], 1u << (id & 31)); }
+
+// Compact the set bits of [0, nbits) into list (ascending) and clear them.
+__device__ uint32_t compact_bits(uint32_t *bits, uint32_t nbits, uint32_t *list, int lane) {
+    uint32_t nw = (nbits + 31) >> 5;
+    uint32_t total = 0;
+    for (uint32_t w0 = 0; w0 < nw; w0 += 32) {
+        uint32_t w = w0 + lane;
+        uint32_t word = w < nw ? bits[w] : 0u;
+        uint32_t c = __popc(word);
+        uint32_t incl = c;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        uint32_t at = total + incl - c;
+        while (word) {
+            int b = __ffs(word) - 1;
+            list[at++] = (w << 5) + b;
+            word &= word - 1;
+        }
+        if (w < nw) bits[w] = 0u;
+        total += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    __syncwarp();
+    return total;
+}
+
+// Children of the queued pixels at layer `li` (their box at the coarser
+// layer, shrunk by 1e-6, then retrieve_pixels' own 1e-6) or the queued pixels
+// themselves; BORDER ones only (Ideal.cpp:2513-2551).
+__device__ uint32_t next_set(const PolyHdr &h, const uint8_t *status, bool advance, uint32_t li, const uint32_t *q,
+                             uint32_t nq, SideScratch &sc, int lane, int cc) {
+    LayerGeom g;
+    layer_geom(h, li, g);
+    LayerGeom pg;
+    if (advance) layer_geom(h, li - 1, pg);
+    const uint8_t *st = status + h.st + g.offset;
+    for (uint32_t k = lane; k < nq; k += 32) {
+        uint32_t id = q[k];
+        if (advance) {
+            Box b = pixel_box(pg, (int)id);
+            b.lo0 += 1e-6;
+            b.lo1 += 1e-6;
+            b.hi0 -= 1e-6;
+            b.hi1 -= 1e-6;
+            int sx = offset_x(g.mbr, g.step_x, g.dimx, b.lo0 + 1e-6);
+            int sy = offset_y(g.mbr, g.step_y, g.dimy, b.lo1 + 1e-6);
+            int ex = offset_x(g.mbr, g.step_x, g.dimx, b.hi0 - 1e-6);
+            int ey = offset_y(g.mbr, g.step_y, g.dimy, b.hi1 - 1e-6);
+            for (int x = sx; x <= ex; x++)
+                for (int y = sy; y <= ey; y++) {
+                    uint32_t c = (uint32_t)(y * g.dimx + x);
+                    if (show_status(st[c], cc) == 1) set_bit(sc.bits, c);
+                }
+        } else if (show_status(st[id], cc) == 1) {
+            set_bit(sc.bits, id);
+        }
+    }
+    __syncwarp();
+    return compact_bits(sc.bits, (uint32_t)(g.dimx * g.dimy), sc.p, lane);
+}
+
+__global__ void __launch_bounds__(256) k_within_descend(const StoreView sv, WithinArgs a) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int cc = sv.category_count;
+    const bool geo = a.geo != 0;
+    uint32_t *base = a.scratch + warp * a.scratch_words;
+    const uint32_t bw = (a.cap_pix >> 5) + 1;
+    SideScratch ss{base, base + bw, base + bw + a.cap_pix};
+    SideScratch ts{base + bw + 2 * a.cap_pix, base + 2 * bw + 2 * a.cap_pix, base + 2 * bw + 3 * a.cap_pix};
+    unsigned long long my_cand = 0, my_box = 0;
+    for (;;) {
+        unsigned long long pid = 0;
+        if (lane == 0) pid = atomicAdd(a.next, 1ull);
+        pid = __shfl_sync(0xffffffffu, pid, 0);
+        if (pid >= a.n) break;
+        const uint32_t s = a.pairs[2 * pid], t = a.pairs[2 * pid + 1];
+        const PolyHdr &S = sv.hdr[s];
+        const PolyHdr &T = sv.hdr[a.tgt_base + t];
+        if (S.err || T.err) {
+            if (lane == 0) a.out[pid] = W_BADPOLY;
+            continue;
+        }
+        if (S.num_layers == 0 || T.num_layers == 0) {
+            if (lane == 0) a.out[pid] = W_RETRY;
+            continue;
+        }
+        const uint32_t sL = S.num_layers - 1, tL = T.num_layers - 1;
+        // initial queue: every layer-0 pixel pair (Ideal.cpp:2483-2488)
+        uint32_t nqs, nqt;
+        {
+            LayerGeom g0;
+            layer_geom(S, 0, g0);
+            nqs = (uint32_t)(g0.dimx * g0.dimy);
+            for (uint32_t k = lane; k < nqs; k += 32) ss.q[k] = k;
+            layer_geom(T, 0, g0);
+            nqt = (uint32_t)(g0.dimx * g0.dimy);
+            for (uint32_t k = lane; k < nqt; k += 32) ts.q[k] = k;
+            __syncwarp();
+        }
+        uint32_t i = 0, j = 0;
+        uint8_t result = W_FALSE;
+        for (;;) {
+            LayerGeom gs, gt;
+            layer_geom(S, i, gs);
+            layer_geom(T, j, gt);
+            const double s_step = gs.step_x, t_step = gt.step_x;
+            bool s_next = false, t_next = false;
+            if (i < sL && (s_step >= t_step || j >= tL)) {
+                i++;
+                s_next = true;
+            }
+            if (j < tL && (s_step <= t_step || i >= sL)) {
+                j++;
+                t_next = true;
+            }
+            if (nqs == 0 || nqt == 0) break;  // empty queue
+            uint32_t np_s = next_set(S, sv.status, s_next, i, ss.q, nqs, ss, lane, cc);
+            uint32_t np_t = next_set(T, sv.status, t_next, j, ts.q, nqt, ts, lane, cc);
+            layer_geom(S, i, gs);
+            layer_geom(T, j, gt);
+            // smallest box max-distance; any <= d decides (Ideal.cpp:2557-2570)
+            const uint64_t tot = (uint64_t)np_s * np_t;
+            double mbd = 100000.0;
+            bool hit = false;
+            for (uint64_t k = lane; k < tot; k += 32) {
+                Box b1 = pixel_box(gs, (int)ss.p[k / np_t]);
+                Box b2 = pixel_box(gt, (int)ts.p[k % np_t]);
+                double md = box_max_distance(b1, b2, geo);
+                if (md <= a.thr) {
+                    hit = true;
+                    break;
+                }
+                mbd = mbd < md ? mbd : md;
+            }
+            if (lane == 0) my_box += tot;
+            if (__any_sync(0xffffffffu, hit)) {
+                result = W_TRUE;
+                break;
+            }
+            for (int o = 16; o; o >>= 1) {
+                double v = __shfl_xor_sync(0xffffffffu, mbd, o);
+                mbd = mbd < v ? mbd : v;
+            }
+            const bool last = !s_next && !t_next;
+            // keep pairs with box distance <= d and < the smallest max-distance
+            bool overflow = false;
+            unsigned long long nc = 0;
+            for (uint64_t k0 = 0; k0 < tot; k0 += 32) {
+                uint64_t k = k0 + lane;
+                bool keep = false;
+                uint32_t id1 = 0, id2 = 0;
+                Box b1, b2;
+                double lo = 0;
+                if (k < tot) {
+                    id1 = ss.p[k / np_t];
+                    id2 = ts.p[k % np_t];
+                    b1 = pixel_box(gs, (int)id1);
+                    b2 = pixel_box(gt, (int)id2);
+                    lo = box_distance(b1, b2, geo);
+                    keep = !(lo > a.thr) && lo < mbd;
+                }
+                if (!last) {
+                    if (keep) {
+                        set_bit(ss.bits, id1);
+                        set_bit(ts.bits, id2);
+                    }
+                    continue;
+                }
+                unsigned m = __ballot_sync(0xffffffffu, keep);
+                if (!m) continue;
+                unsigned long long at = 0;
+                if (lane == 0) at = atomicAdd(a.ncand, (unsigned long long)__popc(m));
+                at = __shfl_sync(0xffffffffu, at, 0) + __popc(m & ((1u << lane) - 1));
+                nc += __popc(m);
+                if (keep) {
+                    if (at < a.cand_cap) {
+                        // Ideal.cpp:2587-2606
+                        double hi = box_max_distance(b1, b2, geo);
+                        int pf = classify(sv.areas[S.pix + id1] + sv.areas[T.pix + id2],
+                                          S.step_x * S.step_y + T.step_x * T.step_y, 20);
+                        WCand c;
+                        c.apx = lo + (double)c_mean20[pf] * (hi - lo);
+                        c.lo = lo;
+                        c.hi = hi;
+                        c.pair = (uint32_t)pid;
+                        c.id1 = (int32_t)id1;
+                        c.id2 = (int32_t)id2;
+                        c.pad = 0;
+                        a.cand[at] = c;
+                    } else {
+                        overflow = true;
+                    }
+                }
+            }
+            if (last) {
+                overflow = __any_sync(0xffffffffu, overflow);
+                result = overflow ? W_RETRY : (nc ? W_REFINE : W_FALSE);
+                if (lane == 0) my_cand += nc;
+                break;
+            }
+            __syncwarp();
+            nqs = compact_bits(ss.bits, (uint32_t)(gs.dimx * gs.dimy), ss.q, lane);
+            nqt = compact_bits(ts.bits, (uint32_t)(gt.dimx * gt.dimy), ts.q, lane);
+        }
+        // leave the scratch bitmaps clean for the next pair
+        __syncwarp();
+        for (uint32_t w = lane; w < bw; w += 32) {
+            ss.bits[w] = 0u;
+            ts.bits[w] = 0u;
+        }
+        __syncwarp();
+        if (lane == 0) a.out[pid] = result;
+    }
+    if (lane == 0) {
+        atomicAdd(&a.stats[0], my_cand);
+        atomicAdd(&a.stats[1], my_box);
+    }
+}
+
+// first candidate of each pair (candidates sorted by pair)
+__global__ void k_cand_bounds(const WCand *__restrict__ c, uint64_t n, uint64_t *__restrict__ first) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        if (k == 0 || c[k - 1].pair != c[k].pair) first[c[k].pair] = k;
+    }
+}
+
+struct RefineArgs {
+    const uint32_t *pairs;
+    uint64_t n;
+    uint64_t tgt_base;
+    double thr;
+    int geo;
+    const WCand *cand;
+    uint64_t ncand;
+    const uint64_t *first;
+    uint8_t *out;
+    unsigned long long *next;
+    unsigned long long *stats;  // seq pairs, point-segment tests
+};
+
+// Ideal.cpp:2612-2643 in the candidates' order.
+__global__ void __launch_bounds__(256) k_within_refine(const StoreView sv, RefineArgs a) {
+    const int lane = threadIdx.x & 31;
+    const bool geo = a.geo != 0;
+    const int cc = sv.category_count;
+    unsigned long long my_seq = 0, my_tests = 0;
+    for (;;) {
+        unsigned long long pid = 0;
+        if (lane == 0) pid = atomicAdd(a.next, 1ull);
+        pid = __shfl_sync(0xffffffffu, pid, 0);
+        if (pid >= a.n) break;
+        if (a.out[pid] != W_REFINE) continue;
+        const uint32_t s = a.pairs[2 * pid], t = a.pairs[2 * pid + 1];
+        const PolyHdr &S = sv.hdr[s];
+        const PolyHdr &T = sv.hdr[a.tgt_base + t];
+        const uint64_t b = a.first[pid];
+        uint64_t e = b;
+        while (e < a.ncand && a.cand[e].pair == pid) e++;
+        const uint32_t *so = sv.offset + S.off, *to = sv.offset + T.off;
+        const uint2 *sseq = sv.seq + S.seq, *tseq = sv.seq + T.seq;
+        const float2 *sr = sv.ring + S.ring, *tr = sv.ring + T.ring;
+        double min_dist = 100000.0;
+        int decided = -1;
+        for (uint64_t k = b; k < e && decided < 0; k++) {
+            // lower bound of every later candidate
+            double ref = 100000.0;
+            for (uint64_t q = k + 1 + lane; q < e; q += 32) ref = ref < a.cand[q].lo ? ref : a.cand[q].lo;
+            for (int o = 16; o; o >>= 1) {
+                double v = __shfl_xor_sync(0xffffffffu, ref, o);
+                ref = ref < v ? ref : v;
+            }
+            const int id1 = a.cand[k].id1, id2 = a.cand[k].id2;
+            uint32_t a0 = 0, a1 = 0, b0 = 0, b1 = 0;
+            if (show_status(sv.status[S.st + id1], cc) == 1) {
+                a0 = so[id1];
+                a1 = so[id1 + 1];
+            }
+            if (show_status(sv.status[T.st + id2], cc) == 1) {
+                b0 = to[id2];
+                b1 = to[id2 + 1];
+            }
+            for (uint32_t ia = a0; ia < a1 && decided < 0; ia++) {
+                uint2 e1 = sseq[ia];
+                for (uint32_t jb = b0; jb < b1; jb++) {
+                    uint2 e2 = tseq[jb];
+                    if (e1.y < 2 || e2.y < 2) continue;
+                    // segment_to_segment_within_batch(target seq, source seq):
+                    // e2.y target points vs e1.y - 1 source segments, and back
+                    const uint32_t n1 = e2.y * (e1.y - 1), n2 = e1.y * (e2.y - 1);
+                    double m = 1.7976931348623157e308;
+                    for (uint32_t k2 = lane; k2 < n1 + n2; k2 += 32) {
+                        double d;
+                        if (k2 < n1) {
+                            uint32_t pi = k2 / (e1.y - 1), si = k2 % (e1.y - 1);
+                            d = pt_seg_dist(tr[e2.x + pi], sr[e1.x + si], sr[e1.x + si + 1], geo);
+                        } else {
+                            uint32_t r = k2 - n1;
+                            uint32_t pi = r / (e2.y - 1), si = r % (e2.y - 1);
+                            d = pt_seg_dist(sr[e1.x + pi], tr[e2.x + si], tr[e2.x + si + 1], geo);
+                        }
+                        m = m < d ? m : d;
+                    }
+                    for (int o = 16; o; o >>= 1) {
+                        double v = __shfl_xor_sync(0xffffffffu, m, o);
+                        m = m < v ? m : v;
+                    }
+                    if (lane == 0) {
+                        my_seq++;
+                        my_tests += n1 + n2;
+                    }
+                    min_dist = min_dist < m ? min_dist : m;
+                    if (min_dist < a.thr) {
+                        decided = 1;
+                        break;
+                    } else if (min_dist < ref) {
+                        decided = 0;
+                        break;
+                    }
+                }
+            }
+        }
+        if (lane == 0) a.out[pid] = decided == 1 ? W_TRUE : W_FALSE;
+    }
+    if (lane == 0) {
+        atomicAdd(&a.stats[0], my_seq);
+        atomicAdd(&a.stats[1], my_tests);
+    }
+}
+
+__global__ void k_within_count(const uint8_t *__restrict__ out, uint64_t n, unsigned long long *found,
+                               unsigned long long *retry) {
+    unsigned long long f = 0, r = 0;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        f += out[k] == W_TRUE;
+        r += out[k] == W_RETRY;
+    }
+    for (int o = 16; o; o >>= 1) {
+        f += __shfl_xor_sync(0xffffffffu, f, o);
+        r += __shfl_xor_sync(0xffffffffu, r, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(found, f);
+        atomicAdd(retry, r);
+    }
+}
+
+__global__ void k_gather_retry(const uint32_t *__restrict__ pairs, const uint8_t *__restrict__ out, uint64_t n,
+                               uint32_t *__restrict__ rp, uint64_t *__restrict__ ridx,
+                               unsigned long long *__restrict__ cnt) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        if (out[k] != W_RETRY) continue;
+        unsigned long long at = atomicAdd(cnt, 1ull);
+        rp[2 * at] = pairs[2 * k];
+        rp[2 * at + 1] = pairs[2 * k + 1];
+        ridx[at] = k;
+    }
+}
+
+__global__ void k_scatter_retry(const uint8_t *__restrict__ rout, const uint64_t *__restrict__ ridx, uint64_t n,
+                                uint8_t *__restrict__ out) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
+        out[ridx[k]] = rout[k];
+}
+
+static unsigned gbw(uint64_t n) {
+    uint64_t g = (n + 255) / 256;
+    uint64_t cap = 32ull * sm_count();
+    if (g > cap) g = cap;
+    return (unsigned)(g ? g : 1);
+}
+
+// One descend + sort + refine round over n device pairs with out in device memory.
+static int within_round(farm_store *s, const uint32_t *dpairs, uint64_t n, uint8_t *dout, double thr, int geo,
+                        uint64_t tgt_base, uint32_t cap_pix, int nwarps, uint64_t cand_cap, farm_stats *acc,
+                        int &launches) {
+    cudaStream_t st = s->stream;
+    StoreView sv = s->view();
+    const uint64_t bw = (cap_pix >> 5) + 1;
+    const uint64_t words = 2 * (bw + 2ull * cap_pix);
+    DevBuf &scr = s->s[26], &cand = s->s[27], &tmp = s->s[28], &first = s->s[29];
+    FARM_TRY(scr.ensure(4 * words * (uint64_t)nwarps + 64));
+    FARM_CUDA(cudaMemsetAsync(scr.p, 0, 4 * words * (uint64_t)nwarps, st));
+    FARM_TRY(cand.ensure(sizeof(WCand) * cand_cap + 64));
+    FARM_TRY(s->d_counters.ensure(256));
+    unsigned long long *ctr = s->d_counters.as<unsigned long long>();
+    FARM_CUDA(cudaMemsetAsync(ctr, 0, 256, st));
+    WithinArgs wa;
+    wa.pairs = dpairs;
+    wa.n = n;
+    wa.tgt_base = tgt_base;
+    wa.thr = thr;
+    wa.geo = geo;
+    wa.cap_pix = cap_pix;
+    wa.scratch = scr.as<uint32_t>();
+    wa.scratch_words = words;
+    wa.cand = cand.as<WCand>();
+    wa.ncand = ctr + 1;
+    wa.cand_cap = cand_cap;
+    wa.out = dout;
+    wa.next = ctr + 0;
+    wa.stats = ctr + 2;
+    k_within_descend<<<nwarps / 8, 256, 0, st>>>(sv, wa);
+    launches++;
+    unsigned long long hc[4];
+    FARM_CUDA(cudaMemcpyAsync(hc, ctr, 32, cudaMemcpyDeviceToHost, st));
+    FARM_CUDA(cudaStreamSynchronize(st));
+    uint64_t nc = hc[1] < cand_cap ? hc[1] : cand_cap;
+    acc->border_pairs += hc[3];
+    acc->in_hits += hc[2];  // candidate pixel pairs
+    if (nc) {
+        // order by pair, then the reference's tuple (Ideal.cpp:2612)
+        size_t bytes = 0;
+        FARM_CUDA(cub::DeviceMergeSort::SortKeys(nullptr, bytes, cand.as<WCand>(), (int64_t)nc, WCandLess(), st));
+        FARM_TRY(tmp.ensure(bytes + 64));
+        FARM_CUDA(cub::DeviceMergeSort::SortKeys(tmp.p, bytes, cand.as<WCand>(), (int64_t)nc, WCandLess(), st));
+        FARM_TRY(first.ensure(8 * n + 64));
+        k_cand_bounds<<<gbw(nc), 256, 0, st>>>(cand.as<WCand>(), nc, first.as<uint64_t>());
+        RefineArgs ra;
+        ra.pairs = dpairs;
+        ra.n = n;
+        ra.tgt_base = tgt_base;
+        ra.thr = thr;
+        ra.geo = geo;
+        ra.cand = cand.as<WCand>();
+        ra.ncand = nc;
+        ra.first = first.as<uint64_t>();
+        ra.out = dout;
+        ra.next = ctr + 4;
+        ra.stats = ctr + 5;
+        k_within_refine<<<sm_count() * 8, 256, 0, st>>>(sv, ra);
+        launches += 2;
+        unsigned long long hs[2];
+        FARM_CUDA(cudaMemcpyAsync(hs, ctr + 5, 16, cudaMemcpyDeviceToHost, st));
+        FARM_CUDA(cudaStreamSynchronize(st));
+        acc->segment_tests += hs[1];
+    }
+    return FARM_OK;
+}
+
+int within(farm_store *s, const uint32_t *pairs, uint64_t n, double distance, int geography, int self, int mem,
+           uint8_t *out, uint64_t *found, farm_stats *st) {
+    if (!s->rasterized || !s->ropts.hierarchy) {
+        set_error("farm_within: rasterize with hierarchy first");
+        return FARM_EINVAL;
+    }
+    if (!self && s->n_side[1] == 0) {
+        set_error("farm_within: no target side loaded (or pass target_is_source)");
+        return FARM_EINVAL;
+    }
+    FARM_TRY(ensure_tables(s->device));
+    cudaStream_t stream = s->stream;
+    const uint64_t tgt_base = self ? 0 : s->n_side[0];
+    const uint32_t *dpairs = pairs;
+    if (mem == FARM_MEM_HOST && n) {
+        FARM_TRY(s->d_pairs.ensure(8 * n));
+        FARM_CUDA(cudaMemcpyAsync(s->d_pairs.p, pairs, 8 * n, cudaMemcpyHostToDevice, stream));
+        dpairs = s->d_pairs.as<uint32_t>();
+    }
+    uint8_t *dout = out;
+    if (mem == FARM_MEM_HOST || !out) {
+        FARM_TRY(s->d_out.ensure(n + 64));
+        dout = s->d_out.as<uint8_t>();
+    }
+    // the largest finest raster bounds a warp's pixel sets
+    uint32_t cap = 64;
+    {
+        std::vector<PolyHdr> hh(s->n_poly);
+        FARM_CUDA(cudaMemcpyAsync(hh.data(), s->d_hdr.p, sizeof(PolyHdr) * s->n_poly, cudaMemcpyDeviceToHost, stream));
+        FARM_CUDA(cudaStreamSynchronize(stream));
+        for (auto &h : hh) {
+            if (h.err) continue;
+            for (uint32_t li = 0; li < h.num_layers; li++) {
+                LayerGeom g;
+                layer_geom(h, li, g);
+                uint32_t np = (uint32_t)(g.dimx * g.dimy);
+                if (np > cap) cap = np;
+            }
+        }
+        cap = (cap + 31) & ~31u;
+    }
+    farm_stats acc;
+    memset(&acc, 0, sizeof acc);
+    int launches = 0;
+    FARM_CUDA(cudaEventRecord(s->ev[6], stream));
+    int nwarps = sm_count() * 8 * 2;
+    size_t freeb = 0, totb = 0;
+    cudaMemGetInfo(&freeb, &totb);
+    const uint64_t words = 2 * (((cap >> 5) + 1) + 2ull * cap);
+    while (nwarps > 64 && 4ull * words * (uint64_t)nwarps > freeb / 4) nwarps /= 2;
+    uint64_t cand_cap = 1ull << 24;
+    if (n) FARM_TRY(within_round(s, dpairs, n, dout, distance, geography, tgt_base, cap, nwarps, cand_cap, &acc,
+                                 launches));
+    // pairs whose candidates did not fit: gather and rerun with a larger buffer
+    for (int round = 0; round < 8 && n; round++) {
+        FARM_TRY(s->d_counters.ensure(256));
+        unsigned long long *ctr = s->d_counters.as<unsigned long long>() + 16;
+        FARM_CUDA(cudaMemsetAsync(ctr, 0, 16, stream));
+        k_within_count<<<gbw(n), 256, 0, stream>>>(dout, n, ctr, ctr + 1);
+        launches++;
+        unsigned long long hc[2];
+        FARM_CUDA(cudaMemcpyAsync(hc, ctr, 16, cudaMemcpyDeviceToHost, stream));
+        FARM_CUDA(cudaStreamSynchronize(stream));
+        if (hc[1] == 0) break;
+        DevBuf &rp = s->s[30], &ro = s->s[31];
+        FARM_TRY(rp.ensure((8 + 8) * hc[1] + 64));
+        FARM_TRY(ro.ensure(hc[1] + 64));
+        uint32_t *rpairs = rp.as<uint32_t>();
+        uint64_t *ridx = reinterpret_cast<uint64_t *>(rpairs + 2 * hc[1] + 2);
+        FARM_CUDA(cudaMemsetAsync(ctr, 0, 8, stream));
+        k_gather_retry<<<gbw(n), 256, 0, stream>>>(dpairs, dout, n, rpairs, ridx, ctr);
+        launches++;
+        cand_cap *= 4;
+        int rw = nwarps > 256 ? 256 : nwarps;
+        FARM_TRY(within_round(s, rpairs, hc[1], ro.as<uint8_t>(), distance, geography, tgt_base, cap, rw, cand_cap,
+                              &acc, launches));
+        k_scatter_retry<<<gbw(hc[1]), 256, 0, stream>>>(ro.as<uint8_t>(), ridx, hc[1], dout);
+        launches++;
+    }
+    FARM_CUDA(cudaEventRecord(s->ev[7], stream));
+    unsigned long long *fc = s->d_counters.as<unsigned long long>() + 20;
+    FARM_CUDA(cudaMemsetAsync(fc, 0, 16, stream));
+    k_within_count<<<gbw(n), 256, 0, stream>>>(dout, n, fc, fc + 1);
+    launches++;
+    unsigned long long hf[2] = {0, 0};
+    FARM_CUDA(cudaMemcpyAsync(hf, fc, 16, cudaMemcpyDeviceToHost, stream));
+    if (mem == FARM_MEM_HOST && out && n) FARM_CUDA(cudaMemcpyAsync(out, dout, n, cudaMemcpyDeviceToHost, stream));
+    FARM_CUDA(cudaStreamSynchronize(stream));
+    s->launches += (uint64_t)launches;
+    if (hf[1]) {
+        set_error("farm_within: some pairs exceeded the candidate buffer after retries");
+        return FARM_ENOMEM;
+    }
+    if (found) *found = hf[0];
+    if (st) {
+        memset(st, 0, sizeof *st);
+        st->pairs = n;
+        st->found = hf[0];
+        st->border_pairs = acc.border_pairs;
+        st->segment_tests = acc.segment_tests;
+        st->in_hits = acc.in_hits;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, s->ev[6], s->ev[7]);
+        st->ms_total = ms;
+        st->ms_stage[1] = ms;
+        st->kernel_launches = launches;
+    }
+    return FARM_OK;
+}
+
+}  // namespace farm
+
+extern "C" int farm_within(farm_store *s, const uint32_t *pairs, uint64_t n, double distance, int geography,
+                           int target_is_source, int mem, uint8_t *out, uint64_t *found, farm_stats *st) {
+    using namespace farm;
+    if (!s || (n && !pairs)) {
+        set_error("invalid arguments to farm_within");
+        return FARM_EINVAL;
+    }
+    return within(s, pairs, n, distance, geography, target_is_source, mem, out, found, st);
+}

@@ -101,11 +101,11 @@ class Store:
             self.load(1, target.off, target.xy)
 
     def rasterize(self, vpr: int = 10, category_count: int = 16, hierarchy: bool = False,
-                  strict: bool = True) -> int:
+                  strict: bool = True, grid_extent: float = 0.0) -> int:
         """Rasterize every loaded polygon. With strict=False, polygons on which
         the reference asserts or never terminates (FARM_EASSERT) are reported
         by count instead of raising; queries then return 2 for their pairs."""
-        o = RasterOpts(vpr, category_count, int(hierarchy), 0)
+        o = RasterOpts(vpr, category_count, int(hierarchy), 0, float(grid_extent))
         rc = self._lib.farm_rasterize(self._h, C.byref(o))
         if rc == -10 and not strict:
             return int((self.raster_errors(0) != 0).sum() + (self.raster_errors(1) != 0).sum())

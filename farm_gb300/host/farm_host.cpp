@@ -124,12 +124,24 @@ int farm_gen_fill(const farm_gen_params *gp, uint64_t seed, uint64_t first, uint
             double lr0 = std::log(gp->r_lo), lr1 = std::log(gp->r_hi);
             double rbar = std::exp(lr0 + rng_open01(seed, i, S_R, 0) * (lr1 - lr0));
             double phi = two_pi * rng_open01(seed, i, S_PHI, 0);
-            // sorted uniform angles as normalised partial sums of Exp(1) gaps
+            // sorted uniform angles as normalised partial sums of Exp(1) gaps;
+            // redrawn (next attempt of the same counter stream) until no
+            // angular gap exceeds 2*pi/3, so the ring is simple and star-shaped
+            // about its centre (a gap beyond pi lets a chord cross other edges)
             cum.resize(n + 1);
             double acc = 0.0;
-            for (uint32_t j = 0; j <= n; j++) {
-                acc += -std::log(rng_open01(seed, i, S_GAP, j));
-                cum[j] = acc;
+            for (uint64_t attempt = 0;; attempt++) {
+                acc = 0.0;
+                double gmax = 0.0, g0 = 0.0, gap = 0.0;
+                for (uint32_t j = 0; j <= n; j++) {
+                    gap = -std::log(rng_open01(seed, i, S_GAP, attempt * (uint64_t)(n + 1) + j));
+                    acc += gap;
+                    cum[j] = acc;
+                    if (j == 0) g0 = gap;
+                    else if (j < n) gmax = std::max(gmax, gap);
+                }
+                gmax = std::max(gmax, g0 + gap);  // the wrap-around gap
+                if (gmax / acc <= 1.0 / 3.0 || attempt >= 64) break;
             }
             float *out = xy + 2 * off[k];
             for (uint32_t j = 0; j < n; j++) {

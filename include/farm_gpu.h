@@ -56,6 +56,11 @@ typedef struct farm_raster_opts {
     int32_t category_count; /* -w: fill classes 4/16/256 (reference fixes 16) */
     int32_t hierarchy;      /* -h: layered rasters (needed by within) */
     int32_t reserved;
+    /* Extent of the hierarchy's global grid in coordinate units: its base step
+     * is that extent / 2^25 rounded to 2 significant digits. 0 means 360 (the
+     * reference's degrees, UniversalGrid.h:29-35); projected coordinates need
+     * a larger extent (e.g. 1e7 for metres up to 5e6). */
+    double grid_extent;
 } farm_raster_opts;
 
 typedef struct farm_stats {
@@ -154,13 +159,6 @@ int farm_event_record(farm_store *s, int slot);
 int farm_event_elapsed(farm_store *s, int a, int b, double *ms);
 /* Engine kernels launched through this store so far. */
 uint64_t farm_store_launches(farm_store *s);
-
-/* Seeded star polygons generated on the device (benchmark inputs): d_off
- * (count + 1 entries, device memory) holds the offsets of farm_gen_counts()'s
- * counts, d_xy receives the rings. Same recipe as farm_gen_fill() on the host;
- * the device libm may round a coordinate differently in its last bit. */
-int farm_gen_device(double dom_lo, double dom_hi, double r_lo, double r_hi, double sigma, uint64_t seed,
-                    uint64_t first, uint64_t count, const uint64_t *d_off, float *d_xy);
 
 #ifdef __cplusplus
 }

@@ -37,9 +37,11 @@ const char *farm_host_last_error(void);
  * independently and in parallel:
  *   centre uniform in [dom_lo, dom_hi]^2; mean radius log-uniform in
  *   [r_lo, r_hi]; vertex count log-uniform in [n_lo, n_hi]; vertex angles
- *   sorted uniform over one turn (counter-clockwise); per-vertex radius =
- *   mean radius x lognormal(0, sigma). Coordinates are computed in FP64 and
- *   rounded to float32, as a .dt file stores them. */
+ *   sorted uniform over one turn (counter-clockwise; redrawn until no angular
+ *   gap exceeds a third of a turn, which keeps every ring simple and
+ *   star-shaped); per-vertex radius = mean radius x lognormal(0, sigma).
+ *   Coordinates are computed in FP64 and rounded to float32, as a .dt file
+ *   stores them. */
 typedef struct farm_gen_params {
     double dom_lo, dom_hi;
     double r_lo, r_hi;

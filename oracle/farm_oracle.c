@@ -628,9 +628,9 @@ static void init_raster(fo_raster *R, int num_pixels) {
 }
 
 /* MyRaster.cpp:444-491 with UniversalGrid::configure(25) (UniversalGrid.h:29-35) */
-static int grid_align(fo_raster *R) {
+static int grid_align(fo_raster *R, double extent) {
     int max_layers = 25;
-    double gstep = round_sig(360.0 / pow(2, max_layers), 2);
+    double gstep = round_sig((extent > 0 ? extent : 360.0) / pow(2, max_layers), 2);
     int flag1 = 0, flag2 = 0;
     double x = gstep, y = gstep;
     if (R->step_x <= x) { R->step_x = x; flag1 = 1; }
@@ -986,7 +986,7 @@ int fo_rasterize(const float *ring, uint32_t nv, const fo_opts *o, fo_raster *R)
     init_raster(R, (int)(nv / (uint32_t)o->vpr));
     int err = FO_OK;
     if (o->hierarchy) {
-        err = grid_align(R);
+        err = grid_align(R, o->grid_extent);
         if (!err) err = layering(R, 1);
     } else {
         R->status_size = (uint32_t)R->dimx * (uint32_t)R->dimy;
@@ -1585,10 +1585,19 @@ static double half_integral(const pt *a, uint32_t ma, const pt *b, uint32_t mb, 
     return 0.5 * acc;
 }
 
+static double orient(const pt *r, uint32_t m, double ox, double oy) {
+    double s = 0;
+    for (uint32_t i = 0; i + 1 < m; i++)
+        s += ((double)r[i].x - ox) * ((double)r[i + 1].y - oy) - ((double)r[i + 1].x - ox) * ((double)r[i].y - oy);
+    return s >= 0 ? 1.0 : -1.0;
+}
+
 double fo_intersection_area(const float *a, uint32_t ma, const float *b, uint32_t mb) {
     const pt *A = (const pt *)a, *B = (const pt *)b;
     if (ma < 4 || mb < 4) return 0.0;
     double ox = A[0].x, oy = A[0].y;
-    double s = half_integral(A, ma, B, mb, ox, oy) + half_integral(B, mb, A, ma, ox, oy);
+    /* each boundary integrated with its own orientation */
+    double s = orient(A, ma, ox, oy) * half_integral(A, ma, B, mb, ox, oy) +
+               orient(B, mb, ox, oy) * half_integral(B, mb, A, ma, ox, oy);
     return fabs(s);
 }

@@ -56,6 +56,7 @@ typedef struct fo_opts {
     int hierarchy;      /* -h: grid_align + layering (preprocessing.cpp:17-19) */
     int category_count; /* fill classes; the reference fixes 16 (MyRaster.h:33) */
     int merge_carry;    /* see fo_rasterize(): how merge_status seeds its status */
+    double grid_extent; /* hierarchy grid extent; 0 = 360 (the reference's degrees) */
 } fo_opts;
 
 /* Rasterize one polygon. `ring` holds the in-memory ring the reference builds

@@ -32,7 +32,8 @@ class FoRaster(C.Structure):
 
 
 class FoOpts(C.Structure):
-    _fields_ = [("vpr", C.c_int), ("hierarchy", C.c_int), ("category_count", C.c_int), ("merge_carry", C.c_int)]
+    _fields_ = [("vpr", C.c_int), ("hierarchy", C.c_int), ("category_count", C.c_int), ("merge_carry", C.c_int),
+                ("grid_extent", C.c_double)]
 
 
 class FoCounters(C.Structure):
@@ -79,11 +80,11 @@ class Raster:
     """One rasterized polygon (owns the C allocation)."""
 
     def __init__(self, stored: np.ndarray, vpr: int, hierarchy: bool = False, category_count: int = 16,
-                 merge_carry: int = 1):
+                 merge_carry: int = 1, grid_extent: float = 0.0):
         self.ring = mem_ring(stored)
         self.nv = len(stored) + 1
         self.r = FoRaster()
-        o = FoOpts(vpr, int(hierarchy), category_count, merge_carry)
+        o = FoOpts(vpr, int(hierarchy), category_count, merge_carry, float(grid_extent))
         rc = lib().fo_rasterize(self.ring.ctypes.data_as(C.POINTER(C.c_float)), self.nv, C.byref(o), C.byref(self.r))
         self.rc = rc
         if rc != 0:
@@ -119,8 +120,9 @@ class Raster:
         return out
 
 
-def rasterize_set(ps, vpr: int, hierarchy: bool = False, category_count: int = 16, merge_carry: int = 1):
-    return [Raster(ps.ring(k), vpr, hierarchy, category_count, merge_carry) for k in range(ps.n)]
+def rasterize_set(ps, vpr: int, hierarchy: bool = False, category_count: int = 16, merge_carry: int = 1,
+                  grid_extent: float = 0.0):
+    return [Raster(ps.ring(k), vpr, hierarchy, category_count, merge_carry, grid_extent) for k in range(ps.n)]
 
 
 def intersect(rs: Raster, rt: Raster, counters: bool = False):

@@ -55,7 +55,9 @@ PAIR_CASES = [
 
 
 def gz(src: Path, dst: Path) -> None:
-    with open(src, "rb") as f, gzip.open(dst, "wb", compresslevel=9) as g:
+    # mtime=0 keeps the fixture bytes reproducible
+    with open(src, "rb") as f, open(dst, "wb") as raw, gzip.GzipFile(fileobj=raw, mode="wb", compresslevel=9,
+                                                                    mtime=0) as g:
         shutil.copyfileobj(f, g)
 
 
