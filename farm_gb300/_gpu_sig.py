@@ -50,6 +50,18 @@ def declare(lib):
     lib.farm_sync.argtypes = [vp]
     lib.farm_raster_errors.argtypes = [vp, C.c_int, vp, C.c_uint64]
     lib.farm_intersect_static.argtypes = [vp, vp, C.c_uint64, vp, u64p]
+    lib.farm_tc_gemm_test.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int]
+    f32p = C.POINTER(C.c_float)
+    lib.farm_mlp_param_count.restype = C.c_uint64
+    lib.farm_mlp_param_count.argtypes = []
+    lib.farm_mlp_init.argtypes = [vp, C.c_uint64]
+    lib.farm_mlp_get.argtypes = [vp, vp]
+    lib.farm_mlp_set.argtypes = [vp, vp]
+    lib.farm_mlp_set_band.argtypes = [vp, C.c_float, C.c_float]
+    lib.farm_mlp_features.argtypes = [vp, vp, C.c_uint64, vp, C.c_uint64]
+    lib.farm_mlp_grad.argtypes = [vp, vp, vp, C.c_uint64, C.c_uint64, f32p, vp]
+    lib.farm_mlp_train.argtypes = [vp, vp, vp, C.c_uint64, C.c_int, C.c_int, C.c_float, C.c_uint64, f32p]
+    lib.farm_mlp_predict.argtypes = [vp, vp, C.c_uint64, vp]
     lib.farm_event_record.argtypes = [vp, C.c_int]
     lib.farm_event_elapsed.argtypes = [vp, C.c_int, C.c_int, f64p]
     lib.farm_store_launches.argtypes = [vp]

@@ -205,5 +205,6 @@ struct farm_store {
     farm::DevBuf d_pairs, d_out, d_counters;
     cudaEvent_t ev[8] = {};
     uint64_t launches = 0;  // engine kernels launched through this store
+    void *mlp = nullptr;    // learned scorer state (mlp.cu)
     farm::StoreView view() const;
 };

@@ -11,6 +11,8 @@
 
 namespace farm {
 
+void mlp_free(void *p);  // mlp.cu
+
 static thread_local std::string g_error;
 
 void set_error(const std::string &msg) { g_error = msg; }
@@ -148,6 +150,8 @@ int farm_store_create(farm_store **out) {
 void farm_store_destroy(farm_store *s) {
     if (!s) return;
     cudaStreamSynchronize(s->stream);
+    farm::mlp_free(s->mlp);
+    s->mlp = nullptr;
     DevBuf *bufs[] = {&s->d_xy_in, &s->d_off, &s->d_ring, &s->d_hdr, &s->d_status, &s->d_offset, &s->d_seq,
                       &s->d_hoff, &s->d_hnodes, &s->d_voff, &s->d_vnodes, &s->d_areas, &s->cub_tmp,
                       &s->d_pairs, &s->d_out, &s->d_counters};

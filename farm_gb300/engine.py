@@ -151,6 +151,53 @@ class Store:
         self.last_stats = stats_dict(st)
         return out
 
+    # ---- learned scorer (device tensors: torch CUDA) -------------------
+    def mlp_init(self, seed: int = 1) -> None:
+        check_gpu(self._lib.farm_mlp_init(self._h, seed))
+
+    def mlp_params(self) -> np.ndarray:
+        out = np.zeros(int(self._lib.farm_mlp_param_count()), np.float32)
+        check_gpu(self._lib.farm_mlp_get(self._h, C.c_void_p(out.ctypes.data)))
+        return out
+
+    def mlp_load(self, params: np.ndarray) -> None:
+        params = np.ascontiguousarray(params, dtype=np.float32)
+        assert params.size == int(self._lib.farm_mlp_param_count())
+        check_gpu(self._lib.farm_mlp_set(self._h, C.c_void_p(params.ctypes.data)))
+
+    def mlp_band(self, lo: float, hi: float) -> None:
+        check_gpu(self._lib.farm_mlp_set_band(self._h, lo, hi))
+
+    def mlp_features(self, d_pairs, rows: int = 0):
+        import torch
+        n = d_pairs.shape[0]
+        rows = max(rows, (n + 127) // 128 * 128)
+        X = torch.empty((rows, 576), dtype=torch.bfloat16, device=d_pairs.device)
+        check_gpu(self._lib.farm_mlp_features(self._h, C.c_void_p(d_pairs.data_ptr()), n, C.c_void_p(X.data_ptr()),
+                                              rows))
+        return X
+
+    def mlp_grad(self, X, y, n: int):
+        loss = C.c_float(0)
+        g = np.zeros(int(self._lib.farm_mlp_param_count()), np.float32)
+        check_gpu(self._lib.farm_mlp_grad(self._h, C.c_void_p(X.data_ptr()), C.c_void_p(y.data_ptr()), n,
+                                          X.shape[0], C.byref(loss), C.c_void_p(g.ctypes.data)))
+        return loss.value, g
+
+    def mlp_train(self, d_pairs, d_labels, epochs: int = 4, batch: int = 4096, lr: float = 2e-3,
+                  seed: int = 1) -> float:
+        loss = C.c_float(0)
+        check_gpu(self._lib.farm_mlp_train(self._h, C.c_void_p(d_pairs.data_ptr()), C.c_void_p(d_labels.data_ptr()),
+                                           d_pairs.shape[0], epochs, batch, lr, seed, C.byref(loss)))
+        return loss.value
+
+    def mlp_predict(self, d_pairs):
+        import torch
+        p = torch.empty(d_pairs.shape[0], dtype=torch.float32, device=d_pairs.device)
+        check_gpu(self._lib.farm_mlp_predict(self._h, C.c_void_p(d_pairs.data_ptr()), d_pairs.shape[0],
+                                             C.c_void_p(p.data_ptr())))
+        return p
+
     @property
     def launches(self) -> int:
         """Engine kernels launched through this store so far."""

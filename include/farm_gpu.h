@@ -146,6 +146,34 @@ int farm_raster_fetch(farm_store *s, int side, uint64_t index, farm_raster_view 
  * loaded and rasterized (those steps allocate). */
 int farm_intersect_static(farm_store *s, const uint32_t *pairs, uint64_t n, uint8_t *out, uint64_t *found);
 
+/* Diagnostics: the learned scorer's tcgen05 GEMM on its own, C[M x N] (fp32)
+ * = A[M x K] * B[N x K]^T (bf16, row-major, device pointers); M, N multiples
+ * of 16, K a multiple of 64, BN the tile width (64, 128, 256). */
+int farm_tc_gemm_test(const void *A, const void *B, float *C, int M, int N, int K, int BN);
+
+/* ---- learned scorer (FARM_MODE_LEARNED): 520 -> 256 -> 256 -> 1 MLP, GELU,
+ * bf16 weights/activations on tcgen05 tensor cores, fp32 accumulate. It takes
+ * the place of the reference's "-a" confidence heuristic
+ * (src/cuda/query_intersect.cu:100-134). Parameters are laid out as
+ * W1 [256 x 576] | W2 [256 x 256] | b1 [256] | b2 [256] | w3 [256] | b3. */
+uint64_t farm_mlp_param_count(void);
+int farm_mlp_init(farm_store *s, uint64_t seed);
+int farm_mlp_get(farm_store *s, float *params);
+int farm_mlp_set(farm_store *s, const float *params);
+/* Probability >= hi decides 1, <= lo decides 0, otherwise exact refinement. */
+int farm_mlp_set_band(farm_store *s, float lo, float hi);
+/* Features (bf16 [rows x 576], rows >= n, zero padding) of n device pairs. */
+int farm_mlp_features(farm_store *s, const uint32_t *d_pairs, uint64_t n, void *d_X, uint64_t rows);
+/* One forward/backward on device features and labels; loss and gradients
+ * (parameter layout) copied to host buffers; no update. */
+int farm_mlp_grad(farm_store *s, const void *d_X, const uint8_t *d_y, uint64_t n, uint64_t rows, float *loss,
+                  float *grad);
+/* Adam training on device pairs with device labels (exact results). */
+int farm_mlp_train(farm_store *s, const uint32_t *d_pairs, const uint8_t *d_labels, uint64_t n, int epochs,
+                   int batch, float lr, uint64_t seed, float *last_loss);
+/* Probabilities of n device pairs into d_prob (device fp32). */
+int farm_mlp_predict(farm_store *s, const uint32_t *d_pairs, uint64_t n, float *d_prob);
+
 /* Per-polygon rasterization status of one side (n = that side's polygon
  * count): 0, or FARM_EASSERT for a polygon on which the reference asserts or
  * never terminates (such polygons are reported, not rasterized). */

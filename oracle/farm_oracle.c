@@ -1190,6 +1190,36 @@ int fo_intersect(const fo_raster *s, const float *sring, const fo_raster *t, con
     return 0;
 }
 
+/* The reference's "-a" intersect heuristic (query_intersect.cu:32-134, the
+ * GPU path with use_approximation): an IN pixel overlapping a non-OUT pixel
+ * decides "true", as does any BORDER x BORDER pixel pair whose fill
+ * probability (mean decoded fill of both pixels over the larger pixel area)
+ * exceeds 1; no segment is tested. */
+int fo_intersect_heuristic(const fo_raster *s, const fo_raster *t) {
+    const int cc = 16;
+    window_t w = retrieve(s->mbr, s->step_x, s->step_y, s->dimx, s->dimy, t->mbr);
+    double spa = s->step_x * s->step_y, tpa = t->step_x * t->step_y;
+    double maxpa = spa > tpa ? spa : tpa;
+    for (int i = w.sx; i <= w.ex; i++)
+        for (int j = w.sy; j <= w.ey; j++) {
+            uint32_t pa = (uint32_t)(j * s->dimx + i);
+            if (rs_show(s, pa, cc) == 0) continue;
+            double bx[4] = {s->mbr[0] + i * s->step_x, s->mbr[1] + j * s->step_y, s->mbr[0] + (i + 1) * s->step_x,
+                            s->mbr[1] + (j + 1) * s->step_y};
+            window_t tw = retrieve(t->mbr, t->step_x, t->step_y, t->dimx, t->dimy, bx);
+            for (int u = tw.sx; u <= tw.ex; u++)
+                for (int v = tw.sy; v <= tw.ey; v++) {
+                    uint32_t pb = (uint32_t)(v * t->dimx + u);
+                    if (rs_show(t, pb, cc) == 0) continue;
+                    if (rs_show(s, pa, cc) == 2 || rs_show(t, pb, cc) == 2) return 1;
+                    double s_apx = (decode_area(s, pa, 1, cc) + decode_area(s, pa, 0, cc)) / 2;
+                    double t_apx = (decode_area(t, pb, 1, cc) + decode_area(t, pb, 0, cc)) / 2;
+                    if ((s_apx + t_apx) / maxpa > 1.0) return 1;
+                }
+        }
+    return 0;
+}
+
 /* Box.cpp:90-118 */
 static double box_distance(const double *a, const double *t, int geography) {
     if (!(t[0] > a[2] || t[2] < a[0] || t[1] > a[3] || t[3] < a[1])) return 0;

@@ -79,6 +79,9 @@ typedef struct fo_counters {
 int fo_intersect(const fo_raster *s, const float *sring, const fo_raster *t, const float *tring,
                  fo_counters *c);
 
+/* The reference's "-a" approximate intersect (query_intersect.cu:32-134). */
+int fo_intersect_heuristic(const fo_raster *s, const fo_raster *t);
+
 /* Ideal::within (Ideal.cpp:2475-2643) with the hierarchy. geography selects
  * the reference's degree-to-km scaling (always on in the reference); off is
  * the planar mode for projected coordinates. */

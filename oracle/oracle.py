@@ -54,6 +54,7 @@ def lib() -> C.CDLL:
         L.fo_raster_free.argtypes = [C.POINTER(FoRaster)]
         L.fo_raster_free.restype = None
         L.fo_intersect.argtypes = [C.POINTER(FoRaster), fp, C.POINTER(FoRaster), fp, C.POINTER(FoCounters)]
+        L.fo_intersect_heuristic.argtypes = [C.POINTER(FoRaster), C.POINTER(FoRaster)]
         L.fo_within.argtypes = [C.POINTER(FoRaster), fp, C.POINTER(FoRaster), fp, C.c_double, C.c_int,
                                 C.POINTER(FoCounters)]
         L.fo_segment_intersect.argtypes = [fp, fp, fp, fp]
@@ -133,6 +134,11 @@ def intersect(rs: Raster, rt: Raster, counters: bool = False):
     if v < 0:
         raise RuntimeError(f"oracle intersect failed: {v}")
     return (bool(v), c) if counters else bool(v)
+
+
+def intersect_heuristic(rs: Raster, rt: Raster) -> bool:
+    """The reference's -a approximate intersect (fill-probability heuristic)."""
+    return bool(lib().fo_intersect_heuristic(C.byref(rs.r), C.byref(rt.r)))
 
 
 def within(rs: Raster, rt: Raster, distance: float = 10.0, geography: bool = True, counters: bool = False):
