@@ -57,6 +57,9 @@ enum Scratch {
     S_TMP_B,
     S_CPOLY,  // column polygons of the fill sweep
     S_SMALL,  // small-point flags / scan / index
+    S_SMALL_K,  // small-point sort keys and dependency lists
+    S_SMALL_V,
+    S_SMALL_D,
 };
 
 // ------------------------------------------------------------ headers ----
@@ -909,73 +912,149 @@ __global__ void k_ptbits(const float2 *__restrict__ pt, uint64_t n, uint64_t *__
 }
 
 // After sorting by (column, bits, position): a non-first element of a run of
-// identical large points is a later duplicate (MyPolygon.h:49-58 drops it).
+// bit-identical points is dropped (MyPolygon.h:49-58 keeps a point only if no
+// earlier kept point equals it). This holds for small points too: a later
+// bitwise copy equals the earlier copy, and if that copy was itself dropped,
+// the kept point that equalled it equals the later copy as well.
 __global__ void k_dup_large(const uint64_t *__restrict__ col, const uint32_t *__restrict__ pos,
                             const float2 *__restrict__ pt, uint64_t n, uint8_t *__restrict__ drop) {
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t me = pos[k];
-        float2 q = pt[me];
-        if (small_pt(q)) continue;
         if (k > 0 && col[k - 1] == col[k]) {
-            float2 o = pt[pos[k - 1]];
-            if (pt_bits(o) == pt_bits(q)) drop[me] = 1;
+            uint32_t me = pos[k];
+            if (pt_bits(pt[pos[k - 1]]) == pt_bits(pt[me])) drop[me] = 1;
         }
     }
 }
 
-__global__ void k_col_count(const uint64_t *__restrict__ colkey, const float2 *__restrict__ pt, uint64_t n,
-                            uint32_t *__restrict__ colcnt, uint8_t *__restrict__ colsmall) {
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
-        atomicAdd(&colcnt[colkey[k]], 1u);
-        if (small_pt(pt[k])) colsmall[colkey[k]] = 1;
-    }
-}
-
-// Columns holding small points: the reference's sequential rule, restricted to
-// the small points (a small point never equals a large one). One warp per
-// column walks the column's small points (compacted, in order) in chunks of
-// 32: each lane first compares its point with every kept point of earlier
-// chunks, then the chunk resolves its own order with one ballot per lane.
-__global__ void k_small_flags(const float2 *__restrict__ pt, uint64_t n, uint64_t *__restrict__ flag) {
+__global__ void k_col_count(const uint64_t *__restrict__ colkey, uint64_t n, uint32_t *__restrict__ colcnt) {
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
-        flag[k] = small_pt(pt[k]) ? 1 : 0;
+        atomicAdd(&colcnt[colkey[k]], 1u);
 }
 
-__global__ void k_small_compact(const float2 *__restrict__ pt, uint64_t n, const uint64_t *__restrict__ sscan,
-                                uint32_t *__restrict__ sidx) {
+// Small points that are the first copy of their bit pattern in their column
+// are the only ones whose fate depends on the 1e-9 tolerance of
+// Point::operator== (Point.h:32). They are sorted by (column, x, y) and each
+// finds the earlier (in clip order) points it equals inside its tolerance
+// window; the reference's sequential rule is then resolved on that small
+// dependency graph: a point is kept iff none of its earlier equal points is.
+__global__ void k_small_flags(const float2 *__restrict__ pt, const uint8_t *__restrict__ drop, uint64_t n,
+                              uint64_t *__restrict__ flag) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
+        flag[k] = (small_pt(pt[k]) && !drop[k]) ? 1 : 0;
+}
+
+__global__ void k_small_compact(const uint64_t *__restrict__ sscan, uint64_t n, uint32_t *__restrict__ sidx) {
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
         if (sscan[k + 1] != sscan[k]) sidx[sscan[k]] = (uint32_t)k;
 }
 
-__global__ void k_dup_small(const uint64_t *__restrict__ colstart, uint64_t ncol, const uint8_t *__restrict__ colsmall,
-                            const uint64_t *__restrict__ sscan, const uint32_t *__restrict__ sidx,
-                            const float2 *__restrict__ pt, uint8_t *__restrict__ drop) {
-    const int lane = threadIdx.x & 31;
-    uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    for (uint64_t c = w; c < ncol; c += nw) {
-        if (!colsmall[c]) continue;
-        uint64_t b = sscan[colstart[c]], e = sscan[colstart[c + 1]];  // this column's small points
-        for (uint64_t base = b; base < e; base += 32) {
-            uint64_t k = base + lane;
-            bool have = k < e;
-            float2 q = have ? pt[sidx[k]] : make_float2(0.f, 0.f);
-            bool dup = false;
-            // against kept points of earlier chunks (already resolved)
-            for (uint64_t j = b; have && j < base && !dup; j++) {
-                uint32_t pj = sidx[j];
-                if (!drop[pj] && pt_eq(pt[pj], q)) dup = true;
+// float bits mapped so that unsigned order is numeric order (-0 just before +0)
+__device__ inline uint32_t ord_f(float v) {
+    uint32_t u = __float_as_uint(v);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__global__ void k_small_ykey(const float2 *__restrict__ pt, const uint32_t *__restrict__ sidx, uint64_t ns,
+                             uint32_t *__restrict__ ky) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += (uint64_t)gridDim.x * blockDim.x)
+        ky[i] = ord_f(pt[sidx[i]].y);
+}
+
+__global__ void k_small_xkey(const float2 *__restrict__ pt, const uint64_t *__restrict__ colkey,
+                             const uint32_t *__restrict__ sidx, uint64_t ns, uint64_t *__restrict__ kx) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t k = sidx[i];
+        kx[i] = (colkey[k] << 32) | ord_f(pt[k].x);
+    }
+}
+
+__device__ inline uint64_t lower_key(const uint64_t *kx, uint64_t lo, uint64_t hi, uint64_t key) {
+    while (lo < hi) {
+        uint64_t mid = (lo + hi) >> 1;
+        if (kx[mid] < key)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+__device__ inline uint64_t upper_key(const uint64_t *kx, uint64_t lo, uint64_t hi, uint64_t key) {
+    while (lo < hi) {
+        uint64_t mid = (lo + hi) >> 1;
+        if (kx[mid] <= key)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// For sorted small point i: the earlier points (clip order) it equals. Runs
+// of one x value are sorted by y; the x values within 1e-9 form a contiguous
+// band of runs, and inside each run the y values within 1e-9 form a
+// contiguous range (float subtraction is monotone), found by binary search.
+template <bool kFill>
+__global__ void k_small_deps(const uint64_t *__restrict__ kx, const uint32_t *__restrict__ ps, uint64_t ns,
+                             const float2 *__restrict__ pt, uint32_t *__restrict__ cnt,
+                             const uint64_t *__restrict__ dscan, uint32_t *__restrict__ deps) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t k = ps[i];
+        const float2 q = pt[k];
+        const uint64_t key = kx[i], col = key >> 32;
+        uint32_t c = 0;
+        uint64_t at = kFill ? dscan[i] : 0;
+        auto visit = [&](uint64_t j) {
+            uint32_t kj = ps[j];
+            if (kj < k && pt_eq(pt[kj], q)) {
+                if (kFill) deps[at++] = kj;
+                c++;
             }
-            // within the chunk, in order
-            for (int i = 0; i < 32; i++) {
-                bool di = __shfl_sync(0xffffffffu, dup, i);
-                float2 qi = make_float2(__shfl_sync(0xffffffffu, q.x, i), __shfl_sync(0xffffffffu, q.y, i));
-                bool hi = __shfl_sync(0xffffffffu, have, i);
-                // a kept point i knocks out later equal points of the chunk
-                if (hi && !di && lane > i && have && !dup && pt_eq(qi, q)) dup = true;
+        };
+        // y range [first j with y_j - q.y > -1e-9, first with >= 1e-9) of run [b, e)
+        auto run = [&](uint64_t b, uint64_t e) {
+            uint64_t lo = b, hi = e;
+            while (lo < hi) {
+                uint64_t mid = (lo + hi) >> 1;
+                if (pt[ps[mid]].y - q.y > -1e-9)
+                    hi = mid;
+                else
+                    lo = mid + 1;
             }
-            if (have && dup) drop[sidx[k]] = 1;
-            __syncwarp();
+            for (uint64_t j = lo; j < e && pt[ps[j]].y - q.y < 1e-9; j++)
+                if (j != i) visit(j);
+        };
+        const uint64_t rb = lower_key(kx, 0, i, key), re = upper_key(kx, i + 1, ns, key);
+        run(rb, re);
+        for (uint64_t r = re; r < ns && (kx[r] >> 32) == col && pt[ps[r]].x - q.x < 1e-9;) {
+            uint64_t e = upper_key(kx, r + 1, ns, kx[r]);
+            run(r, e);
+            r = e;
+        }
+        for (uint64_t r1 = rb; r1 > 0 && (kx[r1 - 1] >> 32) == col && q.x - pt[ps[r1 - 1]].x < 1e-9;) {
+            uint64_t b = lower_key(kx, 0, r1 - 1, kx[r1 - 1]);
+            run(b, r1);
+            r1 = b;
+        }
+        if (!kFill) cnt[i] = c;
+    }
+}
+
+// One round of the sequential rule on the dependency graph (a DAG: every
+// edge points to an earlier point). Rounds repeat until nothing changes; the
+// graph's unique fixed point is the reference's result.
+__global__ void k_small_resolve(const uint32_t *__restrict__ ps, uint64_t ns, const uint64_t *__restrict__ dscan,
+                                const uint32_t *__restrict__ deps, uint8_t *__restrict__ drop,
+                                int *__restrict__ changed) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t b = dscan[i], e = dscan[i + 1];
+        if (b == e) continue;
+        bool d = false;
+        for (uint64_t j = b; j < e && !d; j++) d = !((volatile uint8_t *)drop)[deps[j]];
+        uint32_t k = ps[i];
+        if ((uint8_t)d != ((volatile uint8_t *)drop)[k]) {
+            ((volatile uint8_t *)drop)[k] = (uint8_t)d;
+            *changed = 1;
         }
     }
 }
@@ -1407,33 +1486,76 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
         k_dup_large<<<gb(nX), 256, 0, st>>>(ck_s, pos2, xpt_s, nX, drop);
         L++;
     }
-    // column starts and small-point columns
+    // column starts
     const uint64_t ncol = ch.ncol;
-    FARM_TRY(s->s[S_LINECNT].ensure(4 * (ncol + 1) + (ncol + 1) + 16));
+    FARM_TRY(s->s[S_LINECNT].ensure(4 * (ncol + 1) + 16));
     FARM_TRY(s->s[S_LINESCAN].ensure(8 * (ncol + 1) * 2 + 16));
     uint32_t *colcnt = s->s[S_LINECNT].as<uint32_t>();
-    uint8_t *colsmall = reinterpret_cast<uint8_t *>(colcnt + (ncol + 1));
     uint64_t *cc64 = s->s[S_LINESCAN].as<uint64_t>(), *colstart = cc64 + (ncol + 1);
-    FARM_CUDA(cudaMemsetAsync(colcnt, 0, 4 * (ncol + 1) + (ncol + 1), st));
+    FARM_CUDA(cudaMemsetAsync(colcnt, 0, 4 * (ncol + 1), st));
     if (nX) {
-        k_col_count<<<gb(nX), 256, 0, st>>>(xkey_s, xpt_s, nX, colcnt, colsmall);
+        k_col_count<<<gb(nX), 256, 0, st>>>(xkey_s, nX, colcnt);
         L++;
     }
     k_u32_to_u64<<<gb(ncol + 1), 256, 0, st>>>(colcnt, ncol + 1, cc64);
     L++;
     FARM_TRY(excl_scan(s, cc64, colstart, ncol + 1));
-    {
-        // small points: flag, compact (column order), then one warp per column
+    if (nX) {
+        // small first copies: tolerance-equality dependencies, then the
+        // sequential rule on them
         FARM_TRY(s->s[S_SMALL].ensure(8 * (nX + 1) * 2 + 4 * nX + 32));
         uint64_t *sflag = s->s[S_SMALL].as<uint64_t>(), *sscan = sflag + (nX + 1);
         uint32_t *sidx = reinterpret_cast<uint32_t *>(sscan + (nX + 1));
         FARM_CUDA(cudaMemsetAsync(sflag + nX, 0, 8, st));
-        k_small_flags<<<gb(nX), 256, 0, st>>>(xpt_s, nX, sflag);
+        k_small_flags<<<gb(nX), 256, 0, st>>>(xpt_s, drop, nX, sflag);
         L++;
         FARM_TRY(excl_scan(s, sflag, sscan, nX + 1));
-        k_small_compact<<<gb(nX), 256, 0, st>>>(xpt_s, nX, sscan, sidx);
-        k_dup_small<<<gb(32ull * ncol), 256, 0, st>>>(colstart, ncol, colsmall, sscan, sidx, xpt_s, drop);
-        L += 2;
+        uint64_t ns = 0;
+        FARM_TRY(d2h(s, &ns, sscan + nX, 8));
+        if (ns > 1) {
+            k_small_compact<<<gb(nX), 256, 0, st>>>(sscan, nX, sidx);
+            L++;
+            // 4 B y keys, y-sorted keys, y-sorted indices, final indices; 8 B x keys, sorted x keys
+            const uint64_t ns2 = (ns + 1) & ~1ull;
+            FARM_TRY(s->s[S_SMALL_K].ensure(16 * ns2 + 16 * ns + 64));
+            unsigned char *kb = s->s[S_SMALL_K].as<unsigned char>();
+            uint32_t *ky = reinterpret_cast<uint32_t *>(kb), *ky_s = ky + ns;
+            uint32_t *sidx_y = ky_s + ns, *ps = sidx_y + ns;
+            uint64_t *kx = reinterpret_cast<uint64_t *>(kb + 16 * ns2), *kx_s = kx + ns;
+            k_small_ykey<<<gb(ns), 256, 0, st>>>(xpt_s, sidx, ns, ky);
+            L++;
+            FARM_TRY(sort_pairs(s, ky, ky_s, sidx, sidx_y, ns, 32));
+            k_small_xkey<<<gb(ns), 256, 0, st>>>(xpt_s, xkey_s, sidx_y, ns, kx);
+            L++;
+            FARM_TRY(sort_pairs(s, kx, kx_s, sidx_y, ps, ns, 32 + key_bits(ncol)));
+            // dependency counts -> scan -> lists (counts reuse the flag buffer)
+            uint32_t *dcnt = reinterpret_cast<uint32_t *>(sflag);
+            k_small_deps<false><<<gb(ns), 256, 0, st>>>(kx_s, ps, ns, xpt_s, dcnt, nullptr, nullptr);
+            L++;
+            FARM_TRY(s->s[S_SMALL_V].ensure(8 * (ns + 1) * 2 + 16));
+            uint64_t *d64 = s->s[S_SMALL_V].as<uint64_t>(), *dscan = d64 + (ns + 1);
+            FARM_CUDA(cudaMemsetAsync(dcnt + ns, 0, 4, st));
+            k_u32_to_u64<<<gb(ns + 1), 256, 0, st>>>(dcnt, ns + 1, d64);
+            L++;
+            FARM_TRY(excl_scan(s, d64, dscan, ns + 1));
+            uint64_t nd = 0;
+            FARM_TRY(d2h(s, &nd, dscan + ns, 8));
+            if (nd) {
+                FARM_TRY(s->s[S_SMALL_D].ensure(4 * nd + 64));
+                uint32_t *deps = s->s[S_SMALL_D].as<uint32_t>();
+                int *changed = reinterpret_cast<int *>(deps + ((nd + 3) & ~3ull));
+                k_small_deps<true><<<gb(ns), 256, 0, st>>>(kx_s, ps, ns, xpt_s, nullptr, dscan, deps);
+                L++;
+                for (uint64_t round = 0; round <= ns; round++) {
+                    FARM_CUDA(cudaMemsetAsync(changed, 0, 4, st));
+                    k_small_resolve<<<gb(ns), 256, 0, st>>>(ps, ns, dscan, deps, drop, changed);
+                    L++;
+                    int h = 0;
+                    FARM_TRY(d2h(s, &h, changed, 4));
+                    if (!h) break;
+                }
+            }
+        }
     }
     k_not_u8<<<gb(nX + 1), 256, 0, st>>>(drop, nX + 1, kept64);
     L++;

@@ -81,3 +81,47 @@ def test_gpu_intersect_marks_pairs_of_unrasterizable_polygons(gpu_lib):
     assert out.tolist() == [2, int(O.intersect(RS, RT)), 2, 2]
     assert found == int(out[1] == 1)
     st.close()
+
+
+def test_gpu_intersect_lattice_collinear(gpu_lib):
+    # axis-aligned rectangles and right triangles on an integer lattice: edges
+    # that overlap collinearly, touch end to end or meet at corners, which the
+    # refinement settles with the collinear interval rule
+    rng = np.random.default_rng(5)
+
+    def shapes(n):
+        rings = []
+        for _ in range(n):
+            x0, y0 = rng.integers(0, 12, 2)
+            w, h = rng.integers(1, 5, 2)
+            if rng.random() < 0.5:
+                r = [[x0, y0], [x0 + w, y0], [x0 + w, y0 + h], [x0, y0 + h], [x0, y0]]
+            else:
+                r = [[x0, y0], [x0 + w, y0], [x0, y0 + h], [x0, y0]]
+            rings.append(np.array(r, np.float32))
+        off = np.zeros(n + 1, np.uint64)
+        off[1:] = np.cumsum([len(r) for r in rings])
+        return P.PolygonSet(off, np.ascontiguousarray(np.concatenate(rings)))
+
+    def ras(ps, vpr):
+        out = []
+        for k in range(ps.n):
+            try:
+                out.append(O.Raster(ps.ring(k), vpr))
+            except RuntimeError:  # the reference aborts on this polygon
+                out.append(None)
+        return out
+
+    S, T = shapes(60), shapes(80)
+    pairs = P.mbr_join(S.mbrs(), T.mbrs())
+    for vpr in (1, 2, 3):
+        RS, RT = ras(S, vpr), ras(T, vpr)
+        ok = [i for i, (s, t) in enumerate(pairs) if RS[s] is not None and RT[t] is not None]
+        st = Store()
+        st.load_sets(S, T)
+        st.rasterize(vpr=vpr, strict=False)
+        out, _ = st.intersect(np.ascontiguousarray(pairs, dtype=np.uint32))
+        st.close()
+        exp = np.array([O.intersect(RS[pairs[i][0]], RT[pairs[i][1]]) for i in ok], np.uint8)
+        assert np.array_equal(out[ok], exp), (vpr, int((out[ok] != exp).sum()))
+        assert len(ok) > len(pairs) // 2

@@ -104,3 +104,49 @@ def test_gpu_raster_many_chunks(gpu_lib, monkeypatch):
             r = O.Raster(ps.ring(k), 4, hier).arrays()
             assert not raster_mismatches(got[k], r), (hier, k)
         st.close()
+
+
+def _ulp_chains(ps, steps=(1, 2, 3)):
+    """Each vertex followed by copies nudged by 1..3 float ulps: distinct points
+    within 1e-9 of each other (near the origin), including non-transitive
+    chains (v ~ v+1ulp ~ v+2ulp, but v !~ v+3ulp)."""
+    rings = []
+    for k in range(ps.n):
+        r = ps.ring(k)[:-1]
+        out = []
+        for i, v in enumerate(r):
+            out.append(v)
+            if i % 3 == 0:
+                for s in steps:
+                    w = v.copy()
+                    for _ in range(s):
+                        w = np.nextafter(w, np.float32(np.inf)).astype(np.float32)
+                    out.append(w)
+        out.append(r[0])
+        rings.append(np.array(out, np.float32))
+    off = np.zeros(len(rings) + 1, np.uint64)
+    off[1:] = np.cumsum([len(r) for r in rings])
+    return P.PolygonSet(off, np.ascontiguousarray(np.concatenate(rings)))
+
+
+@pytest.mark.parametrize("vpr,seed", [(1, 31), (4, 32), (16, 33)])
+def test_gpu_raster_small_point_tolerance(gpu_lib, vpr, seed):
+    # every coordinate below 2^-5: the fill clip's point dedup runs on the
+    # 1e-9 tolerance rule, not on bit equality
+    prm = P.StarParams(dom_lo=-0.02, dom_hi=0.02, r_lo=0.001, r_hi=0.01, n_lo=8, n_hi=120)
+    ps = _ulp_chains(P.generate(prm, seed, 60))
+    st = Store()
+    st.load(0, ps.off, ps.xy)
+    st.rasterize(vpr=vpr, strict=False)
+    checked = 0
+    for k in range(ps.n):
+        g = st.fetch_raster(0, k)
+        try:
+            r = O.Raster(ps.ring(k), vpr, False).arrays()
+        except RuntimeError:
+            assert g["err"] == -10, k
+            continue
+        assert g["err"] == 0 and not raster_mismatches(g, r), k
+        checked += 1
+    st.close()
+    assert checked >= ps.n // 2
