@@ -1,19 +1,21 @@
 """Benchmark of the polygon-join hot path: exact intersect pairs/sec on one GB300.
 
-Workload (BASELINE configuration 2): seeded star polygons, 100,000 sources x
+Workload (configuration 2): seeded star polygons, 100,000 sources x
 1,000,000 targets, vertex count log-uniform 16..100,000, mean radius
 log-uniform 0.05..2.0, per-vertex radius x lognormal(0, 0.3); the domain side
-is calibrated so the MBR join yields ~20M candidate pairs. The job runs in
-target batches (all sources + 1/B of the targets, ~20M/B candidates each): one
-"step" is one batch through the whole hot path — ring upload into the store's
-layout, rasterization of every polygon of the batch (stage a), pixel-pair
-filter + border refinement of every candidate (stages b, c), result bytes.
-Inputs are GBs (far larger than the 129 MB L2), so no L2 flush is needed.
+is calibrated so the MBR join yields ~20M candidate pairs. The job is cut into
+spatial strips by source centre: strip b holds the sources centred in it and
+the targets that reach them, and all of its candidate pairs. One "step" is
+one strip through the whole hot path — ring upload into the store's layout,
+rasterization of every polygon of the strip (stage a), pixel-pair filter +
+border refinement of every candidate (stages b, c), result bytes. Steps repeat
+the strip of this rank (the inputs are GBs, far larger than the 129 MB L2, so
+no L2 flush is needed).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Under torchrun each rank takes its own target batches (weak scaling, no
-collective on the data path); value = all ranks' pairs / max rank time.
+Under torchrun each rank takes its own strip (weak scaling, no collective on
+the data path); value = all ranks' pairs / max rank time.
 --impl reference times the reference's CPU algorithm (the oracle port under
 oracle/, all host cores) on a bounded sample of the same workload.
 """
@@ -122,39 +124,51 @@ def log(msg: str) -> None:
     print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
 
 
-def build_workload(seed: int, batch: int, n_batches: int, vpr: int):
-    """Host (pinned) rings of all sources and of target batch `batch`, and its candidates."""
+# every vertex of a generated polygon lies within this many mean radii of its
+# centre unless its lognormal factor exceeds exp(0.3 * 6.5) (probability ~4e-11)
+EXTENT_RADII = math.exp(0.3 * 6.5)
+
+
+def build_workload(seed: int, strip: int, n_strips: int, vpr: int):
+    """Host (pinned) rings and candidate pairs of one strip of the job.
+
+    The domain is cut into n_strips vertical strips by source centre. Strip b
+    holds the sources centred in it and every target whose extent (centre +-
+    EXTENT_RADII x mean radius) reaches the x-range of the strip's source MBRs;
+    its pairs are the MBR-overlapping (source, target) pairs of those sets, so
+    every candidate pair of the job belongs to exactly one strip, and only
+    targets straddling a strip boundary are rasterized in two steps."""
     import torch
     from farm_gb300 import polygons as P
 
     L = calibrate_domain(seed)
     prm = star_params(L)
-    tb = N_TGT // n_batches
-    t_first = batch * tb
-
-    def gen_pinned(seed_, count, first):
-        from farm_gb300._native import check_host, host, ptr, u32p, u64p, f32p
-        import ctypes as C
-        gp = prm.c()
-        counts = np.zeros(count, np.uint32)
-        check_host(host().farm_gen_counts(C.byref(gp), seed_, first, count, ptr(counts, u32p)))
-        off = torch.zeros(count + 1, dtype=torch.int64).pin_memory()
-        offn = off.numpy().view(np.uint64)
-        np.cumsum(counts, dtype=np.uint64, out=offn[1:])
-        xy = torch.empty((int(offn[-1]), 2), dtype=torch.float32).pin_memory()
-        xyn = xy.numpy()
-        check_host(host().farm_gen_fill(C.byref(gp), seed_, first, count, ptr(offn, u64p), ptr(xyn, f32p), 0))
-        return P.PolygonSet(offn, xyn), off, xy
-
     log(f"domain side {L:.2f}")
-    S, S_off_t, S_xy_t = gen_pinned(seed, N_SRC, 0)
-    log(f"sources generated: {S.total} vertices")
-    T, T_off_t, T_xy_t = gen_pinned(seed + 1, tb, t_first)
-    log(f"targets generated: {T.total} vertices")
-    ms, mt = S.mbrs(), T.mbrs()
-    pairs = P.mbr_join(ms, mt)
-    log(f"candidates: {len(pairs)}")
-    return {"L": L, "S": S, "T": T, "pairs": pairs, "tb": tb, "t_first": t_first,
+    w = L / n_strips
+    cs = P.centres(prm, seed, N_SRC)
+    s_idx = np.nonzero((cs[:, 0] >= strip * w) & (cs[:, 0] < (strip + 1) * w))[0].astype(np.uint64)
+
+    def gen_pinned(seed_, idx):
+        counts = P.vertex_counts(prm, seed_, idx)
+        off = torch.zeros(len(idx) + 1, dtype=torch.int64).pin_memory()
+        offn = off.numpy().view(np.uint64)
+        total = int(counts.sum(dtype=np.uint64))
+        xy = torch.empty((total, 2), dtype=torch.float32).pin_memory()
+        ps = P.generate_indices(prm, seed_, idx, out_off=offn, out_xy=xy.numpy())
+        return ps, off, xy
+
+    S, S_off_t, S_xy_t = gen_pinned(seed, s_idx)
+    ms = S.mbrs()
+    log(f"strip {strip}/{n_strips}: {S.n} sources, {S.total} vertices")
+    ct = P.centres(prm, seed + 1, N_TGT)
+    ext = EXTENT_RADII * ct[:, 2]
+    xlo, xhi = ms[:, 0].min(), ms[:, 2].max()
+    t_idx = np.nonzero((ct[:, 0] + ext >= xlo) & (ct[:, 0] - ext <= xhi))[0].astype(np.uint64)
+    T, T_off_t, T_xy_t = gen_pinned(seed + 1, t_idx)
+    pairs = P.mbr_join(ms, T.mbrs())
+    log(f"targets: {T.n} ({T.total} vertices, {len(np.unique(pairs[:, 1]))} with candidates); "
+        f"candidates: {len(pairs)}")
+    return {"L": L, "S": S, "T": T, "pairs": pairs, "strip": strip, "n_strips": n_strips,
             "pinned": (S_off_t, S_xy_t, T_off_t, T_xy_t)}
 
 
@@ -163,6 +177,77 @@ def filter_bytes(stats: dict, n_pairs: int, bits: int) -> float:
     (pair ids) + 2 x 64 (raster headers) + w/8 per source window pixel and per
     target pixel visited + 1/8 (result bit)."""
     return n_pairs * (8 + 128 + 0.125) + bits / 8.0 * (stats["src_window_pixels"] + stats["tgt_window_pixels"])
+
+
+# Peaks. HBM: MEASURED_PEAKS.json (a STREAM-style copy on this GPU model).
+# FP64 / FP32: nominal issue rates, as no measured figure exists for them —
+# GB300 issues FP64 at 2 lanes/clock/SM (1.25 TFLOP/s counts an FMA as two
+# flops; these kernels cannot fuse, so every flop is one instruction) and FP32
+# at 128 lanes/clock/SM; 152 SMs at 2.07 GHz.
+FP64_PEAK = 2 * 152 * 2.07e9
+FP32_PEAK = 128 * 152 * 2.07e9
+
+
+def rooflines(rt: dict, qs: dict, n_pairs: int, stage: dict, steps: int) -> dict:
+    """Roofline of each measured stage from its algorithmic work per unit
+    (counts of the last step; times are the per-step means of the timed steps).
+
+    edge walk (3 launches: totals, count, fill): FP64, 16 flops per edge
+      (endpoint cells, slope and intercept) + 16 per pixel-boundary crossing
+      (both branches of one walk step), the reference's arithmetic for ONE walk;
+    cell clip (count + emit): FP64, 4 flops per emitted clip point (slope and
+      the two line abscissae, shared by ~2 points per edge-row);
+    column clip: FP64, 2 flops per emitted point;
+    cell areas: FP64, 4 flops per clip point (shoelace term + accumulation);
+    filter + refine (k_intersect): FP32, 28 flops per segment-pair test
+      (4 cross products x 7); its HBM bytes per filter_bytes();
+    whole raster stage, HBM view: 8 B per vertex read + the raster written
+      (w P / 8 + 4 (P + n) + 8 sequences + 8 nodes).
+    """
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0)) * 1e9
+    per = lambda k: stage[k] / steps
+    walk_ms = rt["ms_walk"]
+    st = {}
+
+    def fp(name, flops, ms, peak, kind, peak_src):
+        ach = flops / (ms * 1e-3) if ms > 0 else None
+        st[name] = {"bound": kind, "algorithmic_flops": flops, "kernel_ms": ms,
+                    "achieved": ach / 1e12 if ach else None, "peak": peak / 1e12, "unit": "TFLOP/s",
+                    "frac": ach / peak if ach else None, "peak_source": peak_src}
+
+    src64 = "nominal FP64 issue rate (no measured FP64 figure in MEASURED_PEAKS.json)"
+    fp("edge_walk", 16.0 * rt["vertices"] + 16.0 * rt["crossings"], walk_ms, FP64_PEAK, "fp64", src64)
+    fp("cell_clip", 4.0 * rt["clip_y_points"], rt["ms_clip_y"], FP64_PEAK, "fp64", src64)
+    fp("column_clip", 2.0 * rt["clip_x_points"], rt["ms_clip_x"], FP64_PEAK, "fp64", src64)
+    fp("cell_area", 4.0 * rt["clip_y_points"], rt["ms_cells"], FP64_PEAK, "fp64", src64)
+    fp("refine", 28.0 * qs["segment_tests"], per("query_ms"), FP32_PEAK, "fp32",
+       "nominal FP32 issue rate (no measured FP32 figure in MEASURED_PEAKS.json)")
+    fb = filter_bytes(qs, n_pairs, 4)
+    rb = 8.0 * rt["vertices"] + 0.5 * rt["pixels"] + 4.0 * (rt["pixels"] + rt["polygons"]) + \
+        8.0 * rt["sequences"] + 8.0 * (rt["hnodes"] + rt["vnodes"])
+    rms = per("raster_ms")
+    st["raster_hbm_view"] = {"bound": "hbm", "algorithmic_bytes": rb, "kernel_ms": rms,
+                             "achieved": rb / (rms * 1e-3) / 1e9 if rms > 0 else None, "peak": hbm / 1e9,
+                             "unit": "GB/s", "frac": rb / (rms * 1e-3) / hbm if rms > 0 else None,
+                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+    st["filter_hbm_view"] = {"bound": "hbm", "algorithmic_bytes": fb, "kernel_ms": per("query_ms"),
+                             "achieved": fb / (per("query_ms") * 1e-3) / 1e9 if per("query_ms") > 0 else None,
+                             "peak": hbm / 1e9, "unit": "GB/s", "peak_source": "MEASURED_PEAKS.json hbm_gbs"}
+    # the dominant kernel: the stage with the most device time
+    cand = {k: v for k, v in st.items() if k in ("edge_walk", "cell_clip", "column_clip", "cell_area", "refine")}
+    name = max(cand, key=lambda k: cand[k]["kernel_ms"] or 0.0)
+    dom = dict(cand[name])
+    dom["kernel"] = {"edge_walk": "k_walk_tot + k_walk_count + k_walk_fill", "cell_clip": "k_clipy (count + emit)",
+                     "column_clip": "k_clipx (count + emit)", "cell_area": "k_cells",
+                     "refine": "k_intersect (filter + refine)"}[name]
+    dom["traffic"] = None
+    dom["peak"] = dom["peak"]
+    return {"dominant": dom, "stages": st}
 
 
 def run_ours(args) -> dict:
@@ -177,8 +262,7 @@ def run_ours(args) -> dict:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from farm_gb300.engine import Store
 
-    n_batches = args.batches
-    W = build_workload(args.seed, rank % n_batches, n_batches, args.vpr)
+    W = build_workload(args.seed, rank % args.strips, args.strips, args.vpr)
     S, T, pairs = W["S"], W["T"], W["pairs"]
     S_off_t, S_xy_t, T_off_t, T_xy_t = W["pinned"]
     dev = torch.device("cuda", local)
@@ -189,11 +273,21 @@ def run_ours(args) -> dict:
     h_pairs = torch.from_numpy(pairs.view(np.int32)).pin_memory()
     store = Store()
 
-    def step_device():
+    stage = {"load_ms": 0.0, "raster_ms": 0.0, "query_ms": 0.0}
+
+    def step_device(timed=False):
+        store.event_record(4)
         store.load(0, d["so"], d["sx"])
         store.load(1, d["to"], d["tx"])
+        store.event_record(5)
         store.rasterize(vpr=args.vpr, category_count=16, strict=False)
+        if timed:
+            stage["load_ms"] += store.event_elapsed(4, 5)
+        store.event_record(4)
         _, found = store.intersect(d_pairs.view(len(pairs), 2), out=d_out)
+        if timed:
+            stage["raster_ms"] += store.event_elapsed(5, 4)
+            stage["query_ms"] += store.last_stats["ms_total"]
         return found
 
     def step_e2e():
@@ -206,7 +300,9 @@ def run_ours(args) -> dict:
     for i in range(args.warmup):
         t = time.time()
         step_device()
-        log(f"warmup step {i}: {time.time() - t:.2f}s, stats {store.last_stats}")
+        free, total = torch.cuda.mem_get_info(dev)
+        log(f"warmup step {i}: {time.time() - t:.2f}s, device memory in use {(total - free) / 2**30:.1f} GiB, "
+            f"raster {store.raster_totals()}, stats {store.last_stats}")
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
@@ -215,10 +311,8 @@ def run_ours(args) -> dict:
     launches0 = store.launches
     store.event_record(0)
     founds = []
-    stage = {"filter_ms": 0.0}
     for _ in range(args.steps):
-        founds.append(step_device())
-        stage["filter_ms"] += store.last_stats["ms_stage"][1]
+        founds.append(step_device(timed=True))
     store.event_record(1)
     ms = store.event_elapsed(0, 1)
     torch.cuda.synchronize()
@@ -248,36 +342,27 @@ def run_ours(args) -> dict:
         total_pairs = float(len(pairs))
     value = total_pairs * args.steps / t_dev
     e2e_value = total_pairs * args.steps / t_e2e
-    bits = 4
-    fb = filter_bytes(last, len(pairs), bits)
-    kernel_ms = stage["filter_ms"] / args.steps
-    peaks = {}
-    try:
-        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
-    except Exception:
-        pass
-    peak = float(peaks.get("hbm_gbs", 6800.0))
-    achieved = fb / (kernel_ms / 1000.0) / 1e9 if kernel_ms > 0 else None
+    rl = rooflines(store.raster_totals(), last, len(pairs), stage, args.steps)
     h2d = int(S_xy_t.numel() * 4 + T_xy_t.numel() * 4 + S_off_t.numel() * 8 + T_off_t.numel() * 8 + pairs.nbytes)
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64", "data": "synthetic (seeded star polygons, configuration 2 generator)",
         "config": {"workload": "intersect, configuration 2: 100k sources x 1M targets, nv log-uniform 16..100000, "
-                               f"~20M MBR candidates, -v {args.vpr}, -w 16, target batch {W['tb']} of "
-                               f"{N_TGT} (batch {rank % n_batches})",
+                               f"~20M MBR candidates, -v {args.vpr}, -w 16; one step = strip {W['strip']} of "
+                               f"{W['n_strips']} (sources centred in it + the targets reaching them)",
                    "domain_side": W["L"], "vpr": args.vpr, "category_count": 16, "n_source": N_SRC,
-                   "n_target_batch": W["tb"], "candidate_pairs_per_step": len(pairs), "found_per_step": founds[-1],
+                   "n_target": N_TGT, "strips": W["n_strips"], "sources_per_step": int(S.n),
+                   "targets_per_step": int(T.n), "candidate_pairs_per_step": len(pairs), "found_per_step": founds[-1],
                    "vertices_per_step": int(S.total + T.total), "l2": "inputs larger than L2 (no flush needed)",
                    "seed": args.seed, "parallelism": f"weak-dp{world}"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": int(len(pairs))},
         "gpu_launches": int(launches),
         "clocks": clk,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": None,
-                     "kernel": "k_intersect (filter + refine)", "kernel_ms": kernel_ms,
-                     "algorithmic_bytes": fb, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
-        "stage_ms": {"filter_refine": kernel_ms, "step": ms / args.steps},
+        "roofline": rl["dominant"],
+        "stages": rl["stages"],
+        "stage_ms": {"load": stage["load_ms"] / args.steps, "raster": stage["raster_ms"] / args.steps,
+                     "filter_refine": stage["query_ms"] / args.steps, "step": ms / args.steps},
     }
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(W, args, budget_s=args.cpu_seconds, threads=1, gpu_out=h_out.numpy())
@@ -367,7 +452,7 @@ def run_reference(args) -> dict:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return None
-    W = build_workload(args.seed, 0, args.batches, args.vpr)
+    W = build_workload(args.seed, 0, args.strips, args.vpr)
     threads = os.cpu_count() or 1
     vals = []
     t0 = time.perf_counter()
@@ -395,7 +480,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--vpr", type=int, default=64)
-    ap.add_argument("--batches", type=int, default=10, help="target batches the 1M targets are split into")
+    ap.add_argument("--strips", type=int, default=10, help="strips the job is cut into (one per step)")
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--ref-step-seconds", type=float, default=20.0)

@@ -14,6 +14,12 @@ class Stats(C.Structure):
                 ("reserved", C.c_int32), ("src_window_pixels", C.c_uint64), ("tgt_window_pixels", C.c_uint64)]
 
 
+class RasterTotals(C.Structure):
+    _fields_ = [(k, C.c_uint64) for k in ("polygons", "vertices", "pixels", "status_bytes", "sequences", "hnodes",
+                                          "vnodes", "crossings", "clip_x_points", "clip_y_points", "chunks")] + \
+               [(k, C.c_double) for k in ("ms_walk", "ms_clip_x", "ms_clip_y", "ms_cells", "ms_total")]
+
+
 class RasterView(C.Structure):
     _fields_ = [("mbr", C.c_double * 4), ("dimx", C.c_int32), ("dimy", C.c_int32), ("step_x", C.c_double),
                 ("step_y", C.c_double), ("nv", C.c_uint32), ("status_size", C.c_uint32), ("n_seq", C.c_uint32),
@@ -49,6 +55,7 @@ def declare(lib):
                                       u32p, f64p, f64p, f64p]
     lib.farm_sync.argtypes = [vp]
     lib.farm_raster_errors.argtypes = [vp, C.c_int, vp, C.c_uint64]
+    lib.farm_raster_get_totals.argtypes = [vp, C.POINTER(RasterTotals)]
     lib.farm_intersect_static.argtypes = [vp, vp, C.c_uint64, vp, u64p]
     lib.farm_tc_gemm_test.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int]
     f32p = C.POINTER(C.c_float)

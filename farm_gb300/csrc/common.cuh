@@ -199,6 +199,7 @@ struct farm_store {
     farm_raster_opts ropts{};
     farm::DevBuf d_hdr, d_status, d_offset, d_seq, d_hoff, d_hnodes, d_voff, d_vnodes, d_areas;
     uint64_t tot_P = 0, tot_status = 0, tot_seq = 0;
+    farm_raster_totals rtot = {};
     // scratch for the rasterizer and the queries
     farm::DevBuf s[32];
     farm::DevBuf cub_tmp;

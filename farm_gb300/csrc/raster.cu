@@ -255,16 +255,38 @@ __global__ void k_bases(PolyHdr *__restrict__ hdr, uint32_t npoly, const uint64_
 // ---------------------------------------------------------- edge walk ----
 // Ideal.cpp:259-521 for one edge. Sink receives: border(x, y), cross(from,
 // to) (a LEAVE/ENTER pair), hnode(line, value), vnode(line, value).
+//
+// FP64 is GB300's scarcest pipe, and the reference's walk divides three times
+// per step. Every one of those quotients only feeds an integer decision —
+// truncation, the 1e-8 snap of double_to_int, or the 1e-9 grid-corner test —
+// except the h-node abscissa, which is emitted. So each quotient t / d is
+// first taken as t * fl(1/d), which differs from the reference's fl(t / d) by
+// at most ~3 units in the last place of |q| <= grid size (a few 1e-16 * dim);
+// the decision is read off that value unless it lies within a 1e-15 * (dim + 4)
+// band of a decision threshold, where the exact quotient is taken instead.
+// Outside the band both values fall on the same side of every threshold, so
+// the decisions are the reference's. Emitted values (v-node ordinates, h-node
+// abscissae) are always the reference's exact expressions.
 template <typename Sink>
 __device__ void walk_edge(const PolyHdr &h, float2 A, float2 B, Sink &s) {
     const double start_x = h.mbr[0], start_y = h.mbr[1];
     const double step_x = h.step_x, step_y = h.step_y;
+    const double isx = __drcp_rn(step_x), isy = __drcp_rn(step_y);
     const int dimx = h.dimx, dimy = h.dimy;
+    const double qlim = (double)(dimx > dimy ? dimx : dimy) + 2.0;
+    const double band = 1e-15 * (qlim + 2.0);
+    // double_to_int(t / d) for t / d >= 0 (a vertex is never left of or
+    // below its MBR): its only thresholds there sit 1e-8 below each integer
+    auto d2i = [&](double t, double d, double inv) -> int {
+        double v = t * inv;
+        if (!(v >= -0.5 && v <= qlim) || fabs(fabs(v - rint(v)) - 1e-8) <= band) v = t / d;
+        return double_to_int(v);
+    };
     double x1 = A.x, y1 = A.y, x2 = B.x, y2 = B.y;
-    int cur_startx = double_to_int((x1 - start_x) / step_x);
-    int cur_endx = double_to_int((x2 - start_x) / step_x);
-    int cur_starty = double_to_int((y1 - start_y) / step_y);
-    int cur_endy = double_to_int((y2 - start_y) / step_y);
+    int cur_startx = d2i(x1 - start_x, step_x, isx);
+    int cur_endx = d2i(x2 - start_x, step_x, isx);
+    int cur_starty = d2i(y1 - start_y, step_y, isy);
+    int cur_endy = d2i(y2 - start_y, step_y, isy);
     if (cur_startx == dimx) cur_startx--;
     if (cur_endx == dimx) cur_endx--;
     if (cur_starty == dimy) cur_starty--;
@@ -304,8 +326,17 @@ __device__ void walk_edge(const PolyHdr &h, float2 A, float2 B, Sink &s) {
         }
         return;
     }
-    double a = (y1 - y2) / (x1 - x2);
-    double b = (x1 * y2 - x2 * y1) / (x1 - x2);
+    const double a = (y1 - y2) / (x1 - x2);
+    const double b = (x1 * y2 - x2 * y1) / (x1 - x2);
+    const double ia = __drcp_rn(a);
+    // band for the y-branch quotient ((yv - b) / a - start_x) / step_x: the
+    // abscissa's ~3 ulp error, carried through the subtraction and the scaling
+    const double mx = fmax(fabs(x1), fabs(x2));
+    const double band2 = 1e-15 * ((2.0 * mx + fabs(start_x)) * isx + qlim + 2.0);
+    const int ymax = cur_endy > cur_starty ? cur_endy : cur_starty;
+    const int ymin = cur_endy < cur_starty ? cur_endy : cur_starty;
+    const int xmax = cur_endx > cur_startx ? cur_endx : cur_startx;
+    const int xmin = cur_endx < cur_startx ? cur_endx : cur_startx;
     int x = cur_startx, y = cur_starty;
     long guard = 4L * (labs((long)cur_endx - cur_startx) + labs((long)cur_endy - cur_starty) + 4);
     while (x != cur_endx || y != cur_endy) {
@@ -314,14 +345,21 @@ __device__ void walk_edge(const PolyHdr &h, float2 A, float2 B, Sink &s) {
             return;
         }
         bool passed = false;
-        double yval = 0, xval = 0;
         if (x != cur_endx) {
+            double xval;
             if (cur_startx < cur_endx)
                 xval = ((double)x + 1) * step_x + start_x;
             else
                 xval = (double)x * step_x + start_x;
-            yval = xval * a + b;
-            if (fabs((yval - start_y) / step_y - round((yval - start_y) / step_y)) < 1e-9) {
+            const double yval = xval * a + b;
+            const double t = yval - start_y;
+            double q = t * isy;
+            double d = fabs(q - rint(q));
+            if (!(fabs(q) <= qlim) || fabs(d - 1e-9) <= band) {
+                q = t / step_y;
+                d = fabs(q - round(q));
+            }
+            if (d < 1e-9) {
                 // Ideal.cpp:396-422: through a grid corner
                 if (cur_startx < cur_endx && cur_starty < cur_endy) {
                     s.vnode(x + 1, yval);
@@ -344,9 +382,7 @@ __device__ void walk_edge(const PolyHdr &h, float2 A, float2 B, Sink &s) {
                 }
                 continue;
             }
-            int cur_y = (int)((yval - start_y) / step_y);
-            int ymax = cur_endy > cur_starty ? cur_endy : cur_starty;
-            int ymin = cur_endy < cur_starty ? cur_endy : cur_starty;
+            int cur_y = (int)q;
             if (cur_y > ymax) cur_y = ymax;
             if (cur_y < ymin) cur_y = ymin;
             if (cur_y == y) {
@@ -363,18 +399,26 @@ __device__ void walk_edge(const PolyHdr &h, float2 A, float2 B, Sink &s) {
             }
         }
         if (y != cur_endy) {
+            double yval;
             if (cur_starty < cur_endy)
                 yval = (double)(y + 1) * step_y + start_y;
             else
                 yval = (double)y * step_y + start_y;
-            xval = (yval - b) / a;
-            int cur_x = (int)((xval - start_x) / step_x);
-            int xmax = cur_endx > cur_startx ? cur_endx : cur_startx;
-            int xmin = cur_endx < cur_startx ? cur_endx : cur_startx;
+            const double t2 = yval - b;
+            double xv = t2 * ia;
+            double q2 = (xv - start_x) * isx;
+            bool exact = false;
+            if (!(fabs(q2) <= qlim) || fabs(q2 - rint(q2)) <= band2) {
+                xv = t2 / a;
+                q2 = (xv - start_x) / step_x;
+                exact = true;
+            }
+            int cur_x = (int)q2;
             if (cur_x > xmax) cur_x = xmax;
             if (cur_x < xmin) cur_x = xmin;
             if (cur_x == x) {
                 passed = true;
+                const double xval = (Sink::kValues && !exact) ? t2 / a : xv;
                 if (cur_starty < cur_endy) {
                     s.hnode(y + 1, xval);
                     s.cross(x, y, x, y + 1);
@@ -394,6 +438,7 @@ __device__ void walk_edge(const PolyHdr &h, float2 A, float2 B, Sink &s) {
 }
 
 struct CountSink {
+    static constexpr bool kValues = false;
     uint8_t *status;
     int dimx, dimy;
     uint32_t nc = 0, nh = 0, nv = 0;
@@ -430,6 +475,7 @@ struct CountSink {
 // Emits exactly what CountSink counted: the walk is deterministic and both
 // sinks drop the same out-of-range items.
 struct FillSink {
+    static constexpr bool kValues = true;
     int dimx, dimy;
     uint32_t edge;
     uint64_t c, hn, vn;           // output cursors
@@ -474,28 +520,25 @@ __device__ inline bool in_rng(double lo, double hi, double v) { return !(v < lo 
 
 __device__ inline float2 mk(double x, double y) { return make_float2((float)x, (float)y); }
 
+// range test on floats: the reference compares these promoted to double, and
+// the promotion is exact, so comparing in float gives the same answer without
+// the FP64 pipe
+__device__ inline bool in_rngf(float lo, float hi, float v) { return !(v < lo || v > hi); }
+
 // Points one edge contributes to column c's clip (Ideal.cpp:575-678), in order.
+// pi, pi1 are the float points (Xi, yi), (Xi1, yi1) on the column lines, yi and
+// yi1 the edge's ordinates there (ClipXEdge).
 // Returns the count; writes up to 4 points when out != nullptr.
-__device__ int clip_x_points(float2 A, float2 B, double Xi, double Xi1, float2 *out) {
+__device__ inline int clip_x_points(float2 A, float2 B, double Xi, double Xi1, float2 pi, float2 pi1, float2 *out) {
     int n = 0;
-    double yi, yi1;
-    if (A.x == B.x) {
-        yi = A.y < B.y ? A.y : B.y;
-        yi1 = yi;
-    } else {
-        double slope = ((double)B.y - A.y) / (double)(B.x - A.x);
-        yi = slope * (Xi - B.x) + B.y;
-        yi1 = slope * (Xi1 - B.x) + B.y;
-    }
-    float2 pi = mk(Xi, yi), pi1 = mk(Xi1, yi1);
-    double mny = A.y < B.y ? A.y : B.y, mxy = A.y < B.y ? B.y : A.y;
-    double mnx = A.x < B.x ? A.x : B.x, mxx = A.x < B.x ? B.x : A.x;
+    const float mny = A.y < B.y ? A.y : B.y, mxy = A.y < B.y ? B.y : A.y;
+    const float mnx = A.x < B.x ? A.x : B.x, mxx = A.x < B.x ? B.x : A.x;
     if (in_rng(Xi, Xi1, A.x)) {
         if (out) out[n] = A;
         n++;
     }
-    bool c0 = in_rng(mny, mxy, pi.y) && in_rng(mnx, mxx, pi.x);
-    bool c1 = in_rng(mny, mxy, pi1.y) && in_rng(mnx, mxx, pi1.x);
+    bool c0 = in_rngf(mny, mxy, pi.y) && in_rngf(mnx, mxx, pi.x);
+    bool c1 = in_rngf(mny, mxy, pi1.y) && in_rngf(mnx, mxx, pi1.x);
     if (A.x < B.x) {
         if (c0) { if (out) out[n] = pi; n++; }
         if (c1) { if (out) out[n] = pi1; n++; }
@@ -510,41 +553,39 @@ __device__ int clip_x_points(float2 A, float2 B, double Xi, double Xi1, float2 *
     return n;
 }
 
-// Points one column-polygon edge contributes to row r's clip (Ideal.cpp:680-818).
-__device__ int clip_y_points(float2 A, float2 B, double Yi, double Yi1, float2 *out) {
-    int n = 0;
-    bool parallels = false;
-    double xi = 0, xi1 = 0;
-    if (A.x == B.x) {
-        xi = A.x;
-        xi1 = A.x;
-    } else {
-        double slope = ((double)B.y - A.y) / (double)(B.x - A.x);
-        if (A.y == B.y) {
-            if (A.y == Yi) {
-                xi = A.x;
-                xi1 = -INFINITY;  // -DBL_MAX, which converts to -inf in float
-            } else if (A.y == Yi1) {
-                xi = -INFINITY;
-                xi1 = A.x;
-            } else {
-                parallels = true;
-            }
-        } else {
-            xi = ((Yi - B.y) / slope) + B.x;
-            xi1 = ((Yi1 - B.y) / slope) + B.x;
-        }
+// The edge's ordinate at column line X (Ideal.cpp:575-600). The reference
+// computes the slope per column and both lines' ordinates per column; the
+// slope depends only on the edge, and the ordinate at Xi1 is the one the next
+// column needs at its Xi (both lines come from the same repeated addition), so
+// callers compute the slope once and carry the ordinate: same doubles, half
+// the FP64 work.
+struct ClipXEdge {
+    float2 A, B;
+    bool vert;
+    double slope, ymin;
+    __device__ ClipXEdge(float2 a, float2 b) : A(a), B(b) {
+        vert = A.x == B.x;
+        ymin = A.y < B.y ? A.y : B.y;
+        slope = vert ? 0.0 : ((double)B.y - A.y) / (double)(B.x - A.x);
     }
+    __device__ double ord(double X) const { return vert ? ymin : slope * (X - B.x) + B.y; }
+};
+
+// Points one column-polygon edge contributes to row r's clip (Ideal.cpp:680-818),
+// given the float points (xi, Yi), (xi1, Yi1) on the row lines and the
+// parallel flag (ClipYEdge).
+__device__ inline int clip_y_points(float2 A, float2 B, double Yi, double Yi1, float2 pi, float2 pi1, bool parallels,
+                                    float2 *out) {
+    int n = 0;
     if (in_rng(Yi, Yi1, A.y)) {
         if (out) out[n] = A;
         n++;
     }
     if (!parallels) {
-        float2 pi = mk(xi, Yi), pi1 = mk(xi1, Yi1);
-        double mny = A.y < B.y ? A.y : B.y, mxy = A.y < B.y ? B.y : A.y;
-        double mnx = A.x < B.x ? A.x : B.x, mxx = A.x < B.x ? B.x : A.x;
-        bool c0 = in_rng(mnx, mxx, pi.x) && in_rng(mny, mxy, pi.y);
-        bool c1 = in_rng(mnx, mxx, pi1.x) && in_rng(mny, mxy, pi1.y);
+        const float mny = A.y < B.y ? A.y : B.y, mxy = A.y < B.y ? B.y : A.y;
+        const float mnx = A.x < B.x ? A.x : B.x, mxx = A.x < B.x ? B.x : A.x;
+        bool c0 = in_rngf(mnx, mxx, pi.x) && in_rngf(mny, mxy, pi.y);
+        bool c1 = in_rngf(mnx, mxx, pi1.x) && in_rngf(mny, mxy, pi1.y);
         if (A.y < B.y) {
             if (c0) { if (out) out[n] = pi; n++; }
             if (c1) { if (out) out[n] = pi1; n++; }
@@ -555,6 +596,47 @@ __device__ int clip_y_points(float2 A, float2 B, double Yi, double Yi1, float2 *
     }
     return n;
 }
+
+// Ideal.cpp:680-730 per edge: vertical edges cut every row line at A.x;
+// horizontal edges touch only a row line they lie on (the other abscissa is
+// -DBL_MAX, which converts to -inf in float) and are otherwise parallel; the
+// rest cut at ((Y - B.y) / slope) + B.x, carried from Yi1 to the next row's Yi
+// as in ClipXEdge.
+struct ClipYEdge {
+    float2 A, B;
+    bool vert, horiz;
+    double slope;
+    __device__ ClipYEdge(float2 a, float2 b) : A(a), B(b) {
+        vert = A.x == B.x;
+        horiz = !vert && A.y == B.y;
+        slope = (vert || horiz) ? 0.0 : ((double)B.y - A.y) / (double)(B.x - A.x);
+    }
+    __device__ bool general() const { return !vert && !horiz; }
+    __device__ double absc(double Y) const { return ((Y - B.y) / slope) + B.x; }
+    // abscissae for row lines Yi, Yi1; g0, g1 are absc(Yi), absc(Yi1) for general edges
+    __device__ void row(double Yi, double Yi1, double g0, double g1, double &xi, double &xi1, bool &par) const {
+        par = false;
+        if (vert) {
+            xi = A.x;
+            xi1 = A.x;
+        } else if (horiz) {
+            xi = 0;
+            xi1 = 0;
+            if (A.y == Yi) {
+                xi = A.x;
+                xi1 = -INFINITY;
+            } else if (A.y == Yi1) {
+                xi = -INFINITY;
+                xi1 = A.x;
+            } else {
+                par = true;
+            }
+        } else {
+            xi = g0;
+            xi1 = g1;
+        }
+    }
+};
 
 // first index i in [0, n) with lines[i] + step >= v, scanning down from a
 // binary-search guess (lines ascending)
@@ -887,9 +969,13 @@ __global__ void k_clipx(const StoreView sv, const PolyHdr *__restrict__ hdr, con
         uint32_t total = 0;
         uint64_t at = scan ? scan[k] : 0;
         float2 buf[4];
-        for (; c < h.ncols && lines[c] <= mxx + mg; c++) {
-            double Xi = lines[c], Xi1 = Xi + h.step_x;
-            int m = clip_x_points(A, B, Xi, Xi1, okey ? buf : nullptr);
+        const ClipXEdge E(A, B);
+        double Xi = c < h.ncols ? lines[c] : 0.0;
+        float2 pi = mk(Xi, E.ord(Xi));
+        for (; c < h.ncols && Xi <= mxx + mg; c++) {
+            const double Xi1 = Xi + h.step_x;  // == lines[c + 1]
+            const float2 pi1 = mk(Xi1, E.ord(Xi1));
+            int m = clip_x_points(A, B, Xi, Xi1, pi, pi1, okey ? buf : nullptr);
             if (okey) {
                 for (int q = 0; q < m; q++) {
                     okey[at] = (h.col - ch.col0) + (uint64_t)c;
@@ -898,6 +984,8 @@ __global__ void k_clipx(const StoreView sv, const PolyHdr *__restrict__ hdr, con
                 }
             }
             total += (uint32_t)m;
+            Xi = Xi1;
+            pi = pi1;
         }
         if (cnt) cnt[k] = total;
     }
@@ -1103,9 +1191,16 @@ __global__ void k_clipy(const PolyHdr *__restrict__ hdr, const uint64_t *__restr
             int r = first_line(lines, h.nrows, h.step_y, mny - mg);
             uint64_t at = scan ? scan[j] : 0;
             float2 buf[4];
-            for (; r < h.nrows && lines[r] <= mxy + mg; r++) {
-                double Yi = lines[r], Yi1 = Yi + h.step_y;
-                int k = clip_y_points(A, B, Yi, Yi1, okey ? buf : nullptr);
+            const ClipYEdge E(A, B);
+            double Yi = r < h.nrows ? lines[r] : 0.0;
+            double g0 = E.general() ? E.absc(Yi) : 0.0;
+            for (; r < h.nrows && Yi <= mxy + mg; r++) {
+                const double Yi1 = Yi + h.step_y;  // == lines[r + 1]
+                const double g1 = E.general() ? E.absc(Yi1) : 0.0;
+                double xi, xi1;
+                bool par;
+                E.row(Yi, Yi1, g0, g1, xi, xi1, par);
+                int k = clip_y_points(A, B, Yi, Yi1, mk(xi, Yi), mk(xi1, Yi1), par, okey ? buf : nullptr);
                 if (okey && k) {
                     uint64_t cell = (h.pix - ch.pix0) + (uint64_t)r * h.dimx + x;
                     for (int q = 0; q < k; q++) {
@@ -1116,6 +1211,8 @@ __global__ void k_clipy(const PolyHdr *__restrict__ hdr, const uint64_t *__restr
                     atomicAdd(&cellcnt[cell], (uint32_t)k);
                 }
                 total += (uint32_t)k;
+                Yi = Yi1;
+                g0 = g1;
             }
         }
         if (cnt) cnt[j] = total;
@@ -1301,6 +1398,39 @@ static uint64_t env_u64(const char *name, uint64_t dflt) {
     return x ? (uint64_t)x : dflt;
 }
 
+// Device time of the rasterizer's heavy kernels: an event pair around each
+// launch, summed per stage once the call has finished (no synchronisation in
+// between).
+enum { T_WALK, T_CLIPX, T_CLIPY, T_CELLS, T_N };
+struct KTimer {
+    std::vector<cudaEvent_t> ev;
+    std::vector<int> stage;  // per pair
+    cudaEvent_t next() {
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        ev.push_back(e);
+        return e;
+    }
+    template <typename F>
+    void time(int stg, cudaStream_t st, F launch) {
+        cudaEvent_t a = next(), b = next();
+        if (a) cudaEventRecord(a, st);
+        launch();
+        if (b) cudaEventRecord(b, st);
+        stage.push_back(a && b ? stg : -1);
+    }
+    void sum(double *ms) {
+        for (size_t k = 0; k < stage.size(); k++) {
+            float t = 0;
+            if (stage[k] >= 0 && cudaEventElapsedTime(&t, ev[2 * k], ev[2 * k + 1]) == cudaSuccess) ms[stage[k]] += t;
+        }
+    }
+    ~KTimer() {
+        for (auto e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+};
+
 struct RasterCtx {
     farm_store *s;
     uint32_t np;
@@ -1311,6 +1441,7 @@ struct RasterCtx {
     double *colx, *rowy;
     int cc;
     int launches = 0;
+    KTimer timer;
 };
 
 static int raster_chunk(RasterCtx &R, const Chunk &ch) {
@@ -1328,7 +1459,7 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     FARM_TRY(s->s[S_SCAN_E].ensure(3 * ne1 * 8 + 16));
     uint32_t *ecnt = s->s[S_CNT_E].as<uint32_t>();
     FARM_CUDA(cudaMemsetAsync(ecnt, 0, 3 * ne1 * 4, st));
-    k_walk_count<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, ecnt);
+    R.timer.time(T_WALK, st, [&] { k_walk_count<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, ecnt); });
     uint64_t *ecnt64 = s->s[S_TMP_A].as<uint64_t>(), *escan = s->s[S_SCAN_E].as<uint64_t>();
     k_u32_to_u64<<<gb(3 * ne1), 256, 0, st>>>(ecnt, 3 * ne1, ecnt64);
     L += 2;
@@ -1337,6 +1468,8 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     FARM_TRY(d2h(s, &nC, escan + ne, 8));
     FARM_TRY(d2h(s, &nH, escan + ne1 + ne, 8));
     FARM_TRY(d2h(s, &nV, escan + 2 * ne1 + ne, 8));
+    s->rtot.crossings += nC;
+    s->rtot.chunks++;
     FARM_TRY(s->s[S_CFROM].ensure(4 * nC + 16));
     FARM_TRY(s->s[S_CTO].ensure(4 * nC + 16));
     FARM_TRY(s->s[S_CEDGE].ensure(4 * nC + 16));
@@ -1346,9 +1479,9 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     FARM_TRY(s->s[S_VNVAL].ensure(8 * nV + 16));
     uint32_t *cfrom = s->s[S_CFROM].as<uint32_t>(), *cto = s->s[S_CTO].as<uint32_t>(),
              *cedge = s->s[S_CEDGE].as<uint32_t>();
-    k_walk_fill<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, escan, cfrom, cto, cedge, s->s[S_HKEY].as<uint64_t>(),
+    R.timer.time(T_WALK, st, [&] { k_walk_fill<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, escan, cfrom, cto, cedge, s->s[S_HKEY].as<uint64_t>(),
                                         s->s[S_HVAL].as<double>(), s->s[S_VNKEY].as<uint64_t>(),
-                                        s->s[S_VNVAL].as<double>());
+                                        s->s[S_VNVAL].as<double>()); });
     L++;
 
     // ---- visits -> edge sequences (process_crosses)
@@ -1436,7 +1569,7 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     FARM_TRY(s->s[S_CNT_E].ensure(4 * ne1 + 16));
     uint32_t *xcnt = s->s[S_CNT_E].as<uint32_t>();
     FARM_CUDA(cudaMemsetAsync(xcnt, 0, 4 * ne1, st));
-    k_clipx<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, R.colx, xcnt, nullptr, nullptr, nullptr);
+    R.timer.time(T_CLIPX, st, [&] { k_clipx<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, R.colx, xcnt, nullptr, nullptr, nullptr); });
     FARM_TRY(s->s[S_TMP_A].ensure(8 * ne1 + 16));
     uint64_t *x64 = s->s[S_TMP_A].as<uint64_t>();
     k_u32_to_u64<<<gb(ne1), 256, 0, st>>>(xcnt, ne1, x64);
@@ -1446,6 +1579,7 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     FARM_TRY(excl_scan(s, x64, xscan, ne1));
     uint64_t nX;
     FARM_TRY(d2h(s, &nX, xscan + ne, 8));
+    s->rtot.clip_x_points += nX;
     FARM_TRY(s->s[S_VKEY].ensure(8 * nX + 16));
     FARM_TRY(s->s[S_VVAL].ensure(8 * nX + 16));
     FARM_TRY(s->s[S_VKEY2].ensure(8 * nX + 16));
@@ -1454,7 +1588,7 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     float2 *xpt = s->s[S_VVAL].as<float2>(), *xpt_s = s->s[S_VVAL2].as<float2>();
     const int colbits = key_bits(ch.ncol);
     if (nX) {
-        k_clipx<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, R.colx, nullptr, xscan, xkey, xpt);
+        R.timer.time(T_CLIPX, st, [&] { k_clipx<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, R.colx, nullptr, xscan, xkey, xpt); });
         L++;
         FARM_TRY(sort_pairs(s, xkey, xkey_s, reinterpret_cast<uint64_t *>(xpt), reinterpret_cast<uint64_t *>(xpt_s),
                             nX, colbits));
@@ -1583,8 +1717,8 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     uint32_t *cellcnt = s->s[S_PIXCNT].as<uint32_t>();
     FARM_CUDA(cudaMemsetAsync(cellcnt, 0, 4 * (ch.npix + 1), st));
     if (nCP) {
-        k_clipy<<<gb(nCP), 256, 0, st>>>(R.hdr, colbase, ch, cpstart, cpoly, nCP, R.rowy, ycnt, nullptr, nullptr,
-                                         nullptr, nullptr);
+        R.timer.time(T_CLIPY, st, [&] { k_clipy<<<gb(nCP), 256, 0, st>>>(R.hdr, colbase, ch, cpstart, cpoly, nCP, R.rowy, ycnt, nullptr, nullptr,
+                                         nullptr, nullptr); });
         L++;
     }
     FARM_TRY(s->s[S_TMP_A].ensure(8 * (nCP + 1) + 16));
@@ -1596,6 +1730,7 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     FARM_TRY(excl_scan(s, y64, yscan, nCP + 1));
     uint64_t nY;
     FARM_TRY(d2h(s, &nY, yscan + nCP, 8));
+    s->rtot.clip_y_points += nY;
     FARM_TRY(s->s[S_VKEY].ensure(8 * nY + 16));
     FARM_TRY(s->s[S_VVAL].ensure(8 * nY + 16));
     FARM_TRY(s->s[S_HKEY].ensure(8 * nY + 16));
@@ -1603,8 +1738,8 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     uint64_t *ykb = s->s[S_VKEY].as<uint64_t>(), *yks = s->s[S_HKEY].as<uint64_t>();
     float2 *ypb = s->s[S_VVAL].as<float2>(), *yps = s->s[S_HVAL].as<float2>();
     if (nY) {
-        k_clipy<<<gb(nCP), 256, 0, st>>>(R.hdr, colbase, ch, cpstart, cpoly, nCP, R.rowy, nullptr, yscan, ykb, ypb,
-                                         cellcnt);
+        R.timer.time(T_CLIPY, st, [&] { k_clipy<<<gb(nCP), 256, 0, st>>>(R.hdr, colbase, ch, cpstart, cpoly, nCP, R.rowy, nullptr, yscan, ykb, ypb,
+                                         cellcnt); });
         L++;
         FARM_TRY(sort_pairs(s, ykb, yks, reinterpret_cast<uint64_t *>(ypb), reinterpret_cast<uint64_t *>(yps), nY,
                             key_bits(ch.npix)));
@@ -1614,8 +1749,8 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     k_u32_to_u64<<<gb(ch.npix + 1), 256, 0, st>>>(cellcnt, ch.npix + 1, c64);
     L++;
     FARM_TRY(excl_scan(s, c64, cellstart, ch.npix + 1));
-    k_cells<<<gb(ch.npix), 256, 0, st>>>(R.hdr, pixbase, ch, cellstart, yps, cpstart, s->d_status.as<uint8_t>(),
-                                         s->d_areas.as<double>(), R.cc);
+    R.timer.time(T_CELLS, st, [&] { k_cells<<<gb(ch.npix), 256, 0, st>>>(R.hdr, pixbase, ch, cellstart, yps, cpstart, s->d_status.as<uint8_t>(),
+                                         s->d_areas.as<double>(), R.cc); });
     L++;
 
     // ---- hierarchy
@@ -1656,6 +1791,9 @@ int rasterize(farm_store *s, const farm_raster_opts *o, int *launches) {
     }
     cudaStream_t st = s->stream;
     RasterCtx R;
+    cudaEvent_t t_begin = R.timer.next(), t_end = R.timer.next();
+    R.timer.stage.push_back(-1);  // the pair (t_begin, t_end) is read separately
+    if (t_begin) cudaEventRecord(t_begin, st);
     R.s = s;
     R.np = np;
     R.n1 = (uint64_t)np + 1;
@@ -1694,13 +1832,19 @@ int rasterize(farm_store *s, const farm_raster_opts *o, int *launches) {
     k_bases<<<gb(np), 256, 0, st>>>(R.hdr, np, scan, R.colx, R.rowy);
     R.launches++;
 
+    memset(&s->rtot, 0, sizeof s->rtot);
+    s->rtot.polygons = np;
+    s->rtot.vertices = ne;
+    s->rtot.pixels = totP;
+    s->rtot.status_bytes = totStatus;
+
     // ---- phase 1: per-polygon totals size the sequence and node arrays
     {
         StoreView sv = s->view();
         FARM_TRY(s->s[S_TMP_B].ensure(3 * 8 * n1 + 16));
         unsigned long long *tot3 = s->s[S_TMP_B].as<unsigned long long>();
         FARM_CUDA(cudaMemsetAsync(tot3, 0, 3 * 8 * n1, st));
-        k_walk_tot<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, np, ne, tot3);
+        R.timer.time(T_WALK, st, [&] { k_walk_tot<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, np, ne, tot3); });
         FARM_TRY(s->s[S_TMP_A].ensure(2 * 3 * 8 * n1 + 16));
         uint64_t *sz = s->s[S_TMP_A].as<uint64_t>(), *sc = sz + 3 * n1;
         k_tot_sizes<<<gb(n1), 256, 0, st>>>(tot3, R.hdr, np, sz);
@@ -1716,6 +1860,9 @@ int rasterize(farm_store *s, const farm_raster_opts *o, int *launches) {
         FARM_TRY(s->d_hnodes.ensure(8 * th + 16));
         FARM_TRY(s->d_vnodes.ensure(8 * tv + 16));
         s->tot_seq = tseq;
+        s->rtot.sequences = tseq;
+        s->rtot.hnodes = th;
+        s->rtot.vnodes = tv;
     }
 
     // ---- phase 2: chunks
@@ -1762,6 +1909,8 @@ int rasterize(farm_store *s, const farm_raster_opts *o, int *launches) {
     }
     (void)totRow;
 
+    if (t_end) cudaEventRecord(t_end, st);
+
     // errors
     FARM_TRY(s->d_counters.ensure(64));
     int *derr = s->d_counters.as<int>();
@@ -1773,6 +1922,16 @@ int rasterize(farm_store *s, const farm_raster_opts *o, int *launches) {
     FARM_CUDA(cudaStreamSynchronize(st));
     s->tot_P = totP;
     s->tot_status = totStatus;
+    {
+        double ms[T_N] = {0, 0, 0, 0};
+        R.timer.sum(ms);
+        s->rtot.ms_walk = ms[T_WALK];
+        s->rtot.ms_clip_x = ms[T_CLIPX];
+        s->rtot.ms_clip_y = ms[T_CLIPY];
+        s->rtot.ms_cells = ms[T_CELLS];
+        float t = 0;
+        if (t_begin && t_end && cudaEventElapsedTime(&t, t_begin, t_end) == cudaSuccess) s->rtot.ms_total = t;
+    }
     if (launches) *launches = R.launches;
     if (herr) {
         set_error(herr == FARM_EASSERT
@@ -1784,6 +1943,16 @@ int rasterize(farm_store *s, const farm_raster_opts *o, int *launches) {
 }
 
 }  // namespace farm
+
+extern "C" int farm_raster_get_totals(farm_store *s, farm_raster_totals *out) {
+    using namespace farm;
+    if (!s || !out) {
+        set_error("invalid arguments to farm_raster_get_totals");
+        return FARM_EINVAL;
+    }
+    *out = s->rtot;
+    return FARM_OK;
+}
 
 extern "C" int farm_rasterize(farm_store *s, const farm_raster_opts *o) {
     using namespace farm;

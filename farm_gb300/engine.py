@@ -25,7 +25,7 @@ import ctypes as C
 import numpy as np
 
 from . import _native
-from ._gpu_sig import RasterOpts, RasterView, Stats
+from ._gpu_sig import RasterOpts, RasterTotals, RasterView, Stats
 from ._native import check_gpu, gpu
 
 MODE_EXACT = 0
@@ -202,6 +202,12 @@ class Store:
     def launches(self) -> int:
         """Engine kernels launched through this store so far."""
         return int(self._lib.farm_store_launches(self._h))
+
+    def raster_totals(self) -> dict:
+        """Sizes of the last rasterization (units processed, arrays written)."""
+        t = RasterTotals()
+        check_gpu(self._lib.farm_raster_get_totals(self._h, C.byref(t)))
+        return {k: (float(getattr(t, k)) if k.startswith("ms_") else int(getattr(t, k))) for k, _ in RasterTotals._fields_}
 
     def event_record(self, slot: int) -> None:
         check_gpu(self._lib.farm_event_record(self._h, slot))

@@ -103,15 +103,34 @@ int farm_gen_counts(const farm_gen_params *gp, uint64_t seed, uint64_t first, ui
     return FARM_OK;
 }
 
-int farm_gen_fill(const farm_gen_params *gp, uint64_t seed, uint64_t first, uint64_t count,
-                  const uint64_t *off, float *xy, int threads) {
+int farm_gen_centres(const farm_gen_params *gp, uint64_t seed, uint64_t first, uint64_t count, double *cxyr) {
+    if (!gp || (!cxyr && count)) return fail(FARM_EINVAL, "null argument");
+    if (!(gp->r_lo > 0) || gp->r_hi < gp->r_lo) return fail(FARM_EINVAL, "radius range must satisfy 0 < r_lo <= r_hi");
+    const double span = gp->dom_hi - gp->dom_lo;
+    const double lr0 = std::log(gp->r_lo), lr1 = std::log(gp->r_hi);
+    for (uint64_t k = 0; k < count; k++) {
+        uint64_t i = first + k;
+        cxyr[3 * k] = gp->dom_lo + span * rng_open01(seed, i, S_CX, 0);
+        cxyr[3 * k + 1] = gp->dom_lo + span * rng_open01(seed, i, S_CY, 0);
+        cxyr[3 * k + 2] = std::exp(lr0 + rng_open01(seed, i, S_R, 0) * (lr1 - lr0));
+    }
+    return FARM_OK;
+}
+
+}  // extern "C"
+
+namespace {
+// Fills polygon k of the output with generator polygon index(k).
+template <typename Index>
+int gen_fill(const farm_gen_params *gp, uint64_t seed, Index index, uint64_t count, const uint64_t *off, float *xy,
+             int threads) {
     if (!gp || !off || (!xy && count)) return fail(FARM_EINVAL, "null argument");
     const double two_pi = 6.283185307179586476925286766559;
     std::atomic<int> bad(0);
     parallel_chunks(count, threads, 64, [&](uint64_t b, uint64_t e) {
         std::vector<double> cum;
         for (uint64_t k = b; k < e; k++) {
-            uint64_t i = first + k;
+            uint64_t i = index(k);
             uint32_t m = gen_count(gp, seed, i);
             if (off[k + 1] - off[k] != m) {
                 bad = 1;
@@ -158,6 +177,28 @@ int farm_gen_fill(const farm_gen_params *gp, uint64_t seed, uint64_t first, uint
     });
     if (bad) return fail(FARM_EINVAL, "offsets do not match the generator's vertex counts");
     return FARM_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int farm_gen_fill(const farm_gen_params *gp, uint64_t seed, uint64_t first, uint64_t count, const uint64_t *off,
+                  float *xy, int threads) {
+    return gen_fill(gp, seed, [first](uint64_t k) { return first + k; }, count, off, xy, threads);
+}
+
+int farm_gen_counts_idx(const farm_gen_params *gp, uint64_t seed, const uint64_t *idx, uint64_t count,
+                        uint32_t *nverts_out) {
+    if (!gp || (count && (!idx || !nverts_out))) return fail(FARM_EINVAL, "null argument");
+    if (gp->n_lo < 3 || gp->n_hi < gp->n_lo) return fail(FARM_EINVAL, "vertex-count range must satisfy 3 <= n_lo <= n_hi");
+    for (uint64_t k = 0; k < count; k++) nverts_out[k] = gen_count(gp, seed, idx[k]);
+    return FARM_OK;
+}
+
+int farm_gen_fill_idx(const farm_gen_params *gp, uint64_t seed, const uint64_t *idx, uint64_t count,
+                      const uint64_t *off, float *xy, int threads) {
+    if (count && !idx) return fail(FARM_EINVAL, "null argument");
+    return gen_fill(gp, seed, [idx](uint64_t k) { return idx[k]; }, count, off, xy, threads);
 }
 
 static void ring_mbr(const float *p, uint64_t m, double *b) {

@@ -86,6 +86,39 @@ def generate(params: StarParams, seed: int, count: int, first: int = 0, threads:
     return PolygonSet(off, xy)
 
 
+def centres(params: StarParams, seed: int, count: int, first: int = 0) -> np.ndarray:
+    """Centre x, y and mean radius of generator polygons first..first+count-1; float64 [count, 3]."""
+    gp = params.c()
+    out = np.zeros((count, 3), dtype=np.float64)
+    check_host(host().farm_gen_centres(C.byref(gp), seed, first, count, ptr(out, f64p)))
+    return out
+
+
+def generate_indices(params: StarParams, seed: int, idx, threads: int = 0, out_off=None, out_xy=None) -> PolygonSet:
+    """Generator polygons idx[0], idx[1], ... (any order) as one set. out_off / out_xy
+    may supply preallocated (e.g. pinned) arrays of the right sizes."""
+    gp = params.c()
+    idx = np.ascontiguousarray(idx, dtype=np.uint64)
+    lib = host()
+    counts = np.zeros(len(idx), dtype=np.uint32)
+    check_host(lib.farm_gen_counts_idx(C.byref(gp), seed, ptr(idx, u64p), len(idx), ptr(counts, u32p)))
+    off = out_off if out_off is not None else np.zeros(len(idx) + 1, dtype=np.uint64)
+    off[0] = 0
+    np.cumsum(counts, dtype=np.uint64, out=off[1:])
+    xy = out_xy if out_xy is not None else np.empty((int(off[-1]), 2), dtype=np.float32)
+    check_host(lib.farm_gen_fill_idx(C.byref(gp), seed, ptr(idx, u64p), len(idx), ptr(off, u64p), ptr(xy, f32p),
+                                     threads))
+    return PolygonSet(off, xy)
+
+
+def vertex_counts(params: StarParams, seed: int, idx) -> np.ndarray:
+    gp = params.c()
+    idx = np.ascontiguousarray(idx, dtype=np.uint64)
+    counts = np.zeros(len(idx), dtype=np.uint32)
+    check_host(host().farm_gen_counts_idx(C.byref(gp), seed, ptr(idx, u64p), len(idx), ptr(counts, u32p)))
+    return counts
+
+
 def mbr_join(ms: np.ndarray, mt: np.ndarray, expand: float = 0.0, geography: bool = False,
              skip_same: bool = False, threads: int = 0) -> np.ndarray:
     """Candidate pairs (s, t) with overlapping closed MBRs, sorted; uint32 [k, 2]."""

@@ -179,6 +179,22 @@ int farm_mlp_predict(farm_store *s, const uint32_t *d_pairs, uint64_t n, float *
  * never terminates (such polygons are reported, not rasterized). */
 int farm_raster_errors(farm_store *s, int side, int32_t *err, uint64_t n);
 
+/* Sizes of the last rasterization, summed over both sides: the units the
+ * rasterizer's kernels process (crossings, fill-clip points) and the raster
+ * arrays it wrote. No counterpart in the reference. */
+typedef struct farm_raster_totals {
+    uint64_t polygons, vertices;       /* vertices = edges (closing copy included) */
+    uint64_t pixels, status_bytes;     /* finest pixels; status incl. coarser layers */
+    uint64_t sequences, hnodes, vnodes;
+    uint64_t crossings;                /* pixel-boundary crossings of the edge walk */
+    uint64_t clip_x_points, clip_y_points; /* points emitted by the column / cell clips */
+    uint64_t chunks;
+    /* device time (CUDA events) of the edge-walk kernels, the column-clip
+     * kernels, the cell-clip kernels, the cell-area kernel, and the whole call */
+    double ms_walk, ms_clip_x, ms_clip_y, ms_cells, ms_total;
+} farm_raster_totals;
+int farm_raster_get_totals(farm_store *s, farm_raster_totals *out);
+
 /* Wait for outstanding work of the store's stream. */
 int farm_sync(farm_store *s);
 

@@ -52,10 +52,20 @@ typedef struct farm_gen_params {
 /* Pass 1: per-polygon stored vertex counts (N distinct + 1 closing copy). */
 int farm_gen_counts(const farm_gen_params *gp, uint64_t seed, uint64_t first, uint64_t count,
                     uint32_t *nverts_out);
+/* Centre (cx, cy) and mean radius of each polygon, 3 doubles per polygon,
+ * without drawing its vertices (the same counters as farm_gen_fill). */
+int farm_gen_centres(const farm_gen_params *gp, uint64_t seed, uint64_t first, uint64_t count, double *cxyr);
 /* Pass 2: fill rings; off (count+1 entries) must be the exclusive scan of the
  * counts from pass 1 (off[0] may be non-zero: it is an absolute offset into xy). */
 int farm_gen_fill(const farm_gen_params *gp, uint64_t seed, uint64_t first, uint64_t count,
                   const uint64_t *off, float *xy, int threads);
+
+/* The same two passes for an arbitrary list of generator indices: output
+ * polygon k is generator polygon idx[k]. */
+int farm_gen_counts_idx(const farm_gen_params *gp, uint64_t seed, const uint64_t *idx, uint64_t count,
+                        uint32_t *nverts_out);
+int farm_gen_fill_idx(const farm_gen_params *gp, uint64_t seed, const uint64_t *idx, uint64_t count,
+                      const uint64_t *off, float *xy, int threads);
 
 /* .dt files (storage.cpp format): records [size_t holes][size_t nv][nv x float2] ...,
  * then PolygonMeta[n] {uint32 size, uint32 nv, uint64 offset, double mbr[4]},
