@@ -201,7 +201,7 @@ struct farm_store {
     uint64_t tot_P = 0, tot_status = 0, tot_seq = 0;
     farm_raster_totals rtot = {};
     // scratch for the rasterizer and the queries
-    farm::DevBuf s[32];
+    farm::DevBuf s[40];
     farm::DevBuf cub_tmp;
     farm::DevBuf d_pairs, d_out, d_counters;
     cudaEvent_t ev[8] = {};

@@ -16,6 +16,8 @@
 // cost is linear in the output, not columns x vertices.
 #include <cub/cub.cuh>
 
+#include <algorithm>
+
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -60,6 +62,10 @@ enum Scratch {
     S_SMALL_K,  // small-point sort keys and dependency lists
     S_SMALL_V,
     S_SMALL_D,
+    S_PERM_K,  // walk / clip order: per-item cost keys / permutation
+    S_PERM,
+    S_CPCOL,    // column of each column-polygon point
+    S_COLPOLY,  // polygon of each fill column
 };
 
 // ------------------------------------------------------------ headers ----
@@ -681,10 +687,35 @@ struct Chunk {
     uint64_t hn0, vn0;   // global node bases of the chunk's first polygon
 };
 
+// Walk order: an FP32 estimate of the pixels an edge crosses, so that the
+// lanes of a warp walk edges of similar length (the walk's trip count varies
+// from 0 to dozens of steps, and a warp pays for its longest lane). The order
+// only schedules the walks; every walk itself is exact.
+__global__ void k_edge_cost(const StoreView sv, const PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off,
+                            uint32_t p0, uint32_t np, uint64_t e0, uint64_t ne, int x_only, uint8_t *__restrict__ key,
+                            uint32_t *__restrict__ idx) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < ne; k += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t e = e0 + k;
+        uint32_t p = p0 + find_segment(off + p0, np, e);
+        const PolyHdr &h = hdr[p];
+        float c = 0.f;
+        if (h.err == 0) {
+            uint32_t i = (uint32_t)(e - h.edge);
+            const float2 *r = sv.ring + h.ring;
+            float2 A = r[i], B = r[i + 1];
+            c = fabsf(B.x - A.x) / (float)h.step_x + (x_only ? 0.f : fabsf(B.y - A.y) / (float)h.step_y);
+        }
+        key[k] = (uint8_t)(c < 255.f ? c : 255.f);
+        idx[k] = (uint32_t)k;
+    }
+}
+
 __global__ void k_walk_tot(const StoreView sv, PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off,
-                           uint32_t npoly, uint64_t nedges, unsigned long long *__restrict__ tot) {
-    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nedges;
-         e += (uint64_t)gridDim.x * blockDim.x) {
+                           uint32_t npoly, uint64_t e0, uint64_t nedges, const uint32_t *__restrict__ perm,
+                           unsigned long long *__restrict__ tot) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nedges;
+         k += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t e = e0 + perm[k];
         uint32_t p = find_segment(off, npoly, e);
         const PolyHdr &h = hdr[p];
         if (h.err) continue;
@@ -732,10 +763,11 @@ __global__ void k_set_node_bases(PolyHdr *__restrict__ hdr, uint32_t npoly, cons
 }
 
 __global__ void k_walk_count(const StoreView sv, PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off,
-                             Chunk ch, uint32_t *__restrict__ cnt) {
+                             Chunk ch, const uint32_t *__restrict__ perm, uint32_t *__restrict__ cnt) {
     uint64_t n1 = ch.ne + 1;
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < ch.ne;
-         k += (uint64_t)gridDim.x * blockDim.x) {
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < ch.ne;
+         j += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t k = perm[j];
         uint64_t e = ch.e0 + k;
         uint32_t p = ch.p0 + find_segment(off + ch.p0, ch.np, e);
         const PolyHdr &h = hdr[p];
@@ -756,11 +788,13 @@ __global__ void k_walk_count(const StoreView sv, PolyHdr *__restrict__ hdr, cons
 }
 
 __global__ void k_walk_fill(const StoreView sv, const PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off,
-                            Chunk ch, const uint64_t *__restrict__ scan, uint32_t *from, uint32_t *to,
-                            uint32_t *cedge, uint64_t *hkey, double *hval, uint64_t *vkey, double *vval) {
+                            Chunk ch, const uint32_t *__restrict__ perm, const uint64_t *__restrict__ scan,
+                            uint32_t *from, uint32_t *to, uint32_t *cedge, uint64_t *hkey, double *hval,
+                            uint64_t *vkey, double *vval) {
     uint64_t n1 = ch.ne + 1;
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < ch.ne;
-         k += (uint64_t)gridDim.x * blockDim.x) {
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < ch.ne;
+         j += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t k = perm[j];
         // walk exactly the edges the count pass walked (those with output)
         if (scan[k + 1] == scan[k] && scan[n1 + k + 1] == scan[n1 + k] && scan[2 * n1 + k + 1] == scan[2 * n1 + k])
             continue;
@@ -948,10 +982,12 @@ __global__ void k_scanline(const PolyHdr *__restrict__ hdr, const uint64_t *__re
 
 // Per edge: points contributed to every column (count pass or emit pass).
 __global__ void k_clipx(const StoreView sv, const PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off,
-                        Chunk ch, const double *__restrict__ colx, uint32_t *__restrict__ cnt,
-                        const uint64_t *__restrict__ scan, uint64_t *__restrict__ okey, float2 *__restrict__ opt) {
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < ch.ne;
-         k += (uint64_t)gridDim.x * blockDim.x) {
+                        Chunk ch, const uint32_t *__restrict__ perm, const double *__restrict__ colx,
+                        uint32_t *__restrict__ cnt, const uint64_t *__restrict__ scan, uint64_t *__restrict__ okey,
+                        float2 *__restrict__ opt) {
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < ch.ne;
+         j += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t k = perm[j];
         uint64_t e = ch.e0 + k;
         uint32_t p = ch.p0 + find_segment(off + ch.p0, ch.np, e);
         const PolyHdr &h = hdr[p];
@@ -1014,9 +1050,15 @@ __global__ void k_dup_large(const uint64_t *__restrict__ col, const uint32_t *__
     }
 }
 
-__global__ void k_col_count(const uint64_t *__restrict__ colkey, uint64_t n, uint32_t *__restrict__ colcnt) {
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
-        atomicAdd(&colcnt[colkey[k]], 1u);
+// Segment starts of sorted keys: starts[c] = first index k with key[k] >= c,
+// for c in [0, nseg] (keys < nseg). Thread k fills the segments that begin at k.
+__global__ void k_seg_starts(const uint64_t *__restrict__ key, uint64_t n, uint64_t nseg,
+                             uint64_t *__restrict__ starts) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k <= n; k += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t lo = k == 0 ? 0 : key[k - 1] + 1;
+        uint64_t hi = k == n ? nseg : key[k];
+        for (uint64_t c = lo; c <= hi; c++) starts[c] = k;
+    }
 }
 
 // Small points that are the first copy of their bit pattern in their column
@@ -1159,30 +1201,59 @@ __global__ void k_cp_sizes(const uint64_t *__restrict__ colstart, const uint64_t
 __global__ void k_col_polys(const uint64_t *__restrict__ colkey, const float2 *__restrict__ pt,
                             const uint8_t *__restrict__ drop, const uint64_t *__restrict__ keptscan, uint64_t n,
                             const uint64_t *__restrict__ colstart, const uint64_t *__restrict__ cpstart,
-                            float2 *__restrict__ cpoly) {
+                            float2 *__restrict__ cpoly, uint32_t *__restrict__ cpcol) {
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
         if (drop[k]) continue;
         uint64_t c = colkey[k];
         uint64_t rank = keptscan[k] - keptscan[colstart[c]];
         cpoly[cpstart[c] + rank] = pt[k];
+        cpcol[cpstart[c] + rank] = (uint32_t)c;
         if (rank == 0) {
             uint64_t nk = keptscan[colstart[c + 1]] - keptscan[colstart[c]];
             cpoly[cpstart[c] + nk] = pt[k];
+            cpcol[cpstart[c] + nk] = (uint32_t)c;
         }
     }
 }
 
-// Per column-polygon edge: points contributed to each row (count or emit).
-__global__ void k_clipy(const PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ colbase, Chunk ch,
-                        const uint64_t *__restrict__ cpstart, const float2 *__restrict__ cpoly, uint64_t ncp,
-                        const double *__restrict__ rowy, uint32_t *__restrict__ cnt, const uint64_t *__restrict__ scan,
-                        uint64_t *__restrict__ okey, float2 *__restrict__ opt, uint32_t *__restrict__ cellcnt) {
+// polygon owning each fill column of the chunk
+__global__ void k_col_owner(const PolyHdr *__restrict__ hdr, Chunk ch, uint32_t *__restrict__ colpoly) {
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < ch.np; q += gridDim.x * blockDim.x) {
+        const PolyHdr &h = hdr[ch.p0 + q];
+        const uint64_t c0 = h.col - ch.col0;
+        for (int32_t c = 0; c < h.ncols; c++) colpoly[c0 + c] = ch.p0 + q;
+    }
+}
+
+// cell-clip order: rows an edge of a column polygon spans (FP32 estimate)
+__global__ void k_cp_cost(const PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ cpstart,
+                          const float2 *__restrict__ cpoly, const uint32_t *__restrict__ cpcol,
+                          const uint32_t *__restrict__ colpoly, uint64_t ncp, uint8_t *__restrict__ key,
+                          uint32_t *__restrict__ idx) {
     for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < ncp; j += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t c = find_segment(cpstart, (uint32_t)ch.ncol, j);
+        const uint32_t c = cpcol[j];
+        float cost = 0.f;
+        if (j + 1 < cpstart[c + 1]) {
+            float2 A = cpoly[j], B = cpoly[j + 1];
+            cost = fabsf(B.y - A.y) / (float)hdr[colpoly[c]].step_y;
+        }
+        key[j] = (uint8_t)(cost < 255.f ? cost : 255.f);
+        idx[j] = (uint32_t)j;
+    }
+}
+
+// Per column-polygon edge: points contributed to each row (count or emit).
+__global__ void k_clipy(const PolyHdr *__restrict__ hdr, Chunk ch, const uint32_t *__restrict__ perm,
+                        const uint64_t *__restrict__ cpstart, const float2 *__restrict__ cpoly,
+                        const uint32_t *__restrict__ cpcol, const uint32_t *__restrict__ colpoly, uint64_t ncp,
+                        const double *__restrict__ rowy, uint32_t *__restrict__ cnt, const uint64_t *__restrict__ scan,
+                        uint64_t *__restrict__ okey, float2 *__restrict__ opt) {
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < ncp; t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t j = perm[t];
+        const uint64_t c = cpcol[j];
         uint32_t total = 0;
         if (j + 1 < cpstart[c + 1]) {
-            uint32_t p = ch.p0 + find_segment(colbase + ch.p0, ch.np, c + ch.col0);
-            const PolyHdr &h = hdr[p];
+            const PolyHdr &h = hdr[colpoly[c]];
             int x = (int)(c + ch.col0 - h.col);
             float2 A = cpoly[j], B = cpoly[j + 1];
             double mny = A.y < B.y ? A.y : B.y, mxy = A.y < B.y ? B.y : A.y;
@@ -1194,13 +1265,25 @@ __global__ void k_clipy(const PolyHdr *__restrict__ hdr, const uint64_t *__restr
             const ClipYEdge E(A, B);
             double Yi = r < h.nrows ? lines[r] : 0.0;
             double g0 = E.general() ? E.absc(Yi) : 0.0;
+            // the point on line Yi, carried from the previous row's Yi1
+            // (horizontal edges take per-row abscissae instead)
+            float2 pc = mk(E.vert ? (double)A.x : g0, Yi);
             for (; r < h.nrows && Yi <= mxy + mg; r++) {
                 const double Yi1 = Yi + h.step_y;  // == lines[r + 1]
                 const double g1 = E.general() ? E.absc(Yi1) : 0.0;
                 double xi, xi1;
                 bool par;
                 E.row(Yi, Yi1, g0, g1, xi, xi1, par);
-                int k = clip_y_points(A, B, Yi, Yi1, mk(xi, Yi), mk(xi1, Yi1), par, okey ? buf : nullptr);
+                float2 pi, pi1;
+                if (E.horiz) {
+                    pi = mk(xi, Yi);
+                    pi1 = mk(xi1, Yi1);
+                } else {
+                    pi = pc;
+                    pi1 = mk(xi1, Yi1);
+                    pc = pi1;
+                }
+                int k = clip_y_points(A, B, Yi, Yi1, pi, pi1, par, okey ? buf : nullptr);
                 if (okey && k) {
                     uint64_t cell = (h.pix - ch.pix0) + (uint64_t)r * h.dimx + x;
                     for (int q = 0; q < k; q++) {
@@ -1208,7 +1291,6 @@ __global__ void k_clipy(const PolyHdr *__restrict__ hdr, const uint64_t *__restr
                         opt[at] = buf[q];
                         at++;
                     }
-                    atomicAdd(&cellcnt[cell], (uint32_t)k);
                 }
                 total += (uint32_t)k;
                 Yi = Yi1;
@@ -1442,7 +1524,24 @@ struct RasterCtx {
     int cc;
     int launches = 0;
     KTimer timer;
+    std::vector<uint64_t> hoff;  // per-polygon first edge (host copy of doff)
 };
+
+// Edges [e0, e0 + ne) of polygons [p0, p0 + np) in walk order (k_edge_cost).
+static int edge_order(RasterCtx &R, uint32_t p0, uint32_t np, uint64_t e0, uint64_t ne, const uint32_t **perm,
+                      int x_only = 0) {
+    farm_store *s = R.s;
+    cudaStream_t st = s->stream;
+    FARM_TRY(s->s[S_PERM_K].ensure(2 * ne + 16));
+    FARM_TRY(s->s[S_PERM].ensure(8 * ne + 16));
+    uint8_t *key = s->s[S_PERM_K].as<uint8_t>(), *key_s = key + ne;
+    uint32_t *idx = s->s[S_PERM].as<uint32_t>(), *idx_s = idx + ne;
+    k_edge_cost<<<gb(ne), 256, 0, st>>>(s->view(), R.hdr, R.doff, p0, np, e0, ne, x_only, key, idx);
+    R.launches++;
+    FARM_TRY(sort_pairs(s, key, key_s, idx, idx_s, ne, 8));
+    *perm = idx_s;
+    return FARM_OK;
+}
 
 static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     farm_store *s = R.s;
@@ -1450,7 +1549,7 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     int &L = R.launches;
     StoreView sv = s->view();
     sv.category_count = R.cc;
-    const uint64_t *pixbase = R.scan + 0 * R.n1, *colbase = R.scan + 5 * R.n1, *rowbase = R.scan + 7 * R.n1;
+    const uint64_t *pixbase = R.scan + 0 * R.n1, *rowbase = R.scan + 7 * R.n1;
     const uint64_t ne = ch.ne, ne1 = ne + 1;
 
     // ---- edge walk: count, scan, fill
@@ -1459,7 +1558,9 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     FARM_TRY(s->s[S_SCAN_E].ensure(3 * ne1 * 8 + 16));
     uint32_t *ecnt = s->s[S_CNT_E].as<uint32_t>();
     FARM_CUDA(cudaMemsetAsync(ecnt, 0, 3 * ne1 * 4, st));
-    R.timer.time(T_WALK, st, [&] { k_walk_count<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, ecnt); });
+    const uint32_t *perm = nullptr;
+    FARM_TRY(edge_order(R, ch.p0, ch.np, ch.e0, ne, &perm));
+    R.timer.time(T_WALK, st, [&] { k_walk_count<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, perm, ecnt); });
     uint64_t *ecnt64 = s->s[S_TMP_A].as<uint64_t>(), *escan = s->s[S_SCAN_E].as<uint64_t>();
     k_u32_to_u64<<<gb(3 * ne1), 256, 0, st>>>(ecnt, 3 * ne1, ecnt64);
     L += 2;
@@ -1479,7 +1580,7 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     FARM_TRY(s->s[S_VNVAL].ensure(8 * nV + 16));
     uint32_t *cfrom = s->s[S_CFROM].as<uint32_t>(), *cto = s->s[S_CTO].as<uint32_t>(),
              *cedge = s->s[S_CEDGE].as<uint32_t>();
-    R.timer.time(T_WALK, st, [&] { k_walk_fill<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, escan, cfrom, cto, cedge, s->s[S_HKEY].as<uint64_t>(),
+    R.timer.time(T_WALK, st, [&] { k_walk_fill<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, perm, escan, cfrom, cto, cedge, s->s[S_HKEY].as<uint64_t>(),
                                         s->s[S_HVAL].as<double>(), s->s[S_VNKEY].as<uint64_t>(),
                                         s->s[S_VNVAL].as<double>()); });
     L++;
@@ -1569,7 +1670,9 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     FARM_TRY(s->s[S_CNT_E].ensure(4 * ne1 + 16));
     uint32_t *xcnt = s->s[S_CNT_E].as<uint32_t>();
     FARM_CUDA(cudaMemsetAsync(xcnt, 0, 4 * ne1, st));
-    R.timer.time(T_CLIPX, st, [&] { k_clipx<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, R.colx, xcnt, nullptr, nullptr, nullptr); });
+    const uint32_t *xperm = nullptr;
+    FARM_TRY(edge_order(R, ch.p0, ch.np, ch.e0, ne, &xperm, 1));
+    R.timer.time(T_CLIPX, st, [&] { k_clipx<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, xperm, R.colx, xcnt, nullptr, nullptr, nullptr); });
     FARM_TRY(s->s[S_TMP_A].ensure(8 * ne1 + 16));
     uint64_t *x64 = s->s[S_TMP_A].as<uint64_t>();
     k_u32_to_u64<<<gb(ne1), 256, 0, st>>>(xcnt, ne1, x64);
@@ -1588,7 +1691,7 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     float2 *xpt = s->s[S_VVAL].as<float2>(), *xpt_s = s->s[S_VVAL2].as<float2>();
     const int colbits = key_bits(ch.ncol);
     if (nX) {
-        R.timer.time(T_CLIPX, st, [&] { k_clipx<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, R.colx, nullptr, xscan, xkey, xpt); });
+        R.timer.time(T_CLIPX, st, [&] { k_clipx<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, xperm, R.colx, nullptr, xscan, xkey, xpt); });
         L++;
         FARM_TRY(sort_pairs(s, xkey, xkey_s, reinterpret_cast<uint64_t *>(xpt), reinterpret_cast<uint64_t *>(xpt_s),
                             nX, colbits));
@@ -1620,20 +1723,12 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
         k_dup_large<<<gb(nX), 256, 0, st>>>(ck_s, pos2, xpt_s, nX, drop);
         L++;
     }
-    // column starts
+    // column starts (the points are sorted by column)
     const uint64_t ncol = ch.ncol;
-    FARM_TRY(s->s[S_LINECNT].ensure(4 * (ncol + 1) + 16));
-    FARM_TRY(s->s[S_LINESCAN].ensure(8 * (ncol + 1) * 2 + 16));
-    uint32_t *colcnt = s->s[S_LINECNT].as<uint32_t>();
-    uint64_t *cc64 = s->s[S_LINESCAN].as<uint64_t>(), *colstart = cc64 + (ncol + 1);
-    FARM_CUDA(cudaMemsetAsync(colcnt, 0, 4 * (ncol + 1), st));
-    if (nX) {
-        k_col_count<<<gb(nX), 256, 0, st>>>(xkey_s, nX, colcnt);
-        L++;
-    }
-    k_u32_to_u64<<<gb(ncol + 1), 256, 0, st>>>(colcnt, ncol + 1, cc64);
+    FARM_TRY(s->s[S_LINESCAN].ensure(8 * (ncol + 1) + 16));
+    uint64_t *colstart = s->s[S_LINESCAN].as<uint64_t>();
+    k_seg_starts<<<gb(nX + 1), 256, 0, st>>>(xkey_s, nX, ncol, colstart);
     L++;
-    FARM_TRY(excl_scan(s, cc64, colstart, ncol + 1));
     if (nX) {
         // small first copies: tolerance-equality dependencies, then the
         // sequential rule on them
@@ -1703,22 +1798,36 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     uint64_t nCP;
     FARM_TRY(d2h(s, &nCP, cpstart + ncol, 8));
     FARM_TRY(s->s[S_CPOLY].ensure(8 * nCP + 16));
+    FARM_TRY(s->s[S_CPCOL].ensure(4 * nCP + 16));
+    FARM_TRY(s->s[S_COLPOLY].ensure(4 * ncol + 16));
     float2 *cpoly = s->s[S_CPOLY].as<float2>();
+    uint32_t *cpcol = s->s[S_CPCOL].as<uint32_t>(), *colpoly = s->s[S_COLPOLY].as<uint32_t>();
     if (nX) {
-        k_col_polys<<<gb(nX), 256, 0, st>>>(xkey_s, xpt_s, drop, keptscan, nX, colstart, cpstart, cpoly);
+        k_col_polys<<<gb(nX), 256, 0, st>>>(xkey_s, xpt_s, drop, keptscan, nX, colstart, cpstart, cpoly, cpcol);
         L++;
+    }
+    k_col_owner<<<gb(ch.np), 256, 0, st>>>(R.hdr, ch, colpoly);
+    L++;
+    // cell-clip order: edges by the rows they span
+    const uint32_t *yperm = nullptr;
+    if (nCP) {
+        FARM_TRY(s->s[S_PERM_K].ensure(2 * nCP + 16));
+        FARM_TRY(s->s[S_PERM].ensure(8 * nCP + 16));
+        uint8_t *key = s->s[S_PERM_K].as<uint8_t>(), *key_s = key + nCP;
+        uint32_t *idx = s->s[S_PERM].as<uint32_t>(), *idx_s = idx + nCP;
+        k_cp_cost<<<gb(nCP), 256, 0, st>>>(R.hdr, cpstart, cpoly, cpcol, colpoly, nCP, key, idx);
+        L++;
+        FARM_TRY(sort_pairs(s, key, key_s, idx, idx_s, nCP, 8));
+        yperm = idx_s;
     }
 
     // ---- fill: cell clip per row
     FARM_TRY(s->s[S_CNT_E].ensure(4 * (nCP + 1) + 16));
     uint32_t *ycnt = s->s[S_CNT_E].as<uint32_t>();
     FARM_CUDA(cudaMemsetAsync(ycnt, 0, 4 * (nCP + 1), st));
-    FARM_TRY(s->s[S_PIXCNT].ensure(4 * (ch.npix + 1) + 16));
-    uint32_t *cellcnt = s->s[S_PIXCNT].as<uint32_t>();
-    FARM_CUDA(cudaMemsetAsync(cellcnt, 0, 4 * (ch.npix + 1), st));
     if (nCP) {
-        R.timer.time(T_CLIPY, st, [&] { k_clipy<<<gb(nCP), 256, 0, st>>>(R.hdr, colbase, ch, cpstart, cpoly, nCP, R.rowy, ycnt, nullptr, nullptr,
-                                         nullptr, nullptr); });
+        R.timer.time(T_CLIPY, st, [&] { k_clipy<<<gb(nCP), 256, 0, st>>>(R.hdr, ch, yperm, cpstart, cpoly, cpcol, colpoly, nCP, R.rowy, ycnt,
+                                         nullptr, nullptr, nullptr); });
         L++;
     }
     FARM_TRY(s->s[S_TMP_A].ensure(8 * (nCP + 1) + 16));
@@ -1738,17 +1847,17 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     uint64_t *ykb = s->s[S_VKEY].as<uint64_t>(), *yks = s->s[S_HKEY].as<uint64_t>();
     float2 *ypb = s->s[S_VVAL].as<float2>(), *yps = s->s[S_HVAL].as<float2>();
     if (nY) {
-        R.timer.time(T_CLIPY, st, [&] { k_clipy<<<gb(nCP), 256, 0, st>>>(R.hdr, colbase, ch, cpstart, cpoly, nCP, R.rowy, nullptr, yscan, ykb, ypb,
-                                         cellcnt); });
+        R.timer.time(T_CLIPY, st, [&] { k_clipy<<<gb(nCP), 256, 0, st>>>(R.hdr, ch, yperm, cpstart, cpoly, cpcol, colpoly, nCP, R.rowy,
+                                         nullptr, yscan, ykb, ypb); });
         L++;
         FARM_TRY(sort_pairs(s, ykb, yks, reinterpret_cast<uint64_t *>(ypb), reinterpret_cast<uint64_t *>(yps), nY,
                             key_bits(ch.npix)));
     }
-    FARM_TRY(s->s[S_TMP_A].ensure(8 * (ch.npix + 1) * 2 + 16));
-    uint64_t *c64 = s->s[S_TMP_A].as<uint64_t>(), *cellstart = c64 + (ch.npix + 1);
-    k_u32_to_u64<<<gb(ch.npix + 1), 256, 0, st>>>(cellcnt, ch.npix + 1, c64);
+    // cell starts (the points are sorted by cell)
+    FARM_TRY(s->s[S_TMP_A].ensure(8 * (ch.npix + 1) + 16));
+    uint64_t *cellstart = s->s[S_TMP_A].as<uint64_t>();
+    k_seg_starts<<<gb(nY + 1), 256, 0, st>>>(yks, nY, ch.npix, cellstart);
     L++;
-    FARM_TRY(excl_scan(s, c64, cellstart, ch.npix + 1));
     R.timer.time(T_CELLS, st, [&] { k_cells<<<gb(ch.npix), 256, 0, st>>>(R.hdr, pixbase, ch, cellstart, yps, cpstart, s->d_status.as<uint8_t>(),
                                          s->d_areas.as<double>(), R.cc); });
     L++;
@@ -1799,6 +1908,9 @@ int rasterize(farm_store *s, const farm_raster_opts *o, int *launches) {
     R.n1 = (uint64_t)np + 1;
     R.cc = o->category_count;
     R.doff = s->d_off.as<uint64_t>();
+    R.hoff.resize((size_t)np + 1);
+    FARM_CUDA(cudaMemcpyAsync(R.hoff.data(), R.doff, 8 * ((size_t)np + 1), cudaMemcpyDeviceToHost, st));
+    FARM_CUDA(cudaStreamSynchronize(st));
     const uint64_t n1 = R.n1;
     FARM_TRY(s->d_hdr.ensure(sizeof(PolyHdr) * np));
     FARM_TRY(s->s[S_SIZES].ensure(9 * n1 * 8));
@@ -1844,7 +1956,21 @@ int rasterize(farm_store *s, const farm_raster_opts *o, int *launches) {
         FARM_TRY(s->s[S_TMP_B].ensure(3 * 8 * n1 + 16));
         unsigned long long *tot3 = s->s[S_TMP_B].as<unsigned long long>();
         FARM_CUDA(cudaMemsetAsync(tot3, 0, 3 * 8 * n1, st));
-        R.timer.time(T_WALK, st, [&] { k_walk_tot<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, np, ne, tot3); });
+        for (uint64_t e0 = 0; e0 < ne; e0 += 1ull << 27) {
+            const uint64_t n = ne - e0 < (1ull << 27) ? ne - e0 : 1ull << 27;
+            // polygons whose edges meet [e0, e0 + n)
+            uint32_t pa = 0, pb = np;
+            {
+                const std::vector<uint64_t> &ho = R.hoff;
+                pa = (uint32_t)(std::upper_bound(ho.begin(), ho.end(), e0) - ho.begin() - 1);
+                pb = (uint32_t)(std::lower_bound(ho.begin(), ho.end(), e0 + n) - ho.begin());
+                if (pb > np) pb = np;
+            }
+            const uint32_t *perm = nullptr;
+            FARM_TRY(edge_order(R, pa, pb - pa, e0, n, &perm));
+            R.timer.time(T_WALK, st,
+                         [&] { k_walk_tot<<<gb(n), 256, 0, st>>>(sv, R.hdr, R.doff, np, e0, n, perm, tot3); });
+        }
         FARM_TRY(s->s[S_TMP_A].ensure(2 * 3 * 8 * n1 + 16));
         uint64_t *sz = s->s[S_TMP_A].as<uint64_t>(), *sc = sz + 3 * n1;
         k_tot_sizes<<<gb(n1), 256, 0, st>>>(tot3, R.hdr, np, sz);
@@ -1871,11 +1997,10 @@ int rasterize(farm_store *s, const farm_raster_opts *o, int *launches) {
     FARM_CUDA(cudaMemcpyAsync(hscan.data(), scan, 8 * 8 * n1, cudaMemcpyDeviceToHost, st));
     FARM_CUDA(cudaMemcpyAsync(hh.data(), R.hdr, sizeof(PolyHdr) * np, cudaMemcpyDeviceToHost, st));
     FARM_CUDA(cudaStreamSynchronize(st));
-    std::vector<uint64_t> hoff(np + 1);
-    FARM_CUDA(cudaMemcpy(hoff.data(), R.doff, 8 * (np + 1), cudaMemcpyDeviceToHost));
-    const uint64_t kChunkEdges = env_u64("FARM_CHUNK_EDGES", 1ull << 25);
-    const uint64_t kChunkCross = env_u64("FARM_CHUNK_CROSS", 1ull << 25);
-    const uint64_t kChunkPix = env_u64("FARM_CHUNK_PIX", 1ull << 26);
+    const std::vector<uint64_t> &hoff = R.hoff;
+    const uint64_t kChunkEdges = env_u64("FARM_CHUNK_EDGES", 1ull << 27);
+    const uint64_t kChunkCross = env_u64("FARM_CHUNK_CROSS", 1ull << 27);
+    const uint64_t kChunkPix = env_u64("FARM_CHUNK_PIX", 1ull << 27);
     uint32_t p = 0;
     while (p < np) {
         uint32_t q = p;
