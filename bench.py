@@ -250,6 +250,118 @@ def rooflines(rt: dict, qs: dict, n_pairs: int, stage: dict, steps: int) -> dict
     return {"dominant": dom, "stages": st}
 
 
+def choose_band(prob: np.ndarray, y: np.ndarray, budget: float, positives: int = 0) -> tuple:
+    """Narrowest band (lo, hi) whose decided pairs stay within the error
+    budget on held-out pairs: at most budget x positives false positives above
+    hi and at most budget x positives false negatives below lo (positives: of
+    the whole held-out set, default those of y). Pairs strictly inside
+    (lo, hi) are refined exactly and cost no accuracy."""
+    pos = max(int(positives or y.sum()), 1)
+    allow = int(budget * pos)
+    o = np.argsort(-prob, kind="stable")  # descending
+    fp = np.cumsum(y[o] == 0)
+    k = int(np.searchsorted(fp, allow, side="right"))  # first k decided-1 pairs hold <= allow negatives
+    hi = float(prob[o[k - 1]]) if k > 0 else 1.01
+    o2 = np.argsort(prob, kind="stable")  # ascending
+    fn = np.cumsum(y[o2] == 1)
+    k2 = int(np.searchsorted(fn, allow, side="right"))
+    lo = float(prob[o2[k2 - 1]]) if k2 > 0 else -0.01
+    if lo >= hi:  # never let the two decided sets overlap
+        lo = min(lo, hi - 1e-6)
+    # ties at the thresholds: decide only strictly beyond them
+    return np.nextafter(np.float32(lo), np.float32(-1)).item(), np.nextafter(np.float32(hi), np.float32(2)).item()
+
+
+def train_scorer(args, store, dev) -> dict:
+    """Train the learned scorer on pairs of a strip drawn with a separate seed,
+    labelled by the exact path, and set its band from held-out pairs."""
+    import torch
+    Wt = build_workload(args.seed + 1000, 0, args.strips, args.vpr)
+    so, sx, to, tx = (t.to(dev) for t in Wt["pinned"])
+    pairs = Wt["pairs"]
+    store.load(0, so, sx)
+    store.load(1, to, tx)
+    store.rasterize(vpr=args.vpr, category_count=16, strict=False)
+    from farm_gb300.engine import MODE_FILTER
+    dp = torch.from_numpy(pairs.view(np.int32)).to(dev).view(len(pairs), 2)
+    lab, _ = store.intersect(dp)
+    code, _ = store.intersect(dp, mode=MODE_FILTER)  # the scorer only sees pairs the filter leaves (3)
+    keep = torch.nonzero(lab != 2).flatten()
+    g = torch.Generator(device="cpu").manual_seed(args.seed + 1001)
+    keep = keep[torch.randperm(len(keep), generator=g).to(dev)][: args.learned_pairs]
+    nv = max(len(keep) // 10, 1)
+    val, tr = keep[:nv], keep[nv:]
+    tr = tr[code[tr] == 3]
+    pos_val = int((lab[val] == 1).sum())
+    val = val[code[val] == 3]
+    t0 = time.perf_counter()
+    loss = store.mlp_train(dp[tr].contiguous(), lab[tr].contiguous(), epochs=args.learned_epochs, batch=4096,
+                           lr=2e-3, seed=args.seed)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    prob = store.mlp_predict(dp[val].contiguous()).cpu().numpy()
+    y = lab[val].cpu().numpy().astype(np.int64)
+    lo, hi = choose_band(prob, y, args.learned_budget, pos_val)
+    store.mlp_band(lo, hi)
+    inband = float(((prob > lo) & (prob < hi)).mean()) if len(prob) else 0.0
+    log(f"scorer trained on {len(tr)} pairs in {train_s:.1f}s (loss {loss:.4f}); band ({lo:.4f}, {hi:.4f}) "
+        f"from {len(val)} held-out pairs, {inband:.3f} of them inside it")
+    del so, sx, to, tx, dp, lab, code
+    torch.cuda.empty_cache()
+    return {"train_pairs": int(len(tr)), "heldout_pairs": int(len(val)), "epochs": args.learned_epochs,
+            "heldout_inside_band": inband,
+            "train_s": train_s, "final_loss": loss, "band": [lo, hi], "error_budget": args.learned_budget,
+            "seed": args.seed + 1000}
+
+
+def pr(out, ref):
+    """Precision and recall of out against the exact results (pairs the exact
+    path marks 2, unrasterizable, are left out)."""
+    ok = ref != 2
+    o, r = out[ok] == 1, ref[ok] == 1
+    tp = int((o & r).sum())
+    fp = int((o & ~r).sum())
+    fn = int((~o & r).sum())
+    return (tp / max(tp + fp, 1), tp / max(tp + fn, 1))
+
+
+def learned_eval(store, d_pairs, exact_out, exact_query_ms: float, raster_ms: float, reps: int) -> dict:
+    """Learned mode and the -a heuristic on the step's pairs, against exact."""
+    import torch
+    from farm_gb300.engine import MODE_APPROX, MODE_LEARNED
+    res = {}
+    for name, mode in (("learned", MODE_LEARNED), ("heuristic", MODE_APPROX)):
+        out = torch.empty_like(exact_out)
+        store.intersect(d_pairs, mode=mode, out=out)  # warm-up
+        ms = 0.0
+        st = {}
+        for _ in range(reps):
+            store.intersect(d_pairs, mode=mode, out=out)
+            st = store.last_stats
+            ms += st["ms_total"] if mode == MODE_APPROX else 0.0
+        abst = st.get("fp64_rechecks", 0)
+        if mode == MODE_LEARNED:  # timed around the whole call (predict + band + exact refinement)
+            torch.cuda.synchronize()
+            store.event_record(4)
+            for _ in range(reps):
+                store.intersect(d_pairs, mode=mode, out=out)
+            store.event_record(5)
+            ms = store.event_elapsed(4, 5)
+        ms /= reps
+        p, r = pr(out.cpu().numpy(), exact_out.cpu().numpy())
+        n = d_pairs.shape[0]
+        res[name] = {"precision": p, "recall": r, "query_ms": ms, "query_pairs_per_s": n / (ms * 1e-3),
+                     "speedup_vs_exact_query": exact_query_ms / ms,
+                     "step_pairs_per_s": n / ((raster_ms + ms) * 1e-3),
+                     "speedup_vs_exact_step": (raster_ms + exact_query_ms) / (raster_ms + ms)}
+        if mode == MODE_LEARNED:
+            res[name]["filter_decided_pairs"] = int(n - st.get("border_pairs", 0))
+            res[name]["scored_pairs"] = int(st.get("border_pairs", 0))
+            res[name]["abstained_pairs"] = int(abst)
+            res[name]["abstained_frac"] = abst / n
+    return res
+
+
 def run_ours(args) -> dict:
     import torch
     import torch.distributed as dist
@@ -262,16 +374,17 @@ def run_ours(args) -> dict:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from farm_gb300.engine import Store
 
+    dev = torch.device("cuda", local)
+    store = Store()
+    learned_train = train_scorer(args, store, dev) if args.learned else None
     W = build_workload(args.seed, rank % args.strips, args.strips, args.vpr)
     S, T, pairs = W["S"], W["T"], W["pairs"]
     S_off_t, S_xy_t, T_off_t, T_xy_t = W["pinned"]
-    dev = torch.device("cuda", local)
     d = {k: v.to(dev) for k, v in (("so", S_off_t), ("sx", S_xy_t), ("to", T_off_t), ("tx", T_xy_t))}
     d_pairs = torch.from_numpy(pairs.view(np.int32)).to(dev)
     d_out = torch.empty(len(pairs), dtype=torch.uint8, device=dev)
     h_out = torch.empty(len(pairs), dtype=torch.uint8).pin_memory()
     h_pairs = torch.from_numpy(pairs.view(np.int32)).pin_memory()
-    store = Store()
 
     stage = {"load_ms": 0.0, "raster_ms": 0.0, "query_ms": 0.0}
 
@@ -364,6 +477,13 @@ def run_ours(args) -> dict:
         "stage_ms": {"load": stage["load_ms"] / args.steps, "raster": stage["raster_ms"] / args.steps,
                      "filter_refine": stage["query_ms"] / args.steps, "step": ms / args.steps},
     }
+    if learned_train is not None and rank == 0:
+        lr_ = learned_eval(store, d_pairs.view(len(pairs), 2), d_out, stage["query_ms"] / args.steps,
+                           stage["raster_ms"] / args.steps, reps=3)
+        lr_["train"] = learned_train
+        lr_["note"] = ("query = stages b-c on the rasterized strip (learned: predict + band + exact refinement of "
+                       "abstentions); step adds the strip's rasterization, which both modes need")
+        result["learned"] = lr_
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(W, args, budget_s=args.cpu_seconds, threads=1, gpu_out=h_out.numpy())
     store.close()
@@ -485,6 +605,12 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--ref-step-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", dest="learned", action="store_false",
+                    help="skip training and evaluating the learned scorer")
+    ap.add_argument("--learned-pairs", type=int, default=2_000_000, help="training + held-out pairs")
+    ap.add_argument("--learned-epochs", type=int, default=12)
+    ap.add_argument("--learned-budget", type=float, default=5e-4,
+                    help="false positives (negatives) allowed above (below) the band, per positive")
     args = ap.parse_args()
     res = run_reference(args) if args.impl == "reference" else run_ours(args)
     if res is not None:

@@ -174,7 +174,6 @@ __device__ bool refine_pixel_pair(const StoreView &sv, const PolyHdr &S, const P
                     tbuf[lane] = c;
                     __syncwarp();
                     const int m = (int)min(32u, total2 - tb);
-                    const int sxp0 = sxp;
                     const float2 cp0 = cp;
                     const bool pseg0 = pseg;
                     bool coll = false;
@@ -196,7 +195,6 @@ __device__ bool refine_pixel_pair(const StoreView &sv, const PolyHdr &S, const P
                         pseg = (segmask >> j) & 1u;
                     }
                     if (__any_sync(0xffffffffu, coll && valid)) {
-                        int sp = sxp0;
                         float2 cq = cp0;
                         bool ps = pseg0;
                         for (int j = 0; j < m; j++) {
@@ -209,11 +207,9 @@ __device__ bool refine_pixel_pair(const StoreView &sv, const PolyHdr &S, const P
                                 if ((sya | syb) == 0)
                                     hit |= inter1f(a.x, b.x, cq.x, cc.x) && inter1f(a.y, b.y, cq.y, cc.y);
                             }
-                            sp = sxn;
                             cq = cc;
                             ps = (segmask >> j) & 1u;
                         }
-                        (void)sp;
                     }
                     if (valid) tests += nseg;
                     if (__any_sync(0xffffffffu, hit && valid)) return true;
@@ -224,6 +220,23 @@ __device__ bool refine_pixel_pair(const StoreView &sv, const PolyHdr &S, const P
     return false;
 }
 
+// (decodePixelArea(low) + decodePixelArea(high)) / 2 of a fill class
+// (Ideal.cpp:47-62), as the reference's -a heuristic averages them
+__device__ __forceinline__ double apx_area(uint8_t f, double pa, int cc) {
+    if (f == 0) return 0.0;
+    if (f == cc - 1) return (pa + pa) / 2;
+    return ((1.0 * f - 1) / (cc - 2) * pa + (1.0 * f - 0) / (cc - 2) * pa) / 2;
+}
+
+// kMode: K_EXACT refines; K_APPROX is the reference's -a heuristic
+// (kernel_calculate_probability, query_intersect.cu:100-134) instead of
+// refinement — a BORDER x BORDER pixel pair decides "true" when
+// (apx_s + apx_t) / max(pixel areas) > 1, and a pair with no IN overlap and no
+// such pixel pair is "false"; K_FILTER runs the filter alone and writes 1 (an
+// IN overlap: exact "true"), 0 (no non-OUT pixel pair at all: exact "false")
+// or 3 (BORDER x BORDER pixel pairs to refine), the learned mode's first stage.
+enum { K_EXACT = 0, K_APPROX = 1, K_FILTER = 2 };
+template <int kMode>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     k_intersect(const StoreView sv, PairView pv, unsigned long long *__restrict__ next, uint8_t *__restrict__ out,
                 IxCounters *__restrict__ ctr) {
@@ -250,7 +263,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         Window w = retrieve(S.mbr, S.step_x, S.step_y, S.dimx, S.dimy, T.mbr[0], T.mbr[1], T.mbr[2], T.mbr[3]);
         const int wh = w.ey - w.sy + 1;
         const long nw = (long)(w.ex - w.sx + 1) * wh;
-        bool decided = false;
+        bool decided = false, has_bb = false;
         int qn = 0;  // warp-uniform queue fill
         auto flush = [&]() {
             // the warp refines the queued pixel pairs one after another and
@@ -322,10 +335,17 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
                     pb = (uint32_t)(v * T.dimx + u);
                     int pb_st = show_status(tst[pb], cc);
                     if (pb_st != 0) {
-                        if (o_st == 2 || pb_st == 2)
+                        if (o_st == 2 || pb_st == 2) {
                             in_hit = true;
-                        else
+                        } else if (kMode == K_APPROX) {
+                            const double spa = S.step_x * S.step_y, tpa = T.step_x * T.step_y;
+                            const double prob = (apx_area(sst[o_pa], spa, cc) + apx_area(tst[pb], tpa, cc)) /
+                                                (spa > tpa ? spa : tpa);
+                            in_hit = prob > 1.0;
                             bb = true;
+                        } else {
+                            bb = true;
+                        }
                     }
                 }
                 if (__any_sync(0xffffffffu, in_hit)) {
@@ -334,6 +354,11 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
                     break;
                 }
                 unsigned m = __ballot_sync(0xffffffffu, bb);
+                if (kMode != K_EXACT) {  // nothing to refine
+                    if (lane == 0) my_bb += __popc(m);
+                    has_bb |= m != 0;
+                    m = 0;
+                }
                 if (m) {
                     int nb = __popc(m);
                     if (qn + nb > kQueue) {
@@ -355,7 +380,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
             decided = flush();
         }
         if (lane == 0) {
-            if (out) out[pid] = decided ? 1 : 0;
+            if (out) out[pid] = decided ? 1 : (kMode == K_FILTER && has_bb ? 3 : 0);
             my_found += decided;
         }
         __syncwarp();
@@ -374,6 +399,25 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 
 int intersect_learned(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, uint8_t *out, uint64_t *found,
                       farm_stats *st);
+
+// The filter alone over n device pairs: out[k] = 1 / 0 / 3 (K_FILTER). Counts
+// IN-decided pairs into *in_hits.
+int intersect_filter(farm_store *s, const uint32_t *dpairs, uint64_t n, uint8_t *dout, uint64_t *in_hits) {
+    cudaStream_t stream = s->stream;
+    FARM_TRY(s->d_counters.ensure(256));
+    unsigned long long *next = s->d_counters.as<unsigned long long>() + 8;
+    IxCounters *ctr = reinterpret_cast<IxCounters *>(next + 1);
+    FARM_CUDA(cudaMemsetAsync(next, 0, 8 + sizeof(IxCounters), stream));
+    PairView pv{dpairs, n, s->n_side[0]};
+    k_intersect<K_FILTER><<<sm_count() * 8, kWarpsPerBlock * 32, 0, stream>>>(s->view(), pv, next, dout, ctr);
+    s->launches++;
+    FARM_CUDA(cudaGetLastError());
+    IxCounters h{};
+    FARM_CUDA(cudaMemcpyAsync(&h, ctr, sizeof h, cudaMemcpyDeviceToHost, stream));
+    FARM_CUDA(cudaStreamSynchronize(stream));
+    if (in_hits) *in_hits = h.in_hits;
+    return FARM_OK;
+}
 
 int intersect(farm_store *s, const uint32_t *pairs, uint64_t n, int mode, int mem, uint8_t *out, uint64_t *found,
               farm_stats *st) {
@@ -406,7 +450,10 @@ int intersect(farm_store *s, const uint32_t *pairs, uint64_t n, int mode, int me
     StoreView sv = s->view();
     FARM_CUDA(cudaEventRecord(s->ev[6], stream));
     int blocks = sm_count() * 8;
-    k_intersect<<<blocks, kWarpsPerBlock * 32, 0, stream>>>(sv, pv, next, dout, ctr);
+    if (mode == FARM_MODE_APPROX)
+        k_intersect<K_APPROX><<<blocks, kWarpsPerBlock * 32, 0, stream>>>(sv, pv, next, dout, ctr);
+    else
+        k_intersect<K_EXACT><<<blocks, kWarpsPerBlock * 32, 0, stream>>>(sv, pv, next, dout, ctr);
     s->launches++;
     FARM_CUDA(cudaGetLastError());
     FARM_CUDA(cudaEventRecord(s->ev[7], stream));
@@ -430,7 +477,6 @@ int intersect(farm_store *s, const uint32_t *pairs, uint64_t n, int mode, int me
         st->ms_stage[1] = ms;
         st->kernel_launches = 1;
     }
-    (void)mode;
     return FARM_OK;
 }
 
@@ -443,7 +489,31 @@ extern "C" int farm_intersect(farm_store *s, const uint32_t *pairs, uint64_t n, 
         set_error("invalid arguments to farm_intersect");
         return FARM_EINVAL;
     }
-    if (mode != FARM_MODE_EXACT) return intersect_learned(s, pairs, n, mem, out, found, st);
+    if (mode == FARM_MODE_LEARNED) return intersect_learned(s, pairs, n, mem, out, found, st);
+    if (mode == FARM_MODE_FILTER) {
+        if (!s->rasterized) {
+            set_error("farm_intersect: rasterize first");
+            return FARM_EINVAL;
+        }
+        if (mem != FARM_MEM_DEVICE || (n && !out)) {
+            set_error("farm_intersect: FARM_MODE_FILTER takes device pairs and a device output");
+            return FARM_EINVAL;
+        }
+        uint64_t in_hits = 0;
+        FARM_TRY(intersect_filter(s, pairs, n, out, &in_hits));
+        if (found) *found = in_hits;
+        if (st) {
+            memset(st, 0, sizeof *st);
+            st->pairs = n;
+            st->found = in_hits;
+            st->in_hits = in_hits;
+        }
+        return FARM_OK;
+    }
+    if (mode != FARM_MODE_EXACT && mode != FARM_MODE_APPROX) {
+        set_error("farm_intersect: unknown mode");
+        return FARM_EINVAL;
+    }
     return intersect(s, pairs, n, mode, mem, out, found, st);
 }
 
@@ -524,7 +594,7 @@ extern "C" int farm_intersect_static(farm_store *s, const uint32_t *pairs, uint6
         if (e == cudaSuccess && n) e = cudaMemcpyAsync(dpairs, pairs, 8 * n, cudaMemcpyHostToDevice, stream);
         if (e == cudaSuccess && n) {
             PairView pv{dpairs, n, s->n_side[0]};
-            k_intersect<<<sm_count() * 8, kWarpsPerBlock * 32, 0, stream>>>(s->view(), pv, next, dout, ctr);
+            k_intersect<K_EXACT><<<sm_count() * 8, kWarpsPerBlock * 32, 0, stream>>>(s->view(), pv, next, dout, ctr);
             e = cudaGetLastError();
             if (e == cudaSuccess) s->launches++;
         }

@@ -29,7 +29,9 @@ from ._gpu_sig import RasterOpts, RasterTotals, RasterView, Stats
 from ._native import check_gpu, gpu
 
 MODE_EXACT = 0
+MODE_APPROX = 1
 MODE_LEARNED = 2
+MODE_FILTER = 3
 MEM_HOST = 0
 MEM_DEVICE = 1
 

@@ -45,7 +45,10 @@ typedef struct farm_store farm_store;
 
 /* Query modes for farm_intersect. */
 #define FARM_MODE_EXACT 0   /* the reference's decision procedure, bit-exact */
+#define FARM_MODE_APPROX 1  /* the reference's -a fill-ratio heuristic (query_intersect.cu:100-134), no refinement */
 #define FARM_MODE_LEARNED 2 /* MLP scorer; abstentions refined exactly */
+#define FARM_MODE_FILTER 3  /* the exact filter alone (device memory only): 1 = an IN overlap decides true,
+                               0 = no non-OUT pixel pair (false), 3 = BORDER x BORDER pixel pairs to refine */
 
 /* Pointer locations for pair lists and result buffers. */
 #define FARM_MEM_HOST 0

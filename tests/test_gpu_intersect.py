@@ -125,3 +125,22 @@ def test_gpu_intersect_lattice_collinear(gpu_lib):
         exp = np.array([O.intersect(RS[pairs[i][0]], RT[pairs[i][1]]) for i in ok], np.uint8)
         assert np.array_equal(out[ok], exp), (vpr, int((out[ok] != exp).sum()))
         assert len(ok) > len(pairs) // 2
+
+
+@pytest.mark.parametrize("vpr,seed", [(10, 41), (4, 42), (32, 43)])
+def test_gpu_intersect_approx_heuristic_matches_oracle(gpu_lib, vpr, seed):
+    # FARM_MODE_APPROX is the reference's -a fill-ratio heuristic: no
+    # refinement, decided by IN overlaps and (apx_s + apx_t) / max area > 1
+    from farm_gb300.engine import MODE_APPROX
+    prm = P.StarParams(dom_hi=25.0, n_hi=1500)
+    S, T = P.generate(prm, seed, 150), P.generate(prm, seed + 100, 500)
+    pairs = P.mbr_join(S.mbrs(), T.mbrs())
+    st = Store()
+    st.load_sets(S, T)
+    st.rasterize(vpr=vpr)
+    out, found = st.intersect(np.ascontiguousarray(pairs, dtype=np.uint32), mode=MODE_APPROX)
+    st.close()
+    RS, RT = O.rasterize_set(S, vpr), O.rasterize_set(T, vpr)
+    exp = np.array([O.intersect_heuristic(RS[s], RT[t]) for s, t in pairs], np.uint8)
+    assert np.array_equal(out, exp), f"{int((out != exp).sum())} of {len(exp)} differ"
+    assert found == int(exp.sum())

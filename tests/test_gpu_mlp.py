@@ -134,10 +134,21 @@ def test_learned_mode_beats_the_reference_heuristic(gpu_lib):
     acc_l = (learned == truth).mean()
     acc_h = (heur == truth).mean()
     assert acc_l > acc_h, (acc_l, acc_h)
-    # learned mode with a band: confident decisions + exact refinement of the rest
+    # learned mode with a band: the exact filter decides what it can, the
+    # scorer decides its confident pairs among the rest, and the band's pairs
+    # are refined exactly
+    from farm_gb300.engine import MODE_FILTER
+    dte = torch.from_numpy(np.ascontiguousarray(pairs[te]).view(np.int32)).cuda().view(-1, 2)
+    code, _ = st.intersect(dte, mode=MODE_FILTER)
+    code = code.cpu().numpy()
+    assert set(np.unique(code)) <= {0, 1, 3}
+    decided = code != 3
+    assert np.array_equal(code[decided], truth[decided])
     st.mlp_band(0.05, 0.95)
     out, found = st.intersect(np.ascontiguousarray(pairs[te]), mode=MODE_LEARNED)
-    refined = (prob > 0.05) & (prob < 0.95)
+    refined = (code == 3) & (prob > 0.05) & (prob < 0.95)
+    assert np.array_equal(out[decided], truth[decided])
     assert np.array_equal(out[refined], truth[refined])
     assert st.last_stats["fp64_rechecks"] == int(refined.sum())
+    assert st.last_stats["border_pairs"] == int((code == 3).sum())
     st.close()
