@@ -119,6 +119,12 @@ def build_query_exe() -> Path:
     if not _newer(out, deps + [LIB / "libfarm_gpu.so", LIB / "libfarm_host.so"]):
         _run(["g++", *HOST_FLAGS, "-o", str(out), str(src), f"-L{LIB}", "-lfarm_gpu", "-lfarm_host",
               f"-Wl,-rpath,$ORIGIN", "-I", str(ROOT / "include")])
+    # the reference's program names, dispatched on by the binary
+    for name in ("intersect", "within_polygon", "intersection"):
+        link = LIB / name
+        if link.is_symlink() or link.exists():
+            link.unlink()
+        link.symlink_to(out.name)
     return out
 
 

@@ -66,6 +66,7 @@ enum Scratch {
     S_PERM,
     S_CPCOL,    // column of each column-polygon point
     S_COLPOLY,  // polygon of each fill column
+    S_ECNT16,   // per-edge walk counts from phase 1 (u16 x 3), reused by phase 2
 };
 
 // ------------------------------------------------------------ headers ----
@@ -535,11 +536,17 @@ __device__ inline bool in_rngf(float lo, float hi, float v) { return !(v < lo ||
 // pi, pi1 are the float points (Xi, yi), (Xi1, yi1) on the column lines, yi and
 // yi1 the edge's ordinates there (ClipXEdge).
 // Returns the count; writes up to 4 points when out != nullptr.
-__device__ inline int clip_x_points(float2 A, float2 B, double Xi, double Xi1, float2 pi, float2 pi1, float2 *out) {
+// emitA: false for every edge but the ring's first. Edge i's A is edge
+// i-1's B (the same vertex), which edge i-1 emits last into the same column
+// under the same range test, so A would follow its own bit-identical copy in
+// the column's stream — a point the dedup rule always drops (a later copy of
+// a kept point, or of a point dropped for equalling a kept one).
+__device__ inline int clip_x_points(float2 A, float2 B, double Xi, double Xi1, float2 pi, float2 pi1, bool emitA,
+                                    float2 *out) {
     int n = 0;
     const float mny = A.y < B.y ? A.y : B.y, mxy = A.y < B.y ? B.y : A.y;
     const float mnx = A.x < B.x ? A.x : B.x, mxx = A.x < B.x ? B.x : A.x;
-    if (in_rng(Xi, Xi1, A.x)) {
+    if (emitA && in_rng(Xi, Xi1, A.x)) {
         if (out) out[n] = A;
         n++;
     }
@@ -710,15 +717,19 @@ __global__ void k_edge_cost(const StoreView sv, const PolyHdr *__restrict__ hdr,
     }
 }
 
+// Phase 1's walk: per-polygon totals, and each edge's counts kept (u16, for
+// phase 2's chunks, which would otherwise walk every edge a second time only
+// to count); a count above 65535 sets *ovf and phase 2 counts by walking.
 __global__ void k_walk_tot(const StoreView sv, PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off,
                            uint32_t npoly, uint64_t e0, uint64_t nedges, const uint32_t *__restrict__ perm,
-                           unsigned long long *__restrict__ tot) {
+                           unsigned long long *__restrict__ tot, uint16_t *__restrict__ c16, uint64_t ne_all,
+                           int *__restrict__ ovf) {
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nedges;
          k += (uint64_t)gridDim.x * blockDim.x) {
         uint64_t e = e0 + perm[k];
         uint32_t p = find_segment(off, npoly, e);
         const PolyHdr &h = hdr[p];
-        if (h.err) continue;
+        if (h.err) continue;  // phase 2 zeroes the counts of failed polygons
         uint32_t i = (uint32_t)(e - h.edge);
         const float2 *r = sv.ring + h.ring;
         CountSink s;
@@ -727,6 +738,10 @@ __global__ void k_walk_tot(const StoreView sv, PolyHdr *__restrict__ hdr, const 
         s.dimy = h.dimy;
         walk_edge(h, r[i], r[i + 1], s);
         if (s.bad) atomicMin(&hdr[p].err, FARM_EASSERT);
+        if (s.nc > 0xFFFFu || s.nh > 0xFFFFu || s.nv > 0xFFFFu) atomicOr(ovf, 1);
+        c16[e] = (uint16_t)s.nc;
+        c16[ne_all + e] = (uint16_t)s.nh;
+        c16[2 * ne_all + e] = (uint16_t)s.nv;
         if (s.nc) atomicAdd(&tot[3ull * p], (unsigned long long)s.nc);
         if (s.nh) atomicAdd(&tot[3ull * p + 1], (unsigned long long)s.nh);
         if (s.nv) atomicAdd(&tot[3ull * p + 2], (unsigned long long)s.nv);
@@ -784,6 +799,22 @@ __global__ void k_walk_count(const StoreView sv, PolyHdr *__restrict__ hdr, cons
         cnt[k] = s.nc;
         cnt[n1 + k] = s.nh;
         cnt[2 * n1 + k] = s.nv;
+    }
+}
+
+// Phase 2's counts from phase 1's (the same walk, the same sink), zero for
+// polygons whose rasterization failed — what k_walk_count would produce.
+__global__ void k_load_counts(const PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off, Chunk ch,
+                              const uint16_t *__restrict__ c16, uint64_t ne_all, uint32_t *__restrict__ cnt) {
+    uint64_t n1 = ch.ne + 1;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < ch.ne;
+         k += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t e = ch.e0 + k;
+        uint32_t p = ch.p0 + find_segment(off + ch.p0, ch.np, e);
+        const bool ok = hdr[p].err == 0;
+        cnt[k] = ok ? c16[e] : 0u;
+        cnt[n1 + k] = ok ? c16[ne_all + e] : 0u;
+        cnt[2 * n1 + k] = ok ? c16[2 * ne_all + e] : 0u;
     }
 }
 
@@ -1011,7 +1042,7 @@ __global__ void k_clipx(const StoreView sv, const PolyHdr *__restrict__ hdr, con
         for (; c < h.ncols && Xi <= mxx + mg; c++) {
             const double Xi1 = Xi + h.step_x;  // == lines[c + 1]
             const float2 pi1 = mk(Xi1, E.ord(Xi1));
-            int m = clip_x_points(A, B, Xi, Xi1, pi, pi1, okey ? buf : nullptr);
+            int m = clip_x_points(A, B, Xi, Xi1, pi, pi1, i == 0, okey ? buf : nullptr);
             if (okey) {
                 for (int q = 0; q < m; q++) {
                     okey[at] = (h.col - ch.col0) + (uint64_t)c;
@@ -1525,6 +1556,7 @@ struct RasterCtx {
     int launches = 0;
     KTimer timer;
     std::vector<uint64_t> hoff;  // per-polygon first edge (host copy of doff)
+    bool counts_kept = false;    // phase 1's per-edge counts are valid for phase 2
 };
 
 // Edges [e0, e0 + ne) of polygons [p0, p0 + np) in walk order (k_edge_cost).
@@ -1560,7 +1592,11 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     FARM_CUDA(cudaMemsetAsync(ecnt, 0, 3 * ne1 * 4, st));
     const uint32_t *perm = nullptr;
     FARM_TRY(edge_order(R, ch.p0, ch.np, ch.e0, ne, &perm));
-    R.timer.time(T_WALK, st, [&] { k_walk_count<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, perm, ecnt); });
+    if (R.counts_kept) {
+        k_load_counts<<<gb(ne), 256, 0, st>>>(R.hdr, R.doff, ch, s->s[S_ECNT16].as<uint16_t>(), s->n_edges, ecnt);
+    } else {
+        R.timer.time(T_WALK, st, [&] { k_walk_count<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, perm, ecnt); });
+    }
     uint64_t *ecnt64 = s->s[S_TMP_A].as<uint64_t>(), *escan = s->s[S_SCAN_E].as<uint64_t>();
     k_u32_to_u64<<<gb(3 * ne1), 256, 0, st>>>(ecnt, 3 * ne1, ecnt64);
     L += 2;
@@ -1956,6 +1992,11 @@ int rasterize(farm_store *s, const farm_raster_opts *o, int *launches) {
         FARM_TRY(s->s[S_TMP_B].ensure(3 * 8 * n1 + 16));
         unsigned long long *tot3 = s->s[S_TMP_B].as<unsigned long long>();
         FARM_CUDA(cudaMemsetAsync(tot3, 0, 3 * 8 * n1, st));
+        FARM_TRY(s->s[S_ECNT16].ensure(3 * 2 * ne + 64));
+        uint16_t *c16 = s->s[S_ECNT16].as<uint16_t>();
+        FARM_TRY(s->d_counters.ensure(256));
+        int *ovf = reinterpret_cast<int *>(s->d_counters.as<unsigned long long>() + 30);
+        FARM_CUDA(cudaMemsetAsync(ovf, 0, 4, st));
         for (uint64_t e0 = 0; e0 < ne; e0 += 1ull << 27) {
             const uint64_t n = ne - e0 < (1ull << 27) ? ne - e0 : 1ull << 27;
             // polygons whose edges meet [e0, e0 + n)
@@ -1969,8 +2010,12 @@ int rasterize(farm_store *s, const farm_raster_opts *o, int *launches) {
             const uint32_t *perm = nullptr;
             FARM_TRY(edge_order(R, pa, pb - pa, e0, n, &perm));
             R.timer.time(T_WALK, st,
-                         [&] { k_walk_tot<<<gb(n), 256, 0, st>>>(sv, R.hdr, R.doff, np, e0, n, perm, tot3); });
+                         [&] { k_walk_tot<<<gb(n), 256, 0, st>>>(sv, R.hdr, R.doff, np, e0, n, perm, tot3,
+                                                                   c16, ne, ovf); });
         }
+        int h_ovf = 1;
+        FARM_TRY(d2h(s, &h_ovf, ovf, 4));
+        R.counts_kept = h_ovf == 0;
         FARM_TRY(s->s[S_TMP_A].ensure(2 * 3 * 8 * n1 + 16));
         uint64_t *sz = s->s[S_TMP_A].as<uint64_t>(), *sc = sz + 3 * n1;
         k_tot_sizes<<<gb(n1), 256, 0, st>>>(tot3, R.hdr, np, sz);

@@ -30,3 +30,21 @@ def test_gpu_library_loads_and_exports(host_built):
     assert "farm_intersect" in names and "farm_rasterize" in names
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
+
+
+def test_query_program_flags_without_gpu(host_built):
+    """The drop-in programs parse the reference's flags: --help lists them and
+    an unknown flag prints the reference's message (no GPU needed)."""
+    import subprocess
+    from pathlib import Path
+    lib = Path(__file__).resolve().parents[1] / "farm_gb300" / "lib"
+    exe = lib / "intersect"
+    if not exe.exists():
+        pytest.skip("query program not built")
+    h = subprocess.run([str(exe), "--help"], capture_output=True, text=True, timeout=60)
+    assert h.returncode == 0
+    for flag in ("--rasterize", "--gpu", "--approximation", "--hierachy", "--source", "--target", "--threads",
+                 "--vpr", "--batch_size", "--merge_threshold", "--within_distance", "--category_count"):
+        assert flag in h.stderr, flag
+    u = subprocess.run([str(exe), "--bogus"], capture_output=True, text=True, timeout=60)
+    assert "Undefined Option!" in u.stdout

@@ -1,0 +1,47 @@
+"""The drop-in query programs (intersect, within_polygon) print the reference's
+count-found on the golden .dt fixtures."""
+import re
+import subprocess
+from pathlib import Path
+
+import pytest
+
+from fixtures import GOLDEN, manifest, pair_case
+
+pytestmark = pytest.mark.gpu
+LIB = Path(__file__).resolve().parents[1] / "farm_gb300" / "lib"
+M = manifest()
+
+
+@pytest.fixture(scope="module", autouse=True)
+def query_built(gpu_lib):
+    from farm_gb300 import build
+    build.build_query_exe()
+
+
+def run(prog, *args):
+    p = subprocess.run([str(LIB / prog), *args], capture_output=True, text=True, timeout=600)
+    assert p.returncode == 0, p.stderr
+    m = re.search(r"count-found:\t(\d+)", p.stderr)
+    assert m, p.stderr
+    return int(m.group(1))
+
+
+@pytest.mark.parametrize("case", M["pairs"], ids=[c["name"] for c in M["pairs"]])
+def test_query_program_count_matches_reference(gpu_lib, case):
+    _, _, ref = pair_case(case)
+    expected = int((ref[:, 2] == 1).sum())
+    s = str(GOLDEN / f"{case['name']}_S.dt")
+    if case["mode"] == "intersect":
+        got = run("intersect", "-s", s, "-t", str(GOLDEN / f"{case['name']}_T.dt"), "-r", "-g", "-v",
+                  str(case["vpr"]))
+    else:
+        got = run("within_polygon", "-s", s, "-r", "-h", "-g", "-v", str(case["vpr"]))
+    assert got == expected
+
+
+def test_query_program_batches_add_up(gpu_lib):
+    case = next(c for c in M["pairs"] if c["mode"] == "intersect")
+    s, t = str(GOLDEN / f"{case['name']}_S.dt"), str(GOLDEN / f"{case['name']}_T.dt")
+    whole = run("intersect", "-s", s, "-t", t, "-r", "-g", "-v", str(case["vpr"]))
+    assert run("intersect", "-s", s, "-t", t, "-r", "-g", "-v", str(case["vpr"]), "-b", "37") == whole
