@@ -192,7 +192,7 @@ def rooflines(rt: dict, qs: dict, n_pairs: int, stage: dict, steps: int) -> dict
     """Roofline of each measured stage from its algorithmic work per unit
     (counts of the last step; times are the per-step means of the timed steps).
 
-    edge walk (3 launches: totals, count, fill): FP64, 16 flops per edge
+    edge walk (2 launches per edge: totals + counts, then fill): FP64, 16 flops per edge
       (endpoint cells, slope and intercept) + 16 per pixel-boundary crossing
       (both branches of one walk step), the reference's arithmetic for ONE walk;
     cell clip (count + emit): FP64, 4 flops per emitted clip point (slope and
@@ -242,7 +242,7 @@ def rooflines(rt: dict, qs: dict, n_pairs: int, stage: dict, steps: int) -> dict
     cand = {k: v for k, v in st.items() if k in ("edge_walk", "cell_clip", "column_clip", "cell_area", "refine")}
     name = max(cand, key=lambda k: cand[k]["kernel_ms"] or 0.0)
     dom = dict(cand[name])
-    dom["kernel"] = {"edge_walk": "k_walk_tot + k_walk_count + k_walk_fill", "cell_clip": "k_clipy (count + emit)",
+    dom["kernel"] = {"edge_walk": "k_walk_tot + k_walk_fill", "cell_clip": "k_clipy (count + emit)",
                      "column_clip": "k_clipx (count + emit)", "cell_area": "k_cells",
                      "refine": "k_intersect (filter + refine)"}[name]
     dom["traffic"] = None
