@@ -626,6 +626,28 @@ struct ClipYEdge {
     }
     __device__ bool general() const { return !vert && !horiz; }
     __device__ double absc(double Y) const { return ((Y - B.y) / slope) + B.x; }
+    // (float)absc(Y), the only form in which the abscissa is used. With
+    // isl = fl(1 / slope), s' = fl(fl((Y - B.y) * isl) + B.x) is within
+    // 3.02 u |q| + 1.01 ulp(s') of absc(Y) (q the quotient), i.e. within
+    // 2^(k+1) + 1.01 units of s''s last place for k = exp(q) - exp(s') + 1.
+    // Rounding to float changes only at float midpoints — where the 29 bits
+    // of s' below float precision read 2^28 — so when those bits are more
+    // than 2^(k+2) + 2 units from 2^28, (float)s' is (float)absc(Y); else
+    // the exact expression is taken.
+    __device__ float absc_f(double Y, double isl) const {
+        const double t = Y - B.y;
+        const double q = t * isl;
+        const double sx = q + B.x;
+        const long long bs = __double_as_longlong(sx), bq = __double_as_longlong(q);
+        const int es = (int)((bs >> 52) & 0x7FF), eq = (int)((bq >> 52) & 0x7FF);
+        const int k = eq - es + 1;
+        const int low = (int)(bs & 0x1FFFFFFFll);
+        const int dist = low > (1 << 28) ? low - (1 << 28) : (1 << 28) - low;
+        const int thr = (k < 0 ? 4 : (k > 24 ? (1 << 30) : (4 << k))) + 2;
+        // a normal float's exponent range, away from overflow and subnormals
+        if (es >= 1023 - 125 && es <= 1023 + 126 && dist > thr) return (float)sx;
+        return (float)(((Y - B.y) / slope) + B.x);
+    }
     // abscissae for row lines Yi, Yi1; g0, g1 are absc(Yi), absc(Yi1) for general edges
     __device__ void row(double Yi, double Yi1, double g0, double g1, double &xi, double &xi1, bool &par) const {
         par = false;
@@ -1294,24 +1316,23 @@ __global__ void k_clipy(const PolyHdr *__restrict__ hdr, Chunk ch, const uint32_
             uint64_t at = scan ? scan[j] : 0;
             float2 buf[4];
             const ClipYEdge E(A, B);
+            const double isl = E.general() ? __drcp_rn(E.slope) : 0.0;
             double Yi = r < h.nrows ? lines[r] : 0.0;
-            double g0 = E.general() ? E.absc(Yi) : 0.0;
             // the point on line Yi, carried from the previous row's Yi1
             // (horizontal edges take per-row abscissae instead)
-            float2 pc = mk(E.vert ? (double)A.x : g0, Yi);
+            float2 pc = make_float2(E.vert ? A.x : E.absc_f(Yi, isl), (float)Yi);
             for (; r < h.nrows && Yi <= mxy + mg; r++) {
                 const double Yi1 = Yi + h.step_y;  // == lines[r + 1]
-                const double g1 = E.general() ? E.absc(Yi1) : 0.0;
-                double xi, xi1;
-                bool par;
-                E.row(Yi, Yi1, g0, g1, xi, xi1, par);
                 float2 pi, pi1;
+                bool par = false;
                 if (E.horiz) {
+                    double xi, xi1;
+                    E.row(Yi, Yi1, 0.0, 0.0, xi, xi1, par);
                     pi = mk(xi, Yi);
                     pi1 = mk(xi1, Yi1);
                 } else {
                     pi = pc;
-                    pi1 = mk(xi1, Yi1);
+                    pi1 = make_float2(E.vert ? A.x : E.absc_f(Yi1, isl), (float)Yi1);
                     pc = pi1;
                 }
                 int k = clip_y_points(A, B, Yi, Yi1, pi, pi1, par, okey ? buf : nullptr);
@@ -1325,7 +1346,6 @@ __global__ void k_clipy(const PolyHdr *__restrict__ hdr, Chunk ch, const uint32_
                 }
                 total += (uint32_t)k;
                 Yi = Yi1;
-                g0 = g1;
             }
         }
         if (cnt) cnt[j] = total;
@@ -2012,6 +2032,7 @@ int rasterize(farm_store *s, const farm_raster_opts *o, int *launches) {
             R.timer.time(T_WALK, st,
                          [&] { k_walk_tot<<<gb(n), 256, 0, st>>>(sv, R.hdr, R.doff, np, e0, n, perm, tot3,
                                                                    c16, ne, ovf); });
+            R.launches++;
         }
         int h_ovf = 1;
         FARM_TRY(d2h(s, &h_ovf, ovf, 4));
@@ -2019,7 +2040,7 @@ int rasterize(farm_store *s, const farm_raster_opts *o, int *launches) {
         FARM_TRY(s->s[S_TMP_A].ensure(2 * 3 * 8 * n1 + 16));
         uint64_t *sz = s->s[S_TMP_A].as<uint64_t>(), *sc = sz + 3 * n1;
         k_tot_sizes<<<gb(n1), 256, 0, st>>>(tot3, R.hdr, np, sz);
-        R.launches += 2;
+        R.launches++;
         for (int t = 0; t < 3; t++) FARM_TRY(excl_scan(s, sz + t * n1, sc + t * n1, n1));
         k_set_node_bases<<<gb(np), 256, 0, st>>>(R.hdr, np, sz, sc);
         R.launches++;
