@@ -272,6 +272,33 @@ def choose_band(prob: np.ndarray, y: np.ndarray, budget: float, positives: int =
     return np.nextafter(np.float32(lo), np.float32(-1)).item(), np.nextafter(np.float32(hi), np.float32(2)).item()
 
 
+def choose_band_cost(prob: np.ndarray, y: np.ndarray, cost: np.ndarray, budget: float, positives: int) -> tuple:
+    """Lambda of the cost-aware band (decide when min(p, 1 - p) <= lambda x
+    cost). Held-out pairs are decided in order of uncertainty per unit of
+    refinement cost while their errors stay within budget x positives, so the
+    error budget buys the most refinement. Arithmetic in float32, as on the
+    device. Returns (lambda, decided fraction, decided share of cost)."""
+    p = prob.astype(np.float32)
+    c = cost.astype(np.float32)
+    u = np.minimum(p, np.float32(1) - p)
+    err = (p >= np.float32(0.5)) != (y == 1)
+    allow = int(budget * max(int(positives), 1))
+    r = u / c
+    o = np.argsort(r, kind="stable")
+    ce = np.cumsum(err[o])
+    k = int(np.searchsorted(ce, allow, side="right"))
+    if k == 0:
+        return 0.0, 0.0, 0.0
+    lam = np.float32(r[o[k - 1]])
+    for _ in range(64):  # ties and rounding: shrink until the held-out errors fit
+        dec = u <= lam * c
+        if int(err[dec].sum()) <= allow:
+            break
+        lam = np.nextafter(lam, np.float32(0))
+    dec = u <= lam * c
+    return float(lam), float(dec.mean()), float(c[dec].sum() / c.sum())
+
+
 def train_scorer(args, store, dev) -> dict:
     """Train the learned scorer on pairs of a strip drawn with a separate seed,
     labelled by the exact path, and set its band from held-out pairs."""
@@ -285,7 +312,7 @@ def train_scorer(args, store, dev) -> dict:
     from farm_gb300.engine import MODE_FILTER
     dp = torch.from_numpy(pairs.view(np.int32)).to(dev).view(len(pairs), 2)
     lab, _ = store.intersect(dp)
-    code, _ = store.intersect(dp, mode=MODE_FILTER)  # the scorer only sees pairs the filter leaves (3)
+    code, cost = store.filter_costs(dp)  # the scorer only sees pairs the filter leaves (3)
     keep = torch.nonzero(lab != 2).flatten()
     g = torch.Generator(device="cpu").manual_seed(args.seed + 1001)
     keep = keep[torch.randperm(len(keep), generator=g).to(dev)][: args.learned_pairs]
@@ -301,15 +328,26 @@ def train_scorer(args, store, dev) -> dict:
     train_s = time.perf_counter() - t0
     prob = store.mlp_predict(dp[val].contiguous()).cpu().numpy()
     y = lab[val].cpu().numpy().astype(np.int64)
-    lo, hi = choose_band(prob, y, args.learned_budget, pos_val)
-    store.mlp_band(lo, hi)
-    inband = float(((prob > lo) & (prob < hi)).mean()) if len(prob) else 0.0
-    log(f"scorer trained on {len(tr)} pairs in {train_s:.1f}s (loss {loss:.4f}); band ({lo:.4f}, {hi:.4f}) "
-        f"from {len(val)} held-out pairs, {inband:.3f} of them inside it")
-    del so, sx, to, tx, dp, lab, code
+    vcost = cost[val].cpu().numpy()
+    if args.learned_band == "cost":
+        lam, dfrac, dcost = choose_band_cost(prob, y, vcost, args.learned_budget * 0.8, pos_val)
+        lo, hi = -1.0, 2.0
+        store.mlp_band(lo, hi, lam)
+        inband = 1.0 - dfrac
+        log(f"scorer trained on {len(tr)} pairs in {train_s:.1f}s (loss {loss:.4f}); cost-aware band lambda "
+            f"{lam:.3g}: decides {dfrac:.3f} of {len(val)} held-out scored pairs, {dcost:.3f} of their cost")
+    else:
+        lo, hi = choose_band(prob, y, args.learned_budget, pos_val)
+        lam, dcost = 0.0, None
+        store.mlp_band(lo, hi)
+        inband = float(((prob > lo) & (prob < hi)).mean()) if len(prob) else 0.0
+        log(f"scorer trained on {len(tr)} pairs in {train_s:.1f}s (loss {loss:.4f}); band ({lo:.4f}, {hi:.4f}) "
+            f"from {len(val)} held-out pairs, {inband:.3f} of them inside it")
+    del so, sx, to, tx, dp, lab, code, cost
     torch.cuda.empty_cache()
     return {"train_pairs": int(len(tr)), "heldout_pairs": int(len(val)), "epochs": args.learned_epochs,
-            "heldout_inside_band": inband,
+            "heldout_inside_band": inband, "band_kind": args.learned_band, "cost_lambda": lam,
+            "heldout_decided_cost_share": dcost,
             "train_s": train_s, "final_loss": loss, "band": [lo, hi], "error_budget": args.learned_budget,
             "seed": args.seed + 1000}
 
@@ -359,6 +397,7 @@ def learned_eval(store, d_pairs, exact_out, exact_query_ms: float, raster_ms: fl
             res[name]["scored_pairs"] = int(st.get("border_pairs", 0))
             res[name]["abstained_pairs"] = int(abst)
             res[name]["abstained_frac"] = abst / n
+            res[name]["abstained_refine_ms"] = st.get("ms_stage", [0, 0])[1]
     return res
 
 
@@ -609,6 +648,8 @@ def main():
                     help="skip training and evaluating the learned scorer")
     ap.add_argument("--learned-pairs", type=int, default=2_000_000, help="training + held-out pairs")
     ap.add_argument("--learned-epochs", type=int, default=12)
+    ap.add_argument("--learned-band", choices=["cost", "plain"], default="cost",
+                    help="cost-aware band (spend the error budget on expensive pairs) or a plain probability band")
     ap.add_argument("--learned-budget", type=float, default=5e-4,
                     help="false positives (negatives) allowed above (below) the band, per positive")
     args = ap.parse_args()

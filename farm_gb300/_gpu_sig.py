@@ -65,6 +65,8 @@ def declare(lib):
     lib.farm_mlp_get.argtypes = [vp, vp]
     lib.farm_mlp_set.argtypes = [vp, vp]
     lib.farm_mlp_set_band.argtypes = [vp, C.c_float, C.c_float]
+    lib.farm_mlp_set_band_cost.argtypes = [vp, C.c_float]
+    lib.farm_intersect_filter.argtypes = [vp, vp, C.c_uint64, vp, vp]
     lib.farm_mlp_features.argtypes = [vp, vp, C.c_uint64, vp, C.c_uint64]
     lib.farm_mlp_grad.argtypes = [vp, vp, vp, C.c_uint64, C.c_uint64, f32p, vp]
     lib.farm_mlp_train.argtypes = [vp, vp, vp, C.c_uint64, C.c_int, C.c_int, C.c_float, C.c_uint64, f32p]

@@ -27,7 +27,8 @@ constexpr int kQueue = 256;  // BORDER x BORDER pixel pairs buffered per warp
 struct PairView {
     const uint32_t *pairs;
     uint64_t n;
-    uint64_t tgt_base;  // global index of target 0
+    uint64_t tgt_base;         // global index of target 0
+    uint32_t *bb = nullptr;    // K_FILTER: per pair, refinement cost proxy (float bits)
 };
 
 // Point.h:93-97: (a - o) x (b - o) in float, no fused multiply-add
@@ -264,6 +265,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         const int wh = w.ey - w.sy + 1;
         const long nw = (long)(w.ex - w.sx + 1) * wh;
         bool decided = false, has_bb = false;
+        uint32_t pair_bb = 0;
         int qn = 0;  // warp-uniform queue fill
         auto flush = [&]() {
             // the warp refines the queued pixel pairs one after another and
@@ -357,6 +359,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
                 if (kMode != K_EXACT) {  // nothing to refine
                     if (lane == 0) my_bb += __popc(m);
                     has_bb |= m != 0;
+                    pair_bb += __popc(m);
                     m = 0;
                 }
                 if (m) {
@@ -381,6 +384,13 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         }
         if (lane == 0) {
             if (out) out[pid] = decided ? 1 : (kMode == K_FILTER && has_bb ? 3 : 0);
+            if (kMode == K_FILTER && pv.bb) {
+                // refinement cost proxy: BORDER x BORDER pixel pairs x the two
+                // polygons' edges per pixel (segment tests per pixel pair)
+                const float c = (float)pair_bb * ((float)S.nv / (float)(S.P ? S.P : 1)) *
+                                ((float)T.nv / (float)(T.P ? T.P : 1));
+                pv.bb[pid] = __float_as_uint(c);
+            }
             my_found += decided;
         }
         __syncwarp();
@@ -402,13 +412,14 @@ int intersect_learned(farm_store *s, const uint32_t *pairs, uint64_t n, int mem,
 
 // The filter alone over n device pairs: out[k] = 1 / 0 / 3 (K_FILTER). Counts
 // IN-decided pairs into *in_hits.
-int intersect_filter(farm_store *s, const uint32_t *dpairs, uint64_t n, uint8_t *dout, uint64_t *in_hits) {
+int intersect_filter(farm_store *s, const uint32_t *dpairs, uint64_t n, uint8_t *dout, uint64_t *in_hits,
+                     uint32_t *bb) {
     cudaStream_t stream = s->stream;
     FARM_TRY(s->d_counters.ensure(256));
     unsigned long long *next = s->d_counters.as<unsigned long long>() + 8;
     IxCounters *ctr = reinterpret_cast<IxCounters *>(next + 1);
     FARM_CUDA(cudaMemsetAsync(next, 0, 8 + sizeof(IxCounters), stream));
-    PairView pv{dpairs, n, s->n_side[0]};
+    PairView pv{dpairs, n, s->n_side[0], bb};
     k_intersect<K_FILTER><<<sm_count() * 8, kWarpsPerBlock * 32, 0, stream>>>(s->view(), pv, next, dout, ctr);
     s->launches++;
     FARM_CUDA(cudaGetLastError());
@@ -482,6 +493,21 @@ int intersect(farm_store *s, const uint32_t *pairs, uint64_t n, int mode, int me
 
 }  // namespace farm
 
+extern "C" int farm_intersect_filter(farm_store *s, const uint32_t *d_pairs, uint64_t n, uint8_t *d_code,
+                                     float *d_cost) {
+    using namespace farm;
+    if (!s || (n && (!d_pairs || !d_code || !d_cost))) {
+        set_error("invalid arguments to farm_intersect_filter");
+        return FARM_EINVAL;
+    }
+    if (!s->rasterized) {
+        set_error("farm_intersect_filter: rasterize first");
+        return FARM_EINVAL;
+    }
+    if (!n) return FARM_OK;
+    return intersect_filter(s, d_pairs, n, d_code, nullptr, reinterpret_cast<uint32_t *>(d_cost));
+}
+
 extern "C" int farm_intersect(farm_store *s, const uint32_t *pairs, uint64_t n, int mode, int mem, uint8_t *out,
                               uint64_t *found, farm_stats *st) {
     using namespace farm;
@@ -500,7 +526,7 @@ extern "C" int farm_intersect(farm_store *s, const uint32_t *pairs, uint64_t n, 
             return FARM_EINVAL;
         }
         uint64_t in_hits = 0;
-        FARM_TRY(intersect_filter(s, pairs, n, out, &in_hits));
+        FARM_TRY(intersect_filter(s, pairs, n, out, &in_hits, nullptr));
         if (found) *found = in_hits;
         if (st) {
             memset(st, 0, sizeof *st);

@@ -14,11 +14,13 @@ float mlp_band(farm_store *s, int which);
 int intersect(farm_store *s, const uint32_t *pairs, uint64_t n, int mode, int mem, uint8_t *out, uint64_t *found,
               farm_stats *st);
 
-int intersect_filter(farm_store *s, const uint32_t *dpairs, uint64_t n, uint8_t *dout, uint64_t *in_hits);
+int intersect_filter(farm_store *s, const uint32_t *dpairs, uint64_t n, uint8_t *dout, uint64_t *in_hits,
+                     uint32_t *bb);
 
 // pairs the filter left undecided (code 3), compacted with their positions
-__global__ void k_select_undecided(const uint8_t *__restrict__ code, const uint32_t *__restrict__ pairs, uint64_t n,
-                                   uint32_t *__restrict__ upairs, uint64_t *__restrict__ uidx,
+__global__ void k_select_undecided(const uint8_t *__restrict__ code, const uint32_t *__restrict__ pairs,
+                                   const uint32_t *__restrict__ bb, uint64_t n, uint32_t *__restrict__ upairs,
+                                   uint64_t *__restrict__ uidx, uint32_t *__restrict__ ucost,
                                    unsigned long long *__restrict__ nu) {
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
         if (code[k] != 3) continue;
@@ -26,19 +28,26 @@ __global__ void k_select_undecided(const uint8_t *__restrict__ code, const uint3
         upairs[2 * at] = pairs[2 * k];
         upairs[2 * at + 1] = pairs[2 * k + 1];
         uidx[at] = k;
+        ucost[at] = bb[k];
     }
 }
 
-// confident pairs decided, uncertain ones compacted for exact refinement
+// confident pairs decided, uncertain ones compacted for exact refinement.
+// Confidence is p >= hi / p <= lo, or — cost-aware — an uncertainty
+// min(p, 1 - p) no larger than lambda x the pair's refinement cost proxy (its
+// BORDER x BORDER pixel pairs x both polygons' edges per pixel), so the error
+// budget goes where deciding saves the most refinement.
 __global__ void k_band(const float *__restrict__ prob, const uint32_t *__restrict__ upairs,
-                       const uint64_t *__restrict__ uidx, uint64_t nu, float lo, float hi, uint8_t *__restrict__ out,
-                       uint32_t *__restrict__ apairs, uint64_t *__restrict__ aidx,
-                       unsigned long long *__restrict__ na) {
+                       const uint64_t *__restrict__ uidx, const uint32_t *__restrict__ ucost, uint64_t nu, float lo,
+                       float hi, float lambda, uint8_t *__restrict__ out, uint32_t *__restrict__ apairs,
+                       uint64_t *__restrict__ aidx, unsigned long long *__restrict__ na) {
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nu; k += (uint64_t)gridDim.x * blockDim.x) {
-        float p = prob[k];
-        if (p >= hi) {
+        const float p = prob[k];
+        const float u = p < 0.5f ? p : 1.f - p;
+        const bool cheap = lambda > 0.f && u <= lambda * __uint_as_float(ucost[k]);
+        if (p >= hi || (cheap && p >= 0.5f)) {
             out[uidx[k]] = 1;
-        } else if (p <= lo) {
+        } else if (p <= lo || cheap) {
             out[uidx[k]] = 0;
         } else {
             unsigned long long at = atomicAdd(na, 1ull);
@@ -96,11 +105,13 @@ int intersect_learned(farm_store *s, const uint32_t *pairs, uint64_t n, int mem,
         FARM_TRY(s->d_out.ensure(n + 64));
         dout = s->d_out.as<uint8_t>();
     }
-    DevBuf &prob = s->s[26], &up = s->s[27], &ap = s->s[28], &ao = s->s[29];
+    DevBuf &prob = s->s[26], &up = s->s[27], &ap = s->s[28], &ao = s->s[29], &cost = s->s[30];
     FARM_TRY(prob.ensure(4 * n + 64));
     FARM_TRY(up.ensure(16 * n + 64));
     FARM_TRY(ap.ensure(16 * n + 64));
     FARM_TRY(ao.ensure(n + 64));
+    FARM_TRY(cost.ensure(8 * n + 64));
+    uint32_t *bb = cost.as<uint32_t>(), *ucost = bb + n + 16;
     FARM_TRY(s->d_counters.ensure(256));
     unsigned long long *cnt = s->d_counters.as<unsigned long long>() + 24;  // [0] undecided [1] band [2] found
     FARM_CUDA(cudaMemsetAsync(cnt, 0, 24, stream));
@@ -110,10 +121,10 @@ int intersect_learned(farm_store *s, const uint32_t *pairs, uint64_t n, int mem,
     cudaEventCreate(&t1);
     if (t0) cudaEventRecord(t0, stream);
     uint64_t in_hits = 0;
-    if (n) FARM_TRY(intersect_filter(s, dpairs, n, dout, &in_hits));
+    if (n) FARM_TRY(intersect_filter(s, dpairs, n, dout, &in_hits, bb));
     uint32_t *upairs = up.as<uint32_t>();
     uint64_t *uidx = reinterpret_cast<uint64_t *>(upairs + 2 * n + 2);
-    k_select_undecided<<<blocks_for(n), 256, 0, stream>>>(dout, dpairs, n, upairs, uidx, cnt);
+    k_select_undecided<<<blocks_for(n), 256, 0, stream>>>(dout, dpairs, bb, n, upairs, uidx, ucost, cnt);
     unsigned long long h_nu = 0;
     FARM_CUDA(cudaMemcpyAsync(&h_nu, cnt, 8, cudaMemcpyDeviceToHost, stream));
     FARM_CUDA(cudaStreamSynchronize(stream));
@@ -125,8 +136,8 @@ int intersect_learned(farm_store *s, const uint32_t *pairs, uint64_t n, int mem,
         if (rc) return rc;
         uint32_t *apairs = ap.as<uint32_t>();
         uint64_t *aidx = reinterpret_cast<uint64_t *>(apairs + 2 * n + 2);
-        k_band<<<blocks_for(h_nu), 256, 0, stream>>>(prob.as<float>(), upairs, uidx, h_nu, mlp_band(s, 0),
-                                                     mlp_band(s, 1), dout, apairs, aidx, cnt + 1);
+        k_band<<<blocks_for(h_nu), 256, 0, stream>>>(prob.as<float>(), upairs, uidx, ucost, h_nu, mlp_band(s, 0),
+                                                     mlp_band(s, 1), mlp_band(s, 2), dout, apairs, aidx, cnt + 1);
         FARM_CUDA(cudaMemcpyAsync(&h_na, cnt + 1, 8, cudaMemcpyDeviceToHost, stream));
         FARM_CUDA(cudaStreamSynchronize(stream));
         if (h_na) {

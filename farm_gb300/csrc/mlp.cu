@@ -35,6 +35,7 @@ struct Mlp {
     DevBuf adam;                   // fp32 moments for every parameter (m, v)
     uint64_t step = 0;
     float lo = 0.02f, hi = 0.98f;  // abstain band for the learned mode
+    float lambda = 0.f;            // cost-aware band: also decide when min(p, 1-p) <= lambda x cost
     bool ready = false;
     // scratch
     DevBuf X, Z1, H1, Z2, H2, logit, dlogit, dZ2, dZ1, T1, T2, T3, gW1, gW2, gb, err;
@@ -301,7 +302,7 @@ void mlp_free(void *p) {
 
 float mlp_band(farm_store *s, int which) {
     Mlp *m = static_cast<Mlp *>(s->mlp);
-    return m ? (which ? m->hi : m->lo) : 0.f;
+    return m ? (which == 2 ? m->lambda : (which ? m->hi : m->lo)) : 0.f;
 }
 
 static Mlp *mlp_of(farm_store *s) {
@@ -530,10 +531,22 @@ uint64_t farm_mlp_param_count(void) { return n_params(); }
 /* Decision band of the learned mode: probability >= hi decides 1, <= lo
  * decides 0, anything between goes to exact refinement. */
 int farm_mlp_set_band(farm_store *s, float lo, float hi) {
-    if (!s || !(lo >= 0.f) || !(hi <= 1.f) || lo > hi) return FARM_EINVAL;
+    if (!s || !(lo <= hi) || !isfinite(lo) || !isfinite(hi)) {
+        set_error("farm_mlp_set_band: need finite lo <= hi");
+        return FARM_EINVAL;
+    }
     Mlp *m = mlp_of(s);
     m->lo = lo;
     m->hi = hi;
+    return FARM_OK;
+}
+
+int farm_mlp_set_band_cost(farm_store *s, float lambda) {
+    if (!s || !(lambda >= 0.f) || !isfinite(lambda)) {
+        set_error("farm_mlp_set_band_cost: need a finite lambda >= 0");
+        return FARM_EINVAL;
+    }
+    mlp_of(s)->lambda = lambda;
     return FARM_OK;
 }
 

@@ -167,8 +167,20 @@ class Store:
         assert params.size == int(self._lib.farm_mlp_param_count())
         check_gpu(self._lib.farm_mlp_set(self._h, C.c_void_p(params.ctypes.data)))
 
-    def mlp_band(self, lo: float, hi: float) -> None:
+    def mlp_band(self, lo: float, hi: float, cost_lambda: float = 0.0) -> None:
         check_gpu(self._lib.farm_mlp_set_band(self._h, lo, hi))
+        check_gpu(self._lib.farm_mlp_set_band_cost(self._h, cost_lambda))
+
+    def filter_costs(self, d_pairs):
+        """The exact filter alone on device pairs: (codes 0/1/3, refinement cost
+        proxies) as device tensors."""
+        import torch
+        n = d_pairs.shape[0]
+        code = torch.empty(n, dtype=torch.uint8, device=d_pairs.device)
+        cost = torch.empty(n, dtype=torch.float32, device=d_pairs.device)
+        check_gpu(self._lib.farm_intersect_filter(self._h, C.c_void_p(d_pairs.data_ptr()), n,
+                                                  C.c_void_p(code.data_ptr()), C.c_void_p(cost.data_ptr())))
+        return code, cost
 
     def mlp_features(self, d_pairs, rows: int = 0):
         import torch

@@ -106,6 +106,12 @@ int farm_rasterize(farm_store *s, const farm_raster_opts *o);
 int farm_intersect(farm_store *s, const uint32_t *pairs, uint64_t n, int mode, int mem, uint8_t *out,
                    uint64_t *found, farm_stats *st);
 
+/* The exact filter alone on n device pairs (the learned mode's first stage):
+ * d_code[k] as FARM_MODE_FILTER, d_cost[k] = pair k's refinement cost proxy
+ * (float): the BORDER x BORDER pixel pairs it found x both polygons' edges per
+ * pixel. No counterpart in the reference. */
+int farm_intersect_filter(farm_store *s, const uint32_t *d_pairs, uint64_t n, uint8_t *d_code, float *d_cost);
+
 /* Decide Ideal::within(source[p.s], target[p.t]) (hierarchical rasters required).
  * distance in km with geography (the reference: 10 km, degree coordinates),
  * in coordinate units without (planar mode for projected coordinates). */
@@ -165,6 +171,9 @@ int farm_mlp_get(farm_store *s, float *params);
 int farm_mlp_set(farm_store *s, const float *params);
 /* Probability >= hi decides 1, <= lo decides 0, otherwise exact refinement. */
 int farm_mlp_set_band(farm_store *s, float lo, float hi);
+/* Cost-aware band (0 = off): a pair is also decided (by p >= 0.5) when
+ * min(p, 1 - p) <= lambda x its refinement cost proxy (farm_intersect_filter). */
+int farm_mlp_set_band_cost(farm_store *s, float lambda);
 /* Features (bf16 [rows x 576], rows >= n, zero padding) of n device pairs. */
 int farm_mlp_features(farm_store *s, const uint32_t *d_pairs, uint64_t n, void *d_X, uint64_t rows);
 /* One forward/backward on device features and labels; loss and gradients

@@ -151,4 +151,20 @@ def test_learned_mode_beats_the_reference_heuristic(gpu_lib):
     assert np.array_equal(out[refined], truth[refined])
     assert st.last_stats["fp64_rechecks"] == int(refined.sum())
     assert st.last_stats["border_pairs"] == int((code == 3).sum())
+    # cost-aware band: a pair is also decided when min(p, 1 - p) <= lambda x
+    # its refinement cost proxy; every other scored pair is refined
+    code2, cost = st.filter_costs(dte)
+    assert np.array_equal(code2.cpu().numpy(), code)
+    cost = cost.cpu().numpy().astype(np.float32)
+    p32 = prob.astype(np.float32)
+    u = np.minimum(p32, np.float32(1) - p32)
+    lam = np.float32(np.median(u[code == 3] / cost[code == 3]))
+    st.mlp_band(0.05, 0.95, cost_lambda=float(lam))
+    out2, _ = st.intersect(np.ascontiguousarray(pairs[te]), mode=MODE_LEARNED)
+    cheap = u <= lam * cost
+    refined2 = (code == 3) & (p32 > 0.05) & (p32 < 0.95) & ~cheap
+    assert np.array_equal(out2[decided], truth[decided])
+    assert np.array_equal(out2[refined2], truth[refined2])
+    assert st.last_stats["fp64_rechecks"] == int(refined2.sum())
+    assert refined2.sum() < refined.sum()
     st.close()
