@@ -11,7 +11,8 @@ class Stats(C.Structure):
     _fields_ = [("pairs", C.c_uint64), ("found", C.c_uint64), ("in_hits", C.c_uint64),
                 ("border_pairs", C.c_uint64), ("segment_tests", C.c_uint64), ("fp64_rechecks", C.c_uint64),
                 ("ms_total", C.c_double), ("ms_stage", C.c_double * 4), ("kernel_launches", C.c_int32),
-                ("reserved", C.c_int32), ("src_window_pixels", C.c_uint64), ("tgt_window_pixels", C.c_uint64)]
+                ("reserved", C.c_int32), ("src_window_pixels", C.c_uint64), ("tgt_window_pixels", C.c_uint64),
+                ("sequence_pairs", C.c_uint64)]
 
 
 class RasterTotals(C.Structure):

@@ -34,6 +34,7 @@ namespace farm {
 // regenerated on the host from its defining formula.
 __constant__ float c_mean20[20];
 __constant__ double c_deg_lon[900];
+__constant__ float c_inv_deg_lon_f[900];  // 1 / c_deg_lon, rounded to float (FP32 first pass only)
 
 static std::mutex g_tab_mu;
 static bool g_tab_ready[64] = {};
@@ -54,6 +55,9 @@ static int ensure_tables(int dev) {
     }
     FARM_CUDA(cudaMemcpyToSymbol(c_mean20, mean20, sizeof mean20));
     FARM_CUDA(cudaMemcpyToSymbol(c_deg_lon, deg, sizeof deg));
+    float inv[900];
+    for (int i = 0; i < 900; i++) inv[i] = (float)(1.0 / deg[i]);
+    FARM_CUDA(cudaMemcpyToSymbol(c_inv_deg_lon_f, inv, sizeof inv));
     if (dev >= 0 && dev < 64) g_tab_ready[dev] = true;
     return FARM_OK;
 }
@@ -100,25 +104,29 @@ __device__ double box_distance(const Box &a, const Box &t, bool geo) {
     return sqrt(dx * dx + dy * dy);
 }
 
-// Box.cpp:120-149: the corners become float points first
+// Box.cpp:120-149: the corners become float points first, and the result is
+// the largest of the 16 corner-to-corner distances. A corner pair's x
+// difference depends only on the two corners' x choices and its y difference
+// only on their y choices, so the 16 pairs are every combination of one of
+// the 4 x differences with one of the 4 y differences. Every step of a
+// distance — the float subtraction, the division by the degree scale, the
+// square, the sum and sqrt — is monotone in |dx| and |dy| under
+// round-to-nearest, so the largest distance is the one built from the
+// largest |dx| and the largest |dy|: the same double, with 2 divisions and
+// one sqrt instead of 32 and 16.
 __device__ double box_max_distance(const Box &a, const Box &t, bool geo) {
-    float ax[2] = {(float)a.lo0, (float)a.hi0}, ay[2] = {(float)a.lo1, (float)a.hi1};
-    float tx[2] = {(float)t.lo0, (float)t.hi0}, ty[2] = {(float)t.lo1, (float)t.hi1};
-    double dlon = geo ? deg_lon(a.lo1) : 1.0;
-    double md = 0.0;
-    for (int i = 0; i < 4; i++)
-        for (int j = 0; j < 4; j++) {
-            // vertices1[i] = (x, y) with x from {lo, lo, hi, hi}, y from {lo, hi, lo, hi}
-            float vx = ax[i >> 1], vy = ay[i & 1], wx = tx[j >> 1], wy = ty[j & 1];
-            double dx = __fsub_rn(vx, wx), dy = __fsub_rn(vy, wy);
-            if (geo) {
-                dy = dy / DEG_LAT;
-                dx = dx / dlon;
-            }
-            double d = sqrt(dx * dx + dy * dy);
-            md = md > d ? md : d;
-        }
-    return md;
+    const float ax0 = (float)a.lo0, ax1 = (float)a.hi0, ay0 = (float)a.lo1, ay1 = (float)a.hi1;
+    const float tx0 = (float)t.lo0, tx1 = (float)t.hi0, ty0 = (float)t.lo1, ty1 = (float)t.hi1;
+    const float mx = fmaxf(fmaxf(fabsf(__fsub_rn(ax0, tx0)), fabsf(__fsub_rn(ax0, tx1))),
+                           fmaxf(fabsf(__fsub_rn(ax1, tx0)), fabsf(__fsub_rn(ax1, tx1))));
+    const float my = fmaxf(fmaxf(fabsf(__fsub_rn(ay0, ty0)), fabsf(__fsub_rn(ay0, ty1))),
+                           fmaxf(fabsf(__fsub_rn(ay1, ty0)), fabsf(__fsub_rn(ay1, ty1))));
+    double dx = mx, dy = my;
+    if (geo) {
+        dy = dy / DEG_LAT;
+        dx = dx / deg_lon(a.lo1);
+    }
+    return sqrt(dx * dx + dy * dy);
 }
 
 // geometry_computation.h:49-89
@@ -146,6 +154,55 @@ __device__ double pt_seg_dist(float2 p, float2 p1, float2 p2, bool geo) {
         dy = dy / DEG_LAT;
     }
     return sqrt(dx * dx + dy * dy);
+}
+
+// FP32 first pass of pt_seg_dist, with a bound on its distance from the FP64
+// value pt_seg_dist returns. It works relative to p1 — the reference's own
+// float differences A, B, C, D and the projection parameter clamped to
+// [0, 1] — so absolute coordinates never enter its rounding:
+//   |d32 - d64| <= 20 u32 (M + L) S + 7 u32 d32 + 8 u64 (|p| + |p1| + M + L) S
+// (taken about 3x wider below)
+// with M = |A| + |B|, L = |C| + |D|, S the geography scale (1 when planar).
+// The first term covers the FP32 dot/length/parameter/projection rounding
+// and the float roundings of the differences the reference keeps in double;
+// the second the sqrt, scaling and squares; the third the reference's own
+// FP64 rounding (its projection is taken in absolute coordinates). The
+// distance to a segment is 1-Lipschitz in the clamped parameter times the
+// segment length, so branch flips at the clamp stay inside the bound.
+__device__ __forceinline__ float pt_seg_dist32(float2 p, float2 p1, float2 p2, bool geo, float &err) {
+    const float A = __fsub_rn(p.x, p1.x), B = __fsub_rn(p.y, p1.y);
+    const float C = __fsub_rn(p2.x, p1.x), D = __fsub_rn(p2.y, p1.y);
+    const float dot = __fadd_rn(__fmul_rn(A, C), __fmul_rn(B, D));
+    const float len = __fadd_rn(__fmul_rn(C, C), __fmul_rn(D, D));
+    float t = len != 0.f ? __fdiv_rn(dot, len) : 0.f;
+    t = fminf(fmaxf(t, 0.f), 1.f);
+    float dx = __fsub_rn(A, __fmul_rn(t, C)), dy = __fsub_rn(B, __fmul_rn(t, D));
+    float S = 1.f;
+    if (geo) {
+        float a = fabsf(p.y);
+        if (a == 90.f) a = 89.9f;
+        int idx = (int)(a * 10.f);
+        if (idx < 0 || idx >= 900) idx = 899;
+        // the table index may differ from the FP64 one at a boundary; taking
+        // the larger neighbouring scale keeps the bound valid either way
+        const float s0 = c_inv_deg_lon_f[idx];
+        const float s1 = c_inv_deg_lon_f[idx + 1 < 900 ? idx + 1 : 899];
+        const float s2 = c_inv_deg_lon_f[idx > 0 ? idx - 1 : 0];
+        const float sy = (float)(40076.0 / 360.0);
+        dx = __fmul_rn(dx, s0);
+        dy = __fmul_rn(dy, sy);
+        S = fmaxf(fmaxf(fmaxf(s0, s1), s2), sy);
+        // a neighbouring table entry changes dx's scale: widen by that difference
+        err = fabsf(__fsub_rn(A, __fmul_rn(t, C))) * fmaxf(fabsf(s1 - s0), fabsf(s2 - s0));
+    } else {
+        err = 0.f;
+    }
+    const float d = sqrtf(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
+    const float M = fabsf(A) + fabsf(B), L = fabsf(C) + fabsf(D);
+    const float absx = fabsf(p.x) + fabsf(p.y) + fabsf(p1.x) + fabsf(p1.y);
+    // the derivation's constants (20 u32, 7 u32, 8 u64), widened about 3x
+    err += 4e-6f * (M + L) * S + 1.2e-6f * d + 3e-15f * (absx + M + L) * S;
+    return d;
 }
 
 struct WCand {
@@ -423,6 +480,40 @@ __global__ void k_cand_bounds(const WCand *__restrict__ c, uint64_t n, uint64_t 
     }
 }
 
+// suf[k] = the smallest lo of the pair's candidates after k (100000 after the
+// last), the bound Ideal.cpp:2615-2621 recomputes for every candidate; one
+// warp per refined pair scans its candidates backwards 32 at a time.
+__global__ void k_cand_sufmin(const WCand *__restrict__ c, uint64_t ncand, const uint64_t *__restrict__ first,
+                              const uint8_t *__restrict__ out, uint64_t n, double *__restrict__ suf) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t w0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t pid = w0; pid < n; pid += nw) {
+        if (out[pid] != W_REFINE) continue;
+        const uint64_t b = first[pid];
+        uint64_t e = b;
+        while (e < ncand && c[e].pair == pid) e++;
+        double carry = 100000.0;
+        for (uint64_t hi = e; hi > b;) {
+            const uint64_t cnt = hi - b < 32 ? hi - b : 32;
+            const bool v = (uint64_t)lane < cnt;
+            const uint64_t k = hi - 1 - lane;
+            double incl = v ? c[k].lo : 100000.0;
+            // inclusive min over lanes 0..lane (indices hi-1 down to k)
+            for (int o = 1; o < 32; o <<= 1) {
+                double x = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl = incl < x ? incl : x;
+            }
+            double before = __shfl_up_sync(0xffffffffu, incl, 1);  // indices after k in this chunk
+            double r = lane == 0 ? carry : (carry < before ? carry : before);
+            if (v) suf[k] = r;
+            double last = __shfl_sync(0xffffffffu, incl, 31);
+            carry = carry < last ? carry : last;
+            hi -= cnt;
+        }
+    }
+}
+
 struct RefineArgs {
     const uint32_t *pairs;
     uint64_t n;
@@ -432,6 +523,7 @@ struct RefineArgs {
     const WCand *cand;
     uint64_t ncand;
     const uint64_t *first;
+    const double *suf;  // per candidate: smallest lo of the later candidates
     uint8_t *out;
     unsigned long long *next;
     unsigned long long *stats;  // seq pairs, point-segment tests
@@ -442,7 +534,7 @@ __global__ void __launch_bounds__(256) k_within_refine(const StoreView sv, Refin
     const int lane = threadIdx.x & 31;
     const bool geo = a.geo != 0;
     const int cc = sv.category_count;
-    unsigned long long my_seq = 0, my_tests = 0;
+    unsigned long long my_seq = 0, my_tests = 0, my_rechk = 0;
     for (;;) {
         unsigned long long pid = 0;
         if (lane == 0) pid = atomicAdd(a.next, 1ull);
@@ -462,12 +554,7 @@ __global__ void __launch_bounds__(256) k_within_refine(const StoreView sv, Refin
         int decided = -1;
         for (uint64_t k = b; k < e && decided < 0; k++) {
             // lower bound of every later candidate
-            double ref = 100000.0;
-            for (uint64_t q = k + 1 + lane; q < e; q += 32) ref = ref < a.cand[q].lo ? ref : a.cand[q].lo;
-            for (int o = 16; o; o >>= 1) {
-                double v = __shfl_xor_sync(0xffffffffu, ref, o);
-                ref = ref < v ? ref : v;
-            }
+            const double ref = a.suf[k];
             const int id1 = a.cand[k].id1, id2 = a.cand[k].id2;
             uint32_t a0 = 0, a1 = 0, b0 = 0, b1 = 0;
             if (show_status(sv.status[S.st + id1], cc) == 1) {
@@ -486,28 +573,48 @@ __global__ void __launch_bounds__(256) k_within_refine(const StoreView sv, Refin
                     // segment_to_segment_within_batch(target seq, source seq):
                     // e2.y target points vs e1.y - 1 source segments, and back
                     const uint32_t n1 = e2.y * (e1.y - 1), n2 = e1.y * (e2.y - 1);
-                    double m = 1.7976931348623157e308;
+                    // FP32 first: a lower bound on this sequence pair's minimum
+                    float lb = 3.4e38f;
                     for (uint32_t k2 = lane; k2 < n1 + n2; k2 += 32) {
-                        double d;
+                        float d, er;
                         if (k2 < n1) {
                             uint32_t pi = k2 / (e1.y - 1), si = k2 % (e1.y - 1);
-                            d = pt_seg_dist(tr[e2.x + pi], sr[e1.x + si], sr[e1.x + si + 1], geo);
+                            d = pt_seg_dist32(tr[e2.x + pi], sr[e1.x + si], sr[e1.x + si + 1], geo, er);
                         } else {
                             uint32_t r = k2 - n1;
                             uint32_t pi = r / (e2.y - 1), si = r % (e2.y - 1);
-                            d = pt_seg_dist(sr[e1.x + pi], tr[e2.x + si], tr[e2.x + si + 1], geo);
+                            d = pt_seg_dist32(sr[e1.x + pi], tr[e2.x + si], tr[e2.x + si + 1], geo, er);
                         }
-                        m = m < d ? m : d;
+                        lb = fminf(lb, d - er);
                     }
-                    for (int o = 16; o; o >>= 1) {
-                        double v = __shfl_xor_sync(0xffffffffu, m, o);
-                        m = m < v ? m : v;
-                    }
+                    for (int o = 16; o; o >>= 1) lb = fminf(lb, __shfl_xor_sync(0xffffffffu, lb, o));
                     if (lane == 0) {
                         my_seq++;
                         my_tests += n1 + n2;
                     }
-                    min_dist = min_dist < m ? min_dist : m;
+                    // FP64 only when this pair may lower the exact running
+                    // minimum, so min_dist is always the reference's value
+                    if ((double)lb < min_dist) {
+                        double m = 1.7976931348623157e308;
+                        for (uint32_t k2 = lane; k2 < n1 + n2; k2 += 32) {
+                            double d;
+                            if (k2 < n1) {
+                                uint32_t pi = k2 / (e1.y - 1), si = k2 % (e1.y - 1);
+                                d = pt_seg_dist(tr[e2.x + pi], sr[e1.x + si], sr[e1.x + si + 1], geo);
+                            } else {
+                                uint32_t r = k2 - n1;
+                                uint32_t pi = r / (e2.y - 1), si = r % (e2.y - 1);
+                                d = pt_seg_dist(sr[e1.x + pi], tr[e2.x + si], tr[e2.x + si + 1], geo);
+                            }
+                            m = m < d ? m : d;
+                        }
+                        for (int o = 16; o; o >>= 1) {
+                            double v = __shfl_xor_sync(0xffffffffu, m, o);
+                            m = m < v ? m : v;
+                        }
+                        if (lane == 0) my_rechk++;
+                        min_dist = min_dist < m ? min_dist : m;
+                    }
                     if (min_dist < a.thr) {
                         decided = 1;
                         break;
@@ -523,6 +630,7 @@ __global__ void __launch_bounds__(256) k_within_refine(const StoreView sv, Refin
     if (lane == 0) {
         atomicAdd(&a.stats[0], my_seq);
         atomicAdd(&a.stats[1], my_tests);
+        atomicAdd(&a.stats[2], my_rechk);
     }
 }
 
@@ -623,15 +731,23 @@ static int within_round(farm_store *s, const uint32_t *dpairs, uint64_t n, uint8
         ra.cand = cand.as<WCand>();
         ra.ncand = nc;
         ra.first = first.as<uint64_t>();
+        DevBuf &suf = s->s[35];
+        FARM_TRY(suf.ensure(8 * nc + 64));
+        k_cand_sufmin<<<sm_count() * 8, 256, 0, st>>>(cand.as<WCand>(), nc, first.as<uint64_t>(), dout, n,
+                                                      suf.as<double>());
+        launches++;
+        ra.suf = suf.as<double>();
         ra.out = dout;
         ra.next = ctr + 4;
         ra.stats = ctr + 5;
         k_within_refine<<<sm_count() * 8, 256, 0, st>>>(sv, ra);
         launches += 2;
-        unsigned long long hs[2];
-        FARM_CUDA(cudaMemcpyAsync(hs, ctr + 5, 16, cudaMemcpyDeviceToHost, st));
+        unsigned long long hs[3];
+        FARM_CUDA(cudaMemcpyAsync(hs, ctr + 5, 24, cudaMemcpyDeviceToHost, st));
         FARM_CUDA(cudaStreamSynchronize(st));
+        acc->sequence_pairs += hs[0];
         acc->segment_tests += hs[1];
+        acc->fp64_rechecks += hs[2];
     }
     return FARM_OK;
 }
@@ -736,6 +852,8 @@ int within(farm_store *s, const uint32_t *pairs, uint64_t n, double distance, in
         st->found = hf[0];
         st->border_pairs = acc.border_pairs;
         st->segment_tests = acc.segment_tests;
+        st->fp64_rechecks = acc.fp64_rechecks;
+        st->sequence_pairs = acc.sequence_pairs;
         st->in_hits = acc.in_hits;
         float ms = 0;
         cudaEventElapsedTime(&ms, s->ev[6], s->ev[7]);

@@ -53,7 +53,8 @@ def stats_dict(st: Stats) -> dict:
     return {"pairs": st.pairs, "found": st.found, "in_hits": st.in_hits, "border_pairs": st.border_pairs,
             "segment_tests": st.segment_tests, "fp64_rechecks": st.fp64_rechecks, "ms_total": st.ms_total,
             "ms_stage": list(st.ms_stage), "kernel_launches": st.kernel_launches,
-            "src_window_pixels": st.src_window_pixels, "tgt_window_pixels": st.tgt_window_pixels}
+            "src_window_pixels": st.src_window_pixels, "tgt_window_pixels": st.tgt_window_pixels,
+            "sequence_pairs": st.sequence_pairs}
 
 
 class Store:

@@ -72,13 +72,15 @@ typedef struct farm_stats {
     uint64_t in_hits;        /* decided by an IN pixel overlap (intersect) */
     uint64_t border_pairs;   /* BORDER x BORDER pixel pairs examined */
     uint64_t segment_tests;  /* segment-pair (or point-segment) evaluations */
-    uint64_t fp64_rechecks;  /* within: distances re-evaluated in FP64 */
+    uint64_t fp64_rechecks;  /* within: edge-sequence pairs re-evaluated in FP64 after the FP32 pass;
+                                learned intersect: pairs refined exactly */
     double ms_total;         /* device time of the call (CUDA events) */
     double ms_stage[4];      /* raster, filter, refine, other */
     int32_t kernel_launches; /* engine kernels launched by the call */
     int32_t reserved;
     uint64_t src_window_pixels; /* source pixels in the target-MBR windows */
     uint64_t tgt_window_pixels; /* target pixels visited under non-OUT source pixels */
+    uint64_t sequence_pairs;    /* within: edge-sequence pairs evaluated (FP32 pass) */
 } farm_stats;
 
 const char *farm_last_error(void);

@@ -59,3 +59,21 @@ def test_gpu_within_planar_metres(gpu_lib):
     exp = np.array([O.within(RS[s], RS[t], distance=d, geography=False) for s, t in pairs], np.uint8)
     assert np.array_equal(out, exp), f"{int((out != exp).sum())} of {len(exp)} differ"
     assert 0 < found < len(pairs)
+
+
+def test_gpu_within_planar_large_coordinates(gpu_lib):
+    # metre coordinates up to ~1e5 (the reference's Box starts at +-100000,
+    # Box.h:6-12, so beyond that its MBRs clamp): the FP32 first pass works
+    # relative to each segment, so only sequence pairs whose lower bound can
+    # lower the running minimum are re-evaluated in FP64; the pair set must
+    # still be the reference's
+    prm = P.StarParams(dom_lo=5.0e4, dom_hi=9.5e4, r_lo=50.0, r_hi=3000.0, n_lo=32, n_hi=1500)
+    S = P.generate(prm, 52, 300)
+    d = 500.0
+    pairs = P.mbr_join(S.mbrs(), S.mbrs(), expand=d, geography=False, skip_same=True)
+    out, found, stats = run_within(S, S, pairs, 10, True, distance=d, geography=False, grid_extent=1e7)
+    RS = O.rasterize_set(S, 10, True, grid_extent=1e7)
+    exp = np.array([O.within(RS[s], RS[t], distance=d, geography=False) for s, t in pairs], np.uint8)
+    assert np.array_equal(out, exp), f"{int((out != exp).sum())} of {len(exp)} differ"
+    assert 0 < found < len(pairs)
+    assert stats["fp64_rechecks"] > 0
