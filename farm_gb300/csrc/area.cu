@@ -23,26 +23,48 @@
 // vertex); crossings at a shared vertex are counted once by half-open ranges.
 #include <cub/cub.cuh>
 
+#include <algorithm>
 #include <cstring>
+#include <string>
+#include <vector>
 
 #include "common.cuh"
 
 namespace farm {
 
+// Edges per work item by size bucket: bucket b holds pairs whose larger edge
+// count has floor(log2) == b. Chosen by farm_area_autotune (default 256).
+struct Chunks {
+    uint16_t c[32];
+    __host__ __device__ uint32_t of(uint32_t es, uint32_t et) const {
+        uint32_t m = es > et ? es : et;
+        int b = m ? 31 - clz32(m) : 0;
+        return c[b];
+    }
+    __host__ __device__ static int clz32(uint32_t x) {
+#ifdef __CUDA_ARCH__
+        return __clz(x);
+#else
+        return __builtin_clz(x);
+#endif
+    }
+};
+
 struct AreaArgs {
     const uint32_t *pairs;
-    uint64_t n;
+    const uint64_t *n;           // pair count (device scalar)
     uint64_t tgt_base;
-    uint32_t chunk;              // edges per item
-    const uint64_t *item_start;  // per pair: first item (n + 1)
-    uint64_t nitems;
+    Chunks chunks;               // edges per item, by size bucket
+    const uint64_t *item_start;  // per pair: first item; item_start[*n] = item count
+    uint64_t cap_items;          // partial's capacity
     double *partial;             // per item
     const int8_t *orient;        // per polygon: +1 counter-clockwise, -1 clockwise
     unsigned long long *next;
-    unsigned long long *overflow;
+    unsigned long long *overflow;  // [0] crossings beyond the fast path, [1] items beyond cap_items
 };
 
-constexpr int kMaxCross = 48;
+constexpr int kMaxCross = 48;     // crossings per edge deduplicated in registers
+constexpr int kHashSlots = 1024;  // beyond that, a per-lane hash set (half full at most)
 
 __device__ __forceinline__ double cross2(double ax, double ay, double bx, double by) { return ax * by - ay * bx; }
 
@@ -126,22 +148,29 @@ __global__ void __launch_bounds__(256) k_area(const StoreView sv, AreaArgs a) {
     const int lane = threadIdx.x & 31;
     const int cc = sv.category_count;
     for (;;) {
+        const uint64_t n = *a.n;
+        const uint64_t nitems = a.item_start[n];
+        if (nitems > a.cap_items) {  // a plan's capacity was exceeded: report, compute nothing
+            if (lane == 0 && blockIdx.x == 0 && threadIdx.x == 0) atomicExch(&a.overflow[1], 1ull);
+            break;
+        }
         unsigned long long it = 0;
         if (lane == 0) it = atomicAdd(a.next, 1ull);
         it = __shfl_sync(0xffffffffu, it, 0);
-        if (it >= a.nitems) break;
-        uint32_t p = find_segment(a.item_start, (uint32_t)a.n, it);
+        if (it >= nitems) break;
+        uint32_t p = find_segment(a.item_start, (uint32_t)n, it);
         uint64_t rel = it - a.item_start[p];
         const PolyHdr &S = sv.hdr[a.pairs[2 * p]];
         const PolyHdr &T = sv.hdr[a.tgt_base + a.pairs[2 * p + 1]];
         uint32_t es = S.nv - 1, et = T.nv - 1;  // edges (the ring's last edge is the zero-length closing one)
-        uint64_t cs = (es + a.chunk - 1) / a.chunk;
+        const uint32_t chunk = a.chunks.of(es, et);
+        uint64_t cs = (es + chunk - 1) / chunk;
         bool side_t = rel >= cs;
         const PolyHdr &M = side_t ? T : S;  // the boundary integrated
         const PolyHdr &O = side_t ? S : T;  // the polygon it is clipped by
-        uint32_t first = (uint32_t)((side_t ? rel - cs : rel) * a.chunk);
+        uint32_t first = (uint32_t)((side_t ? rel - cs : rel) * chunk);
         uint32_t me = side_t ? et : es;
-        uint32_t last = first + a.chunk < me ? first + a.chunk : me;
+        uint32_t last = first + chunk < me ? first + chunk : me;
         const float2 *mr = sv.ring + M.ring, *orr = sv.ring + O.ring;
         const float2 o0 = sv.ring[S.ring];
         const double ox = o0.x, oy = o0.y;
@@ -186,7 +215,35 @@ __global__ void __launch_bounds__(256) k_area(const StoreView sv, AreaArgs a) {
                         sum_t += (osign * den > 0) ? t : -t;
                     });
                     if (slow) {
-                        // many crossings: find earlier listings of the same edge by re-enumeration
+                        // many crossings: an open-addressing set of the edges
+                        // already counted (per lane, local memory)
+                        nc = 0;
+                        sum_t = 0;
+                        uint32_t table[kHashSlots];
+                        for (int q = 0; q < kHashSlots; q++) table[q] = 0xFFFFFFFFu;
+                        int used = 0;
+                        bool full = false;
+                        for_candidate_edges(sv, O, P.x, P.y, Q.x, Q.y, cc, [&](uint32_t f) {
+                            double t, den;
+                            if (full || !crossing(px, py, dx, dy, orr, f, ox, oy, t, den)) return;
+                            uint32_t h = (f * 2654435761u) & (kHashSlots - 1);
+                            while (table[h] != 0xFFFFFFFFu) {
+                                if (table[h] == f) return;
+                                h = (h + 1) & (kHashSlots - 1);
+                            }
+                            if (++used > kHashSlots / 2) {
+                                full = true;
+                                return;
+                            }
+                            table[h] = f;
+                            nc++;
+                            sum_t += (osign * den > 0) ? t : -t;
+                        });
+                        slow = full;
+                    }
+                    if (slow) {
+                        // beyond the set's capacity: find earlier listings of the
+                        // same edge by re-enumeration
                         nc = 0;
                         sum_t = 0;
                         uint64_t pos = 0;
@@ -235,10 +292,12 @@ __global__ void k_orient(const StoreView sv, uint32_t npoly, int8_t *__restrict_
     }
 }
 
-__global__ void k_area_items(const StoreView sv, const uint32_t *__restrict__ pairs, uint64_t n, uint64_t tgt_base,
-                             uint32_t chunk, uint64_t *__restrict__ cnt) {
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k <= n; k += (uint64_t)gridDim.x * blockDim.x) {
-        if (k == n) {
+// items per pair, for every slot up to cap (0 past the pair count)
+__global__ void k_area_items(const StoreView sv, const uint32_t *__restrict__ pairs, const uint64_t *__restrict__ np,
+                             uint64_t cap, uint64_t tgt_base, Chunks chunks, uint64_t *__restrict__ cnt) {
+    const uint64_t n = *np;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k <= cap; k += (uint64_t)gridDim.x * blockDim.x) {
+        if (k >= n) {
             cnt[k] = 0;
             continue;
         }
@@ -249,14 +308,16 @@ __global__ void k_area_items(const StoreView sv, const uint32_t *__restrict__ pa
             continue;
         }
         uint32_t es = S.nv - 1, et = T.nv - 1;
+        const uint32_t chunk = chunks.of(es, et);
         cnt[k] = (es + chunk - 1) / chunk + (et + chunk - 1) / chunk;
     }
 }
 
 // fixed-order sum of each pair's item partials
-__global__ void k_area_reduce(const uint64_t *__restrict__ item_start, uint64_t n, const double *__restrict__ partial,
-                              const StoreView sv, const uint32_t *__restrict__ pairs, uint64_t tgt_base,
-                              double *__restrict__ out) {
+__global__ void k_area_reduce(const uint64_t *__restrict__ item_start, const uint64_t *__restrict__ np,
+                              const double *__restrict__ partial, const StoreView sv,
+                              const uint32_t *__restrict__ pairs, uint64_t tgt_base, double *__restrict__ out) {
+    const uint64_t n = *np;
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
         const PolyHdr &S = sv.hdr[pairs[2 * k]];
         const PolyHdr &T = sv.hdr[tgt_base + pairs[2 * k + 1]];
@@ -270,17 +331,92 @@ __global__ void k_area_reduce(const uint64_t *__restrict__ item_start, uint64_t 
     }
 }
 
-int intersection_area(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, double *out, farm_stats *st) {
+// ---------------------------------------------------------------- host --
+
+static Chunks chunks_of(const farm_store *s) {
+    Chunks c;
+    for (int b = 0; b < 32; b++) c.c[b] = (uint16_t)(s->area_chunk[b] > 0 ? s->area_chunk[b] : 256);
+    return c;
+}
+
+// polygon orientations, computed once per rasterization, in a scratch slot of
+// their own (a captured plan holds its address)
+constexpr int kOrientSlot = 36;
+static int ensure_orient(farm_store *s, cudaStream_t st) {
+    DevBuf &ori = s->s[kOrientSlot];
+    if (s->orient_epoch == s->raster_epoch && ori.cap >= s->n_poly) return FARM_OK;
+    FARM_TRY(ori.ensure(s->n_poly + 64));
+    unsigned ob = (unsigned)((32ull * s->n_poly + 255) / 256);
+    if (ob > 8192) ob = 8192;
+    k_orient<<<ob, 256, 0, st>>>(s->view(), (uint32_t)s->n_poly, ori.as<int8_t>());
+    s->launches++;
+    FARM_CUDA(cudaGetLastError());
+    s->orient_epoch = s->raster_epoch;
+    return FARM_OK;
+}
+
+// Buffers of one area pass. Everything the kernels need to know about the
+// batch (pair count, item count) is read on the device, so the same sequence
+// can be captured once in a CUDA graph and replayed for any batch that fits.
+struct AreaBufs {
+    const uint32_t *pairs;
+    const uint64_t *n;  // device scalar
+    uint64_t cap_pairs;
+    uint64_t *cnt, *start;  // cap_pairs + 1 each
+    double *partial;
+    uint64_t cap_items;
+    unsigned long long *ctr;  // [0] work counter, [1] [2] overflow flags
+    void *scan_tmp;
+    size_t scan_bytes;
+    double *out;
+    Chunks chunks;
+};
+
+static int scan_bytes(uint64_t cap, size_t *bytes) {
+    FARM_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, *bytes, (const uint64_t *)nullptr, (uint64_t *)nullptr,
+                                            (int64_t)(cap + 1)));
+    return FARM_OK;
+}
+
+static int area_items(farm_store *s, const AreaBufs &b, cudaStream_t st) {
+    unsigned blocks = (unsigned)((b.cap_pairs + 256) / 256);
+    if (blocks > 4096) blocks = 4096;
+    k_area_items<<<blocks, 256, 0, st>>>(s->view(), b.pairs, b.n, b.cap_pairs, s->n_side[0], b.chunks, b.cnt);
+    FARM_CUDA(cudaGetLastError());
+    size_t bytes = b.scan_bytes;
+    FARM_CUDA(cub::DeviceScan::ExclusiveSum(b.scan_tmp, bytes, b.cnt, b.start, (int64_t)(b.cap_pairs + 1), st));
+    return FARM_OK;
+}
+
+static int area_compute(farm_store *s, const AreaBufs &b, cudaStream_t st) {
+    FARM_CUDA(cudaMemsetAsync(b.ctr, 0, 24, st));
+    AreaArgs aa{b.pairs, b.n, s->n_side[0], b.chunks, b.start, b.cap_items, b.partial, s->s[kOrientSlot].as<int8_t>(),
+                b.ctr, b.ctr + 1};
+    k_area<<<sm_count() * 8, 256, 0, st>>>(s->view(), aa);
+    FARM_CUDA(cudaGetLastError());
+    unsigned blocks = (unsigned)((b.cap_pairs + 255) / 256);
+    if (blocks > 4096) blocks = 4096;
+    if (!blocks) blocks = 1;
+    k_area_reduce<<<blocks, 256, 0, st>>>(b.start, b.n, b.partial, s->view(), b.pairs, s->n_side[0], b.out);
+    FARM_CUDA(cudaGetLastError());
+    return FARM_OK;
+}
+
+static int area_checks(farm_store *s, const char *who) {
     if (!s->rasterized) {
-        set_error("farm_intersection_area: rasterize first");
+        set_error(std::string(who) + ": rasterize first");
         return FARM_EINVAL;
     }
     if (s->n_side[1] == 0) {
-        set_error("farm_intersection_area: no target side loaded");
+        set_error(std::string(who) + ": no target side loaded");
         return FARM_EINVAL;
     }
+    return FARM_OK;
+}
+
+int intersection_area(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, double *out, farm_stats *st) {
+    FARM_TRY(area_checks(s, "farm_intersection_area"));
     cudaStream_t stream = s->stream;
-    const uint64_t tgt_base = s->n_side[0];
     const uint32_t *dpairs = pairs;
     if (mem == FARM_MEM_HOST && n) {
         FARM_TRY(s->d_pairs.ensure(8 * n));
@@ -292,47 +428,39 @@ int intersection_area(farm_store *s, const uint32_t *pairs, uint64_t n, int mem,
         FARM_TRY(s->d_out.ensure(8 * n + 64));
         dout = s->d_out.as<double>();
     }
-    StoreView sv = s->view();
-    const uint32_t chunk = 256;
-    DevBuf &cnt = s->s[26], &start = s->s[27], &part = s->s[28], &tmp = s->cub_tmp;
+    DevBuf &cnt = s->s[26], &start = s->s[27], &part = s->s[28];
     FARM_TRY(cnt.ensure(8 * (n + 1) + 64));
     FARM_TRY(start.ensure(8 * (n + 1) + 64));
     FARM_TRY(s->d_counters.ensure(256));
     unsigned long long *ctr = s->d_counters.as<unsigned long long>();
-    FARM_CUDA(cudaMemsetAsync(ctr, 0, 64, stream));
+    uint64_t *dn = reinterpret_cast<uint64_t *>(ctr + 8);
+    FARM_CUDA(cudaMemcpyAsync(dn, &n, 8, cudaMemcpyHostToDevice, stream));
+    FARM_TRY(ensure_orient(s, stream));
+    AreaBufs b{};
+    b.pairs = dpairs;
+    b.n = dn;
+    b.cap_pairs = n;
+    b.cnt = cnt.as<uint64_t>();
+    b.start = start.as<uint64_t>();
+    b.ctr = ctr;
+    b.out = dout;
+    b.chunks = chunks_of(s);
+    FARM_TRY(scan_bytes(n, &b.scan_bytes));
+    FARM_TRY(s->cub_tmp.ensure(b.scan_bytes + 64));
+    b.scan_tmp = s->cub_tmp.p;
     FARM_CUDA(cudaEventRecord(s->ev[6], stream));
-    unsigned blocks = (unsigned)((n + 256) / 256);
-    if (blocks > 4096) blocks = 4096;
-    k_area_items<<<blocks, 256, 0, stream>>>(sv, dpairs, n, tgt_base, chunk, cnt.as<uint64_t>());
-    size_t bytes = 0;
-    FARM_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, bytes, cnt.as<uint64_t>(), start.as<uint64_t>(), (int64_t)(n + 1),
-                                            stream));
-    FARM_TRY(tmp.ensure(bytes + 64));
-    FARM_CUDA(cub::DeviceScan::ExclusiveSum(tmp.p, bytes, cnt.as<uint64_t>(), start.as<uint64_t>(), (int64_t)(n + 1),
-                                            stream));
+    FARM_TRY(area_items(s, b, stream));
     uint64_t nitems = 0;
-    FARM_CUDA(cudaMemcpyAsync(&nitems, start.as<uint64_t>() + n, 8, cudaMemcpyDeviceToHost, stream));
+    FARM_CUDA(cudaMemcpyAsync(&nitems, b.start + n, 8, cudaMemcpyDeviceToHost, stream));
     FARM_CUDA(cudaStreamSynchronize(stream));
     FARM_TRY(part.ensure(8 * nitems + 64));
-    DevBuf &ori = s->s[29];
-    FARM_TRY(ori.ensure(s->n_poly + 64));
-    {
-        unsigned ob = (unsigned)((32ull * s->n_poly + 255) / 256);
-        if (ob > 8192) ob = 8192;
-        k_orient<<<ob, 256, 0, stream>>>(sv, (uint32_t)s->n_poly, ori.as<int8_t>());
-    }
-    AreaArgs aa{dpairs, n, tgt_base, chunk, start.as<uint64_t>(), nitems, part.as<double>(), ori.as<int8_t>(), ctr,
-                ctr + 1};
-    if (nitems) k_area<<<sm_count() * 8, 256, 0, stream>>>(sv, aa);
-    k_area_reduce<<<blocks, 256, 0, stream>>>(start.as<uint64_t>(), n, part.as<double>(), sv, dpairs, tgt_base, dout);
-    FARM_CUDA(cudaGetLastError());
+    b.partial = part.as<double>();
+    b.cap_items = nitems;
+    FARM_TRY(area_compute(s, b, stream));
     FARM_CUDA(cudaEventRecord(s->ev[7], stream));
-    unsigned long long over = 0;
-    FARM_CUDA(cudaMemcpyAsync(&over, ctr + 1, 8, cudaMemcpyDeviceToHost, stream));
     if (mem == FARM_MEM_HOST && out && n) FARM_CUDA(cudaMemcpyAsync(out, dout, 8 * n, cudaMemcpyDeviceToHost, stream));
     FARM_CUDA(cudaStreamSynchronize(stream));
-    s->launches += 4 + (nitems ? 1 : 0);
-    (void)over;
+    s->launches += 4;
     if (st) {
         memset(st, 0, sizeof *st);
         st->pairs = n;
@@ -340,7 +468,7 @@ int intersection_area(farm_store *s, const uint32_t *pairs, uint64_t n, int mem,
         cudaEventElapsedTime(&ms, s->ev[6], s->ev[7]);
         st->ms_total = ms;
         st->ms_stage[2] = ms;
-        st->kernel_launches = 4 + (nitems ? 1 : 0);
+        st->kernel_launches = 4;
     }
     return FARM_OK;
 }
@@ -355,4 +483,231 @@ extern "C" int farm_intersection_area(farm_store *s, const uint32_t *pairs, uint
         return FARM_EINVAL;
     }
     return intersection_area(s, pairs, n, mem, out, st);
+}
+
+// ------------------------------------------------------ plans and tuning --
+// A plan owns fixed-capacity buffers for one area pass and the CUDA graph of
+// that pass (items, scan, the persistent work-stealing kernel, the per-pair
+// reduction), captured once. Running it copies a batch of pairs in and
+// replays the graph: one launch for any batch within capacity, whatever its
+// mix of tiny and huge pairs.
+struct farm_area_plan {
+    farm_store *s = nullptr;
+    uint64_t cap_pairs = 0, cap_items = 0, epoch = 0;
+    farm::DevBuf pairs, n, cnt, start, partial, ctr, tmp, out;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+void plan_free(farm_area_plan *p) {
+    if (!p) return;
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    for (farm::DevBuf *b : {&p->pairs, &p->n, &p->cnt, &p->start, &p->partial, &p->ctr, &p->tmp, &p->out})
+        b->release();
+    delete p;
+}
+}  // namespace
+
+extern "C" int farm_area_plan_create(farm_store *s, uint64_t max_pairs, uint64_t max_items, farm_area_plan **out) {
+    using namespace farm;
+    if (!s || !out || max_pairs == 0 || max_items == 0) {
+        set_error("invalid arguments to farm_area_plan_create");
+        return FARM_EINVAL;
+    }
+    *out = nullptr;
+    FARM_TRY(area_checks(s, "farm_area_plan_create"));
+    cudaStream_t st = s->stream;
+    FARM_TRY(ensure_orient(s, st));
+    farm_area_plan *p = new farm_area_plan();
+    p->s = s;
+    p->cap_pairs = max_pairs;
+    p->cap_items = max_items;
+    p->epoch = s->raster_epoch;
+    AreaBufs b{};
+    int rc = FARM_OK;
+    if (rc == FARM_OK) rc = p->pairs.ensure(8 * max_pairs + 64);
+    if (rc == FARM_OK) rc = p->n.ensure(64);
+    if (rc == FARM_OK) rc = p->cnt.ensure(8 * (max_pairs + 1) + 64);
+    if (rc == FARM_OK) rc = p->start.ensure(8 * (max_pairs + 1) + 64);
+    if (rc == FARM_OK) rc = p->partial.ensure(8 * max_items + 64);
+    if (rc == FARM_OK) rc = p->ctr.ensure(64);
+    if (rc == FARM_OK) rc = p->out.ensure(8 * max_pairs + 64);
+    if (rc == FARM_OK) rc = scan_bytes(max_pairs, &b.scan_bytes);
+    if (rc == FARM_OK) rc = p->tmp.ensure(b.scan_bytes + 64);
+    if (rc == FARM_OK) {
+        cudaError_t e = cudaMemsetAsync(p->n.p, 0, 8, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) rc = cuda_fail(e, "farm_area_plan_create");
+    }
+    if (rc != FARM_OK) {
+        plan_free(p);
+        return rc;
+    }
+    b.pairs = p->pairs.as<uint32_t>();
+    b.n = p->n.as<uint64_t>();
+    b.cap_pairs = max_pairs;
+    b.cnt = p->cnt.as<uint64_t>();
+    b.start = p->start.as<uint64_t>();
+    b.partial = p->partial.as<double>();
+    b.cap_items = max_items;
+    b.ctr = p->ctr.as<unsigned long long>();
+    b.scan_tmp = p->tmp.p;
+    b.out = p->out.as<double>();
+    b.chunks = chunks_of(s);
+    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        plan_free(p);
+        return cuda_fail(e, "cudaStreamBeginCapture");
+    }
+    int rc1 = area_items(s, b, st);
+    int rc2 = rc1 == FARM_OK ? area_compute(s, b, st) : rc1;
+    e = cudaStreamEndCapture(st, &p->graph);
+    if (rc2 != FARM_OK || e != cudaSuccess) {
+        plan_free(p);
+        return rc2 != FARM_OK ? rc2 : cuda_fail(e, "cudaStreamEndCapture");
+    }
+    e = cudaGraphInstantiate(&p->exec, p->graph, 0);
+    if (e != cudaSuccess) {
+        plan_free(p);
+        return cuda_fail(e, "cudaGraphInstantiate");
+    }
+    *out = p;
+    return FARM_OK;
+}
+
+extern "C" int farm_area_plan_run(farm_area_plan *p, const uint32_t *pairs, uint64_t n, int mem, double *out,
+                                  farm_stats *st_out) {
+    using namespace farm;
+    if (!p || (n && (!pairs || !out))) {
+        set_error("invalid arguments to farm_area_plan_run");
+        return FARM_EINVAL;
+    }
+    farm_store *s = p->s;
+    if (n > p->cap_pairs) {
+        set_error("farm_area_plan_run: " + std::to_string(n) + " pairs exceed the plan's capacity of " +
+                  std::to_string(p->cap_pairs));
+        return FARM_EINVAL;
+    }
+    if (s->raster_epoch != p->epoch) {
+        set_error("farm_area_plan_run: the store was reloaded or rasterized again since the plan was made");
+        return FARM_EINVAL;
+    }
+    cudaStream_t st = s->stream;
+    const cudaMemcpyKind k_in = mem == FARM_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    const cudaMemcpyKind k_out = mem == FARM_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    if (n) FARM_CUDA(cudaMemcpyAsync(p->pairs.p, pairs, 8 * n, k_in, st));
+    FARM_CUDA(cudaMemcpyAsync(p->n.p, &n, 8, cudaMemcpyHostToDevice, st));
+    FARM_CUDA(cudaEventRecord(s->ev[6], st));
+    FARM_CUDA(cudaGraphLaunch(p->exec, st));
+    FARM_CUDA(cudaEventRecord(s->ev[7], st));
+    unsigned long long flags[3] = {0, 0, 0};
+    FARM_CUDA(cudaMemcpyAsync(flags, p->ctr.p, 24, cudaMemcpyDeviceToHost, st));
+    if (n) FARM_CUDA(cudaMemcpyAsync(out, p->out.p, 8 * n, k_out, st));
+    FARM_CUDA(cudaStreamSynchronize(st));
+    s->launches += 3;
+    if (flags[2]) {
+        set_error("farm_area_plan_run: the batch needs more work items than the plan's capacity of " +
+                  std::to_string(p->cap_items));
+        return FARM_EOVERFLOW;
+    }
+    if (st_out) {
+        memset(st_out, 0, sizeof *st_out);
+        st_out->pairs = n;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, s->ev[6], s->ev[7]);
+        st_out->ms_total = ms;
+        st_out->ms_stage[2] = ms;
+        st_out->kernel_launches = 1;  // one graph launch
+    }
+    return FARM_OK;
+}
+
+extern "C" void farm_area_plan_destroy(farm_area_plan *p) { plan_free(p); }
+
+extern "C" int farm_area_set_chunks(farm_store *s, const int32_t *chunk_by_bucket) {
+    using namespace farm;
+    if (!s || !chunk_by_bucket) {
+        set_error("invalid arguments to farm_area_set_chunks");
+        return FARM_EINVAL;
+    }
+    for (int b = 0; b < 32; b++)
+        if (chunk_by_bucket[b] < 0 || chunk_by_bucket[b] > 32768) {
+            set_error("farm_area_set_chunks: chunk sizes must lie in 1..32768 (0 = default)");
+            return FARM_EINVAL;
+        }
+    for (int b = 0; b < 32; b++) s->area_chunk[b] = chunk_by_bucket[b];
+    return FARM_OK;
+}
+
+// Autotuner: for every size bucket present in the sample (floor(log2) of a
+// pair's larger edge count), time the area pass on up to 2048 of its pairs
+// with each candidate chunk size and keep the fastest. The store keeps the
+// table (farm_area_set_chunks); it is also returned.
+extern "C" int farm_area_autotune(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, int32_t *table_out) {
+    using namespace farm;
+    if (!s || (n && !pairs)) {
+        set_error("invalid arguments to farm_area_autotune");
+        return FARM_EINVAL;
+    }
+    FARM_TRY(area_checks(s, "farm_area_autotune"));
+    std::vector<uint32_t> hp(2 * n);
+    if (n) {
+        if (mem == FARM_MEM_HOST) {
+            memcpy(hp.data(), pairs, 8 * n);
+        } else {
+            FARM_CUDA(cudaMemcpyAsync(hp.data(), pairs, 8 * n, cudaMemcpyDeviceToHost, s->stream));
+            FARM_CUDA(cudaStreamSynchronize(s->stream));
+        }
+    }
+    auto edges = [&](int side, uint32_t k) -> uint32_t {
+        const std::vector<uint64_t> &o = s->h_off[side];
+        return (uint32_t)(o[k + 1] - o[k]);  // stored vertices = edges of the in-memory ring
+    };
+    std::vector<std::vector<uint32_t>> byb(32);
+    for (uint64_t i = 0; i < n; i++) {
+        if (hp[2 * i] >= s->n_side[0] || hp[2 * i + 1] >= s->n_side[1]) {
+            set_error("farm_area_autotune: pair index out of range");
+            return FARM_EINVAL;
+        }
+        uint32_t m = std::max(edges(0, hp[2 * i]), edges(1, hp[2 * i + 1]));
+        int b = m ? 31 - __builtin_clz(m) : 0;
+        if (byb[b].size() < 2 * 2048) {
+            byb[b].push_back(hp[2 * i]);
+            byb[b].push_back(hp[2 * i + 1]);
+        }
+    }
+    static const int32_t kCand[] = {32, 64, 128, 256, 512, 1024, 2048};
+    int32_t saved[32];
+    memcpy(saved, s->area_chunk, sizeof saved);
+    int32_t best_tab[32];
+    memcpy(best_tab, s->area_chunk, sizeof best_tab);
+    for (int b = 0; b < 32; b++) {
+        if (byb[b].empty()) continue;
+        const uint64_t nb = byb[b].size() / 2;
+        double best_ms = 1e300;
+        int32_t best = 256;
+        for (int32_t c : kCand) {
+            for (int q = 0; q < 32; q++) s->area_chunk[q] = c;
+            double ms = 1e300;
+            for (int rep = 0; rep < 2; rep++) {  // the first run warms up
+                farm_stats stt;
+                int rc = intersection_area(s, byb[b].data(), nb, FARM_MEM_HOST, nullptr, &stt);
+                if (rc != FARM_OK) {
+                    memcpy(s->area_chunk, saved, sizeof saved);
+                    return rc;
+                }
+                if (rep) ms = stt.ms_total;
+            }
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = c;
+            }
+        }
+        best_tab[b] = best;
+    }
+    memcpy(s->area_chunk, best_tab, sizeof best_tab);
+    if (table_out) memcpy(table_out, best_tab, sizeof best_tab);
+    return FARM_OK;
 }

@@ -207,5 +207,8 @@ struct farm_store {
     cudaEvent_t ev[8] = {};
     uint64_t launches = 0;  // engine kernels launched through this store
     void *mlp = nullptr;    // learned scorer state (mlp.cu)
+    uint64_t raster_epoch = 0;     // bumped by every rasterization (plans check it)
+    uint64_t orient_epoch = ~0ull;  // raster_epoch the cached orientations belong to
+    int32_t area_chunk[32] = {};   // edges per area item by size bucket (0: the default 256)
     farm::StoreView view() const;
 };

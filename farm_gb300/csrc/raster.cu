@@ -2162,6 +2162,7 @@ extern "C" int farm_rasterize(farm_store *s, const farm_raster_opts *o) {
     s->launches += (uint64_t)launches;
     // with FARM_EASSERT the other polygons' rasters stay valid and inspectable;
     // queries refuse to run on such a store
+    s->raster_epoch++;
     if (rc == FARM_OK || rc == FARM_EASSERT) s->rasterized = true;
     s->raster_err = rc == FARM_EASSERT ? rc : 0;
     return rc;

@@ -154,6 +154,24 @@ class Store:
         self.last_stats = stats_dict(st)
         return out
 
+    # ---- batched area (captured CUDA graph, autotuned chunks) ------------
+    def area_plan(self, max_pairs: int, max_items: int) -> "AreaPlan":
+        h = C.c_void_p()
+        check_gpu(self._lib.farm_area_plan_create(self._h, max_pairs, max_items, C.byref(h)))
+        return AreaPlan(self, h)
+
+    def area_autotune(self, pairs) -> np.ndarray:
+        pairs = np.ascontiguousarray(pairs, dtype=np.uint32)
+        tab = np.zeros(32, np.int32)
+        check_gpu(self._lib.farm_area_autotune(self._h, C.c_void_p(pairs.ctypes.data), pairs.shape[0], MEM_HOST,
+                                               C.c_void_p(tab.ctypes.data)))
+        return tab
+
+    def area_set_chunks(self, table) -> None:
+        tab = np.ascontiguousarray(table, dtype=np.int32)
+        assert tab.size == 32
+        check_gpu(self._lib.farm_area_set_chunks(self._h, C.c_void_p(tab.ctypes.data)))
+
     # ---- learned scorer (device tensors: torch CUDA) -------------------
     def mlp_init(self, seed: int = 1) -> None:
         check_gpu(self._lib.farm_mlp_init(self._h, seed))
@@ -292,3 +310,34 @@ def device_name() -> str:
     ordn = C.c_int(0)
     check_gpu(gpu().farm_device_info(C.byref(ordn), buf, 256))
     return buf.value.decode()
+
+
+class AreaPlan:
+    """A captured area pass (farm_area_plan): run() replays it on a batch."""
+
+    def __init__(self, store: Store, handle):
+        self._store, self._h = store, handle
+        self.last_stats = {}
+
+    def run(self, pairs, out=None):
+        n = pairs.shape[0]
+        pp, mem = _addr(pairs)
+        if out is None:
+            out = np.zeros(n, dtype=np.float64) if mem == MEM_HOST else _torch_empty_f64(n, pairs.device)
+        po, _ = _addr(out)
+        st = Stats()
+        check_gpu(self._store._lib.farm_area_plan_run(self._h, pp, n, mem, po, C.byref(st)))
+        self.last_stats = stats_dict(st)
+        return out
+
+    def close(self):
+        if self._h:
+            self._store._lib.farm_area_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+

@@ -162,6 +162,27 @@ int farm_intersect_static(farm_store *s, const uint32_t *pairs, uint64_t n, uint
  * of 16, K a multiple of 64, BN the tile width (64, 128, 256). */
 int farm_tc_gemm_test(const void *A, const void *B, float *C, int M, int N, int K, int BN);
 
+/* ---- batched area queries (no counterpart in the reference) ----
+ * A plan captures one area pass — work items per pair, their scan, the
+ * persistent work-stealing area kernel and the per-pair reduction — in a CUDA
+ * graph over buffers of fixed capacity. farm_area_plan_run copies a batch of
+ * up to max_pairs pairs in and replays the graph (results as
+ * farm_intersection_area). max_items bounds the batch's work items: each pair
+ * has ceil(edges_s / chunk) + ceil(edges_t / chunk) of them (chunk per size
+ * bucket, 256 by default); a batch needing more fails with FARM_EOVERFLOW.
+ * A plan is tied to the store's current rasterization. */
+typedef struct farm_area_plan farm_area_plan;
+int farm_area_plan_create(farm_store *s, uint64_t max_pairs, uint64_t max_items, farm_area_plan **out);
+int farm_area_plan_run(farm_area_plan *p, const uint32_t *pairs, uint64_t n, int mem, double *out, farm_stats *st);
+void farm_area_plan_destroy(farm_area_plan *p);
+/* Edges per area work item by size bucket b = floor(log2(larger edge count of
+ * the pair)), 32 entries (0 = default 256). */
+int farm_area_set_chunks(farm_store *s, const int32_t *chunk_by_bucket);
+/* Time each candidate chunk size (32 ... 2048) on up to 2048 pairs of every
+ * bucket present in the sample, keep the fastest per bucket in the store and
+ * return the table (32 entries). */
+int farm_area_autotune(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, int32_t *table_out);
+
 /* ---- learned scorer (FARM_MODE_LEARNED): 520 -> 256 -> 256 -> 1 MLP, GELU,
  * bf16 weights/activations on tcgen05 tensor cores, fp32 accumulate. It takes
  * the place of the reference's "-a" confidence heuristic

@@ -71,3 +71,69 @@ def test_gpu_area_matches_oracle(gpu_lib, vpr, seed):
     out = run_area(S, T, pairs, vpr)
     check(S, T, pairs, out)
     assert (out > 0).sum() > len(out) // 4
+
+
+def _mixed_sets(seed):
+    # configuration 4 in miniature: tiny and huge polygons mixed in one batch
+    rng = np.random.default_rng(seed)
+    small = P.StarParams(dom_hi=12.0, r_lo=0.2, r_hi=1.0, n_lo=8, n_hi=40)
+    big = P.StarParams(dom_hi=12.0, r_lo=1.0, r_hi=2.0, n_lo=500, n_hi=3000)
+    A, B = P.generate(small, seed, 120), P.generate(big, seed + 1, 12)
+    C, D = P.generate(small, seed + 2, 120), P.generate(big, seed + 3, 12)
+    S = P.PolygonSet(np.concatenate([A.off[:-1], A.off[-1] + B.off]).astype(np.uint64), np.concatenate([A.xy, B.xy]))
+    T = P.PolygonSet(np.concatenate([C.off[:-1], C.off[-1] + D.off]).astype(np.uint64), np.concatenate([C.xy, D.xy]))
+    pairs = P.mbr_join(S.mbrs(), T.mbrs())
+    return S, T, pairs[rng.permutation(len(pairs))]
+
+
+def _checkable(S, T, pairs, k=40):
+    # pairs the O(n m) oracle finishes quickly: tiny x tiny and tiny x huge
+    return [i for i, (s, t) in enumerate(pairs) if len(S.ring(s)) * len(T.ring(t)) < 2_000_000][:k]
+
+
+def test_gpu_area_plan_replays_graph(gpu_lib):
+    # one captured graph, replayed on two different batches: the same doubles
+    # as the direct call, and a batch beyond capacity is refused
+    S, T, pairs = _mixed_sets(61)
+    assert len(pairs) > 200
+    st = Store()
+    st.load_sets(S, T)
+    st.rasterize(vpr=10)
+    half = len(pairs) // 2
+    b1, b2 = np.ascontiguousarray(pairs[:half]), np.ascontiguousarray(pairs[half:])
+    ref1, ref2 = st.intersection_area(b1), st.intersection_area(b2)
+    plan = st.area_plan(max_pairs=len(pairs), max_items=1 << 20)
+    got1, got2 = plan.run(b1), plan.run(b2)
+    assert np.array_equal(got1, ref1) and np.array_equal(got2, ref2)
+    assert plan.last_stats["kernel_launches"] == 1
+    from farm_gb300._native import FarmError
+    with pytest.raises(FarmError):
+        plan.run(np.ascontiguousarray(np.concatenate([pairs, pairs])))
+    small = st.area_plan(max_pairs=len(pairs), max_items=4)
+    with pytest.raises(FarmError) as ei:
+        small.run(b1)
+    assert ei.value.code == -4  # FARM_EOVERFLOW
+    plan.close()
+    small.close()
+    sel = _checkable(S, T, b1)
+    check(S, T, b1[sel], ref1[sel])
+    st.close()
+
+
+def test_gpu_area_autotune(gpu_lib):
+    # the tuned chunk table changes how edges are split into work items, not
+    # the answer (within the FP64 tolerance)
+    S, T, pairs = _mixed_sets(62)
+    st = Store()
+    st.load_sets(S, T)
+    st.rasterize(vpr=10)
+    base = st.intersection_area(pairs)
+    tab = st.area_autotune(pairs)
+    assert tab.shape == (32,) and (tab > 0).any()
+    assert set(np.unique(tab[tab > 0])) <= {32, 64, 128, 256, 512, 1024, 2048}
+    tuned = st.intersection_area(pairs)
+    st.close()
+    scale = np.maximum(base, 1e-300)
+    assert np.all(np.abs(tuned - base) <= 1e-9 * scale + 1e-12)
+    sel = _checkable(S, T, pairs)
+    check(S, T, pairs[sel], tuned[sel])
