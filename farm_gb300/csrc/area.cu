@@ -117,8 +117,35 @@ __device__ void for_candidate_edges(const StoreView &sv, const PolyHdr &O, doubl
     const uint8_t *st = sv.status + O.st;
     const uint32_t *off = sv.offset + O.off;
     const uint2 *seq = sv.seq + O.seq;
-    for (int y = sy; y <= ey; y++)
-        for (int x = sx; x <= ex; x++) {
+    for (int y = sy; y <= ey; y++) {
+        // only the columns the segment spans within rows y-1 .. y+1, one more
+        // on either side: every pixel within a pixel of the segment's path,
+        // which holds every edge of O that the segment crosses (an edge is
+        // listed in each pixel it passes through, or, where the reference's
+        // walk cuts a grid corner, in the diagonal neighbours)
+        int xa = sx, xb = ex;
+        if (y1 != y0) {
+            const double ylo = O.mbr[1] + (double)(y - 1) * O.step_y, yhi = O.mbr[1] + (double)(y + 2) * O.step_y;
+            double ta = (ylo - y0) / (y1 - y0), tb = (yhi - y0) / (y1 - y0);
+            if (ta > tb) {
+                const double tmp = ta;
+                ta = tb;
+                tb = tmp;
+            }
+            ta = ta < 0 ? 0 : ta;
+            tb = tb > 1 ? 1 : tb;
+            if (ta > tb) continue;
+            double xa_ = x0 + ta * (x1 - x0), xb_ = x0 + tb * (x1 - x0);
+            if (xa_ > xb_) {
+                const double tmp = xa_;
+                xa_ = xb_;
+                xb_ = tmp;
+            }
+            const int ca = offset_x(O.mbr, O.step_x, O.dimx, xa_) - 1, cb = offset_x(O.mbr, O.step_x, O.dimx, xb_) + 1;
+            xa = ca > sx ? ca : sx;
+            xb = cb < ex ? cb : ex;
+        }
+        for (int x = xa; x <= xb; x++) {
             uint32_t pid = (uint32_t)(y * O.dimx + x);
             if (show_status(st[pid], cc) != 1) continue;
             for (uint32_t q = off[pid]; q < off[pid + 1]; q++) {
@@ -126,10 +153,31 @@ __device__ void for_candidate_edges(const StoreView &sv, const PolyHdr &O, doubl
                 for (uint32_t k = 0; k < sq.y; k++) f(sq.x + k);
             }
         }
+    }
 }
 
 // Crossing parameter t of segment p -> p + d with edge e of ring r, in [0, 1)
 // on both (half-open, so a crossing at a shared vertex counts once).
+// FP32 rejection ahead of crossing(): edge A->B lies strictly on one side of
+// the line through P->Q, or P->Q strictly on one side of the line through
+// A->B, by a margin of 1e-6 (~17 u32) times the orientation products'
+// magnitudes. That is far above the rounding of this test (~4 u32) and of
+// crossing()'s FP64 arithmetic, so such segments cannot cross and crossing()
+// would return false as well; only the candidates near a crossing pay for
+// FP64, which on GB300 issues at 1/64 of the FP32 rate.
+__device__ __forceinline__ bool apart32(float2 P, float2 Q, float2 A, float2 B) {
+    const float ex = Q.x - P.x, ey = Q.y - P.y;
+    const float ax = A.x - P.x, ay = A.y - P.y, bx = B.x - P.x, by = B.y - P.y;
+    const float oa = ex * ay - ey * ax, ob = ex * by - ey * bx;
+    const float ma = 1e-6f * (fabsf(ex * ay) + fabsf(ey * ax)), mb = 1e-6f * (fabsf(ex * by) + fabsf(ey * bx));
+    if ((oa > ma && ob > mb) || (oa < -ma && ob < -mb)) return true;
+    const float gx = B.x - A.x, gy = B.y - A.y;
+    const float px = P.x - A.x, py = P.y - A.y, qx = Q.x - A.x, qy = Q.y - A.y;
+    const float op = gx * py - gy * px, oq = gx * qy - gy * qx;
+    const float mp = 1e-6f * (fabsf(gx * py) + fabsf(gy * px)), mq = 1e-6f * (fabsf(gx * qy) + fabsf(gy * qx));
+    return (op > mp && oq > mq) || (op < -mp && oq < -mq);
+}
+
 __device__ __forceinline__ bool crossing(double px, double py, double dx, double dy, const float2 *r, uint32_t e,
                                          double ox, double oy, double &t, double &den) {
     float2 a = r[e], b = r[e + 1];
@@ -203,7 +251,9 @@ __global__ void __launch_bounds__(256) k_area(const StoreView sv, AreaArgs a) {
                     bool slow = false;
                     for_candidate_edges(sv, O, P.x, P.y, Q.x, Q.y, cc, [&](uint32_t f) {
                         double t, den;
-                        if (slow || !crossing(px, py, dx, dy, orr, f, ox, oy, t, den)) return;
+                        if (slow || apart32(P, Q, orr[f], orr[f + 1]) ||
+                            !crossing(px, py, dx, dy, orr, f, ox, oy, t, den))
+                            return;
                         for (int q = 0; q < ns; q++)
                             if (seen[q] == f) return;
                         if (ns == kMaxCross) {
@@ -225,7 +275,9 @@ __global__ void __launch_bounds__(256) k_area(const StoreView sv, AreaArgs a) {
                         bool full = false;
                         for_candidate_edges(sv, O, P.x, P.y, Q.x, Q.y, cc, [&](uint32_t f) {
                             double t, den;
-                            if (full || !crossing(px, py, dx, dy, orr, f, ox, oy, t, den)) return;
+                            if (full || apart32(P, Q, orr[f], orr[f + 1]) ||
+                                !crossing(px, py, dx, dy, orr, f, ox, oy, t, den))
+                                return;
                             uint32_t h = (f * 2654435761u) & (kHashSlots - 1);
                             while (table[h] != 0xFFFFFFFFu) {
                                 if (table[h] == f) return;
@@ -250,7 +302,9 @@ __global__ void __launch_bounds__(256) k_area(const StoreView sv, AreaArgs a) {
                         for_candidate_edges(sv, O, P.x, P.y, Q.x, Q.y, cc, [&](uint32_t f) {
                             uint64_t mine = pos++;
                             double t, den;
-                            if (!crossing(px, py, dx, dy, orr, f, ox, oy, t, den)) return;
+                            if (apart32(P, Q, orr[f], orr[f + 1]) ||
+                                !crossing(px, py, dx, dy, orr, f, ox, oy, t, den))
+                                return;
                             bool dup = false;
                             uint64_t p2 = 0;
                             for_candidate_edges(sv, O, P.x, P.y, Q.x, Q.y, cc, [&](uint32_t g) {
