@@ -395,7 +395,7 @@ static Chunks chunks_of(const farm_store *s) {
 
 // polygon orientations, computed once per rasterization, in a scratch slot of
 // their own (a captured plan holds its address)
-constexpr int kOrientSlot = 36;
+constexpr int kOrientSlot = Q_AREA_ORIENT;
 static int ensure_orient(farm_store *s, cudaStream_t st) {
     DevBuf &ori = s->s[kOrientSlot];
     if (s->orient_epoch == s->raster_epoch && ori.cap >= s->n_poly) return FARM_OK;
@@ -482,7 +482,7 @@ int intersection_area(farm_store *s, const uint32_t *pairs, uint64_t n, int mem,
         FARM_TRY(s->d_out.ensure(8 * n + 64));
         dout = s->d_out.as<double>();
     }
-    DevBuf &cnt = s->s[26], &start = s->s[27], &part = s->s[28];
+    DevBuf &cnt = s->s[Q_SCR0], &start = s->s[Q_SCR1], &part = s->s[Q_SCR2];
     FARM_TRY(cnt.ensure(8 * (n + 1) + 64));
     FARM_TRY(start.ensure(8 * (n + 1) + 64));
     FARM_TRY(s->d_counters.ensure(256));

@@ -182,6 +182,24 @@ int sm_count();
 }  // namespace farm
 
 // The store object behind the C ABI.
+namespace farm {
+// Scratch slots of farm_store::s. The rasterizer's pipeline uses slots 0-33
+// (raster.cu) only while farm_rasterize runs; the queries reuse Q_SCR0-5
+// within one call; Q_WITHIN_SUF and Q_AREA_ORIENT are theirs alone (the
+// area orientations stay valid across calls and a captured area plan holds
+// their address).
+enum ScratchSlot : int {
+    Q_SCR0 = 26,
+    Q_SCR1 = 27,
+    Q_SCR2 = 28,
+    Q_SCR3 = 29,
+    Q_SCR4 = 30,
+    Q_SCR5 = 31,
+    Q_WITHIN_SUF = 35,
+    Q_AREA_ORIENT = 36,
+};
+}  // namespace farm
+
 struct farm_store {
     cudaStream_t stream = nullptr;
     int device = 0;

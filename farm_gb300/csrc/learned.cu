@@ -105,7 +105,7 @@ int intersect_learned(farm_store *s, const uint32_t *pairs, uint64_t n, int mem,
         FARM_TRY(s->d_out.ensure(n + 64));
         dout = s->d_out.as<uint8_t>();
     }
-    DevBuf &prob = s->s[26], &up = s->s[27], &ap = s->s[28], &ao = s->s[29], &cost = s->s[30];
+    DevBuf &prob = s->s[Q_SCR0], &up = s->s[Q_SCR1], &ap = s->s[Q_SCR2], &ao = s->s[Q_SCR3], &cost = s->s[Q_SCR4];
     FARM_TRY(prob.ensure(4 * n + 64));
     FARM_TRY(up.ensure(16 * n + 64));
     FARM_TRY(ap.ensure(16 * n + 64));

@@ -601,7 +601,7 @@ int farm_mlp_train(farm_store *s, const uint32_t *d_pairs, const uint8_t *d_labe
     if (!m->ready) FARM_TRY(farm_mlp_init(s, seed));
     cudaStream_t st = s->stream;
     const uint64_t rows_all = pad128(n);
-    DevBuf &Xall = s->s[26], &perm = s->s[27], &yb = s->s[28];
+    DevBuf &Xall = s->s[Q_SCR0], &perm = s->s[Q_SCR1], &yb = s->s[Q_SCR2];
     FARM_TRY(Xall.ensure(2 * rows_all * kInPad));
     k_features<<<gbm(32 * rows_all), 256, 0, st>>>(s->view(), d_pairs, n, rows_all, s->n_side[0],
                                                    Xall.as<__nv_bfloat16>());

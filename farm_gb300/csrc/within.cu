@@ -684,7 +684,7 @@ static int within_round(farm_store *s, const uint32_t *dpairs, uint64_t n, uint8
     StoreView sv = s->view();
     const uint64_t bw = (cap_pix >> 5) + 1;
     const uint64_t words = 2 * (bw + 2ull * cap_pix);
-    DevBuf &scr = s->s[26], &cand = s->s[27], &tmp = s->s[28], &first = s->s[29];
+    DevBuf &scr = s->s[Q_SCR0], &cand = s->s[Q_SCR1], &tmp = s->s[Q_SCR2], &first = s->s[Q_SCR3];
     FARM_TRY(scr.ensure(4 * words * (uint64_t)nwarps + 64));
     FARM_CUDA(cudaMemsetAsync(scr.p, 0, 4 * words * (uint64_t)nwarps, st));
     FARM_TRY(cand.ensure(sizeof(WCand) * cand_cap + 64));
@@ -731,7 +731,7 @@ static int within_round(farm_store *s, const uint32_t *dpairs, uint64_t n, uint8
         ra.cand = cand.as<WCand>();
         ra.ncand = nc;
         ra.first = first.as<uint64_t>();
-        DevBuf &suf = s->s[35];
+        DevBuf &suf = s->s[Q_WITHIN_SUF];
         FARM_TRY(suf.ensure(8 * nc + 64));
         k_cand_sufmin<<<sm_count() * 8, 256, 0, st>>>(cand.as<WCand>(), nc, first.as<uint64_t>(), dout, n,
                                                       suf.as<double>());
@@ -816,7 +816,7 @@ int within(farm_store *s, const uint32_t *pairs, uint64_t n, double distance, in
         FARM_CUDA(cudaMemcpyAsync(hc, ctr, 16, cudaMemcpyDeviceToHost, stream));
         FARM_CUDA(cudaStreamSynchronize(stream));
         if (hc[1] == 0) break;
-        DevBuf &rp = s->s[30], &ro = s->s[31];
+        DevBuf &rp = s->s[Q_SCR4], &ro = s->s[Q_SCR5];
         FARM_TRY(rp.ensure((8 + 8) * hc[1] + 64));
         FARM_TRY(ro.ensure(hc[1] + 64));
         uint32_t *rpairs = rp.as<uint32_t>();
