@@ -1080,25 +1080,35 @@ __global__ void k_clipx(const StoreView sv, const PolyHdr *__restrict__ hdr, con
     }
 }
 
-__global__ void k_ptbits(const float2 *__restrict__ pt, uint64_t n, uint64_t *__restrict__ bits,
-                         uint32_t *__restrict__ idx) {
+// Dedup key of clip point k: (column, 16-bit hash of its bits). After a
+// stable sort by it, bit-identical points of a column share a run, in clip
+// order; hash collisions only lengthen runs.
+__global__ void k_ptbits(const float2 *__restrict__ pt, const uint64_t *__restrict__ col, uint64_t n,
+                         uint64_t *__restrict__ key, uint32_t *__restrict__ idx) {
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
-        bits[k] = pt_bits(pt[k]);
+        uint64_t b = pt_bits(pt[k]);
+        b ^= b >> 33;
+        b *= 0xff51afd7ed558ccdull;
+        b ^= b >> 29;
+        key[k] = (col[k] << 16) | (b & 0xFFFFull);
         idx[k] = (uint32_t)k;
     }
 }
 
-// After sorting by (column, bits, position): a non-first element of a run of
-// bit-identical points is dropped (MyPolygon.h:49-58 keeps a point only if no
+// A point with an earlier bit-identical point in its (column, hash) run is a
+// later copy, which MyPolygon.h:49-58 drops (it keeps a point only if no
 // earlier kept point equals it). This holds for small points too: a later
 // bitwise copy equals the earlier copy, and if that copy was itself dropped,
 // the kept point that equalled it equals the later copy as well.
-__global__ void k_dup_large(const uint64_t *__restrict__ col, const uint32_t *__restrict__ pos,
-                            const float2 *__restrict__ pt, uint64_t n, uint8_t *__restrict__ drop) {
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
-        if (k > 0 && col[k - 1] == col[k]) {
-            uint32_t me = pos[k];
-            if (pt_bits(pt[pos[k - 1]]) == pt_bits(pt[me])) drop[me] = 1;
+__global__ void k_dup_hash(const uint64_t *__restrict__ key, const uint32_t *__restrict__ pos,
+                           const float2 *__restrict__ pt, uint64_t n, uint8_t *__restrict__ drop) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t me = pt_bits(pt[pos[i]]), kk = key[i];
+        for (uint64_t j = i; j > 0 && key[j - 1] == kk; j--) {
+            if (pt_bits(pt[pos[j - 1]]) == me) {
+                drop[pos[i]] = 1;
+                break;
+            }
         }
     }
 }
@@ -1470,11 +1480,6 @@ __global__ void k_err_reduce(const PolyHdr *__restrict__ hdr, uint32_t npoly, in
         if (hdr[p].err) atomicMin(out, hdr[p].err);
 }
 
-__global__ void k_gather_u64(const uint64_t *src, const uint32_t *idx, uint64_t n, uint64_t *out) {
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
-        out[k] = src[idx[k]];
-}
-
 // ------------------------------------------------------------ host ----
 
 template <typename F>
@@ -1752,31 +1757,24 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
         FARM_TRY(sort_pairs(s, xkey, xkey_s, reinterpret_cast<uint64_t *>(xpt), reinterpret_cast<uint64_t *>(xpt_s),
                             nX, colbits));
     }
-    // duplicates: sort (bits, position), then stable by column
+    // duplicates: one stable sort by (column, 16-bit hash of the bits), then
+    // a backward scan of each run
     FARM_TRY(s->s[S_HKEY].ensure(8 * nX + 16));
     FARM_TRY(s->s[S_HVAL].ensure(8 * nX + 16));
-    FARM_TRY(s->s[S_VNKEY].ensure(8 * nX + 16));
-    FARM_TRY(s->s[S_VNVAL].ensure(8 * nX + 16));
     FARM_TRY(s->s[S_CFROM].ensure(4 * nX + 16));
     FARM_TRY(s->s[S_CTO].ensure(4 * nX + 16));
-    FARM_TRY(s->s[S_CEDGE].ensure(4 * nX + 16));
     FARM_TRY(s->s[S_SEQW].ensure(nX + 32 + 8 * (nX + 1) * 2));
     uint64_t *bits = s->s[S_HKEY].as<uint64_t>(), *bits_s = s->s[S_HVAL].as<uint64_t>();
-    uint64_t *ck = s->s[S_VNKEY].as<uint64_t>(), *ck_s = s->s[S_VNVAL].as<uint64_t>();
     uint32_t *pos = s->s[S_CFROM].as<uint32_t>(), *pos_s = s->s[S_CTO].as<uint32_t>();
-    uint32_t *pos2 = s->s[S_CEDGE].as<uint32_t>();
     uint8_t *drop = s->s[S_SEQW].as<uint8_t>();
     uint64_t *keptscan = reinterpret_cast<uint64_t *>(drop + ((nX + 16 + 7) & ~7ull));
     uint64_t *kept64 = keptscan + (nX + 1);
     FARM_CUDA(cudaMemsetAsync(drop, 0, nX + 1, st));
     if (nX) {
-        k_ptbits<<<gb(nX), 256, 0, st>>>(xpt_s, nX, bits, pos);
+        k_ptbits<<<gb(nX), 256, 0, st>>>(xpt_s, xkey_s, nX, bits, pos);
         L++;
-        FARM_TRY(sort_pairs(s, bits, bits_s, pos, pos_s, nX, 64));
-        k_gather_u64<<<gb(nX), 256, 0, st>>>(xkey_s, pos_s, nX, ck);
-        L++;
-        FARM_TRY(sort_pairs(s, ck, ck_s, pos_s, pos2, nX, colbits));
-        k_dup_large<<<gb(nX), 256, 0, st>>>(ck_s, pos2, xpt_s, nX, drop);
+        FARM_TRY(sort_pairs(s, bits, bits_s, pos, pos_s, nX, colbits + 16));
+        k_dup_hash<<<gb(nX), 256, 0, st>>>(bits_s, pos_s, xpt_s, nX, drop);
         L++;
     }
     // column starts (the points are sorted by column)
