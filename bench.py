@@ -140,13 +140,12 @@ def build_workload(seed: int, strip: int, n_strips: int, vpr: int):
     targets straddling a strip boundary are rasterized in two steps."""
     import torch
     from farm_gb300 import polygons as P
+    from farm_gb300 import shard
 
     L = calibrate_domain(seed)
     prm = star_params(L)
     log(f"domain side {L:.2f}")
-    w = L / n_strips
-    cs = P.centres(prm, seed, N_SRC)
-    s_idx = np.nonzero((cs[:, 0] >= strip * w) & (cs[:, 0] < (strip + 1) * w))[0].astype(np.uint64)
+    s_idx = shard.strip_sources(P.centres(prm, seed, N_SRC), strip, n_strips, L)
 
     def gen_pinned(seed_, idx):
         counts = P.vertex_counts(prm, seed_, idx)
@@ -160,10 +159,7 @@ def build_workload(seed: int, strip: int, n_strips: int, vpr: int):
     S, S_off_t, S_xy_t = gen_pinned(seed, s_idx)
     ms = S.mbrs()
     log(f"strip {strip}/{n_strips}: {S.n} sources, {S.total} vertices")
-    ct = P.centres(prm, seed + 1, N_TGT)
-    ext = EXTENT_RADII * ct[:, 2]
-    xlo, xhi = ms[:, 0].min(), ms[:, 2].max()
-    t_idx = np.nonzero((ct[:, 0] + ext >= xlo) & (ct[:, 0] - ext <= xhi))[0].astype(np.uint64)
+    t_idx = shard.strip_targets(ms, P.centres(prm, seed + 1, N_TGT), EXTENT_RADII)
     T, T_off_t, T_xy_t = gen_pinned(seed + 1, t_idx)
     pairs = P.mbr_join(ms, T.mbrs())
     log(f"targets: {T.n} ({T.total} vertices, {len(np.unique(pairs[:, 1]))} with candidates); "
@@ -411,12 +407,16 @@ def run_ours(args) -> dict:
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from farm_gb300 import shard
     from farm_gb300.engine import Store
 
     dev = torch.device("cuda", local)
     store = Store()
     learned_train = train_scorer(args, store, dev) if args.learned else None
-    W = build_workload(args.seed, rank % args.strips, args.strips, args.vpr)
+    mine = shard.strips_of_rank(rank, world, args.strips)
+    if not mine:
+        raise SystemExit(f"{world} ranks need at least {world} strips (--strips {args.strips})")
+    W = build_workload(args.seed, mine[0], args.strips, args.vpr)
     S, T, pairs = W["S"], W["T"], W["pairs"]
     S_off_t, S_xy_t, T_off_t, T_xy_t = W["pinned"]
     d = {k: v.to(dev) for k, v in (("so", S_off_t), ("sx", S_xy_t), ("to", T_off_t), ("tx", T_xy_t))}
@@ -483,15 +483,7 @@ def run_ours(args) -> dict:
     store.event_record(3)
     ms_e2e = store.event_elapsed(2, 3)
     t_e2e = ms_e2e / 1000.0
-    if world > 1:
-        tt = torch.tensor([t_dev, t_e2e], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_dev, t_e2e = tt.tolist()
-        npairs = torch.tensor([len(pairs)], device=dev, dtype=torch.float64)
-        dist.all_reduce(npairs)
-        total_pairs = float(npairs.item())
-    else:
-        total_pairs = float(len(pairs))
+    t_dev, t_e2e, total_pairs = shard.reduce_job(t_dev, t_e2e, len(pairs), device=dev)
     value = total_pairs * args.steps / t_dev
     e2e_value = total_pairs * args.steps / t_e2e
     rl = rooflines(store.raster_totals(), last, len(pairs), stage, args.steps)
