@@ -50,6 +50,8 @@ def declare(lib):
     if hasattr(lib, "farm_within"):
         lib.farm_within.argtypes = [vp, vp, C.c_uint64, C.c_double, C.c_int, C.c_int, C.c_int, vp, u64p,
                                     C.POINTER(Stats)]
+    lib.farm_within_mode.argtypes = [vp, vp, C.c_uint64, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, vp, u64p,
+                                     C.POINTER(Stats)]
     if hasattr(lib, "farm_intersection_area"):
         lib.farm_intersection_area.argtypes = [vp, vp, C.c_uint64, C.c_int, vp, C.POINTER(Stats)]
     lib.farm_raster_fetch.argtypes = [vp, C.c_int, C.c_uint64, C.POINTER(RasterView), u8p, u32p, u32p, u32p, f64p,

@@ -669,6 +669,28 @@ __global__ void k_scatter_retry(const uint8_t *__restrict__ rout, const uint64_t
         out[ridx[k]] = rout[k];
 }
 
+// Within "-a" (query_within_polygon.cu:332-375): a pair the descent left
+// undecided is within when one of its surviving finest pixel pairs has
+// apxDist = minDist + mean (maxDist - minDist) <= the distance, in float.
+// mean is (1.0 - pf / category_count) * 0.5 with both operands 8-bit
+// integers (:352), so the quotient is 0 and mean is 0.5; 0.5 (max - min) is
+// exact in float, so contracting the sum into an FMA rounds the same.
+__global__ void k_within_apx(const WCand *__restrict__ c, uint64_t nc, const uint8_t *__restrict__ out, double thr,
+                             uint8_t *__restrict__ hit) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nc; k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t p = c[k].pair;
+        if (out[p] != W_REFINE) continue;
+        const float lo = (float)c[k].lo, hi = (float)c[k].hi;
+        const float apx = lo + 0.5f * (hi - lo);
+        if ((double)apx <= thr) hit[p] = 1;
+    }
+}
+
+__global__ void k_within_apx_final(const uint8_t *__restrict__ hit, uint64_t n, uint8_t *__restrict__ out) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
+        if (out[k] == W_REFINE) out[k] = hit[k] ? W_TRUE : W_FALSE;
+}
+
 static unsigned gbw(uint64_t n) {
     uint64_t g = (n + 255) / 256;
     uint64_t cap = 32ull * sm_count();
@@ -678,8 +700,8 @@ static unsigned gbw(uint64_t n) {
 
 // One descend + sort + refine round over n device pairs with out in device memory.
 static int within_round(farm_store *s, const uint32_t *dpairs, uint64_t n, uint8_t *dout, double thr, int geo,
-                        uint64_t tgt_base, uint32_t cap_pix, int nwarps, uint64_t cand_cap, farm_stats *acc,
-                        int &launches) {
+                        int mode, uint64_t tgt_base, uint32_t cap_pix, int nwarps, uint64_t cand_cap,
+                        farm_stats *acc, int &launches) {
     cudaStream_t st = s->stream;
     StoreView sv = s->view();
     const uint64_t bw = (cap_pix >> 5) + 1;
@@ -714,7 +736,15 @@ static int within_round(farm_store *s, const uint32_t *dpairs, uint64_t n, uint8
     uint64_t nc = hc[1] < cand_cap ? hc[1] : cand_cap;
     acc->border_pairs += hc[3];
     acc->in_hits += hc[2];  // candidate pixel pairs
-    if (nc) {
+    if (nc && mode == FARM_MODE_APPROX) {
+        // no order and no refinement: one pass over the candidates
+        FARM_TRY(first.ensure(n + 64));
+        uint8_t *hit = first.as<uint8_t>();
+        FARM_CUDA(cudaMemsetAsync(hit, 0, n, st));
+        k_within_apx<<<gbw(nc), 256, 0, st>>>(cand.as<WCand>(), nc, dout, thr, hit);
+        k_within_apx_final<<<gbw(n), 256, 0, st>>>(hit, n, dout);
+        launches += 2;
+    } else if (nc) {
         // order by pair, then the reference's tuple (Ideal.cpp:2612)
         size_t bytes = 0;
         FARM_CUDA(cub::DeviceMergeSort::SortKeys(nullptr, bytes, cand.as<WCand>(), (int64_t)nc, WCandLess(), st));
@@ -752,8 +782,12 @@ static int within_round(farm_store *s, const uint32_t *dpairs, uint64_t n, uint8
     return FARM_OK;
 }
 
-int within(farm_store *s, const uint32_t *pairs, uint64_t n, double distance, int geography, int self, int mem,
-           uint8_t *out, uint64_t *found, farm_stats *st) {
+int within(farm_store *s, const uint32_t *pairs, uint64_t n, double distance, int geography, int self, int mode,
+           int mem, uint8_t *out, uint64_t *found, farm_stats *st) {
+    if (mode != FARM_MODE_EXACT && mode != FARM_MODE_APPROX) {
+        set_error("farm_within: mode must be FARM_MODE_EXACT or FARM_MODE_APPROX");
+        return FARM_EINVAL;
+    }
     if (!s->rasterized || !s->ropts.hierarchy) {
         set_error("farm_within: rasterize with hierarchy first");
         return FARM_EINVAL;
@@ -803,8 +837,8 @@ int within(farm_store *s, const uint32_t *pairs, uint64_t n, double distance, in
     const uint64_t words = 2 * (((cap >> 5) + 1) + 2ull * cap);
     while (nwarps > 64 && 4ull * words * (uint64_t)nwarps > freeb / 4) nwarps /= 2;
     uint64_t cand_cap = 1ull << 24;
-    if (n) FARM_TRY(within_round(s, dpairs, n, dout, distance, geography, tgt_base, cap, nwarps, cand_cap, &acc,
-                                 launches));
+    if (n) FARM_TRY(within_round(s, dpairs, n, dout, distance, geography, mode, tgt_base, cap, nwarps, cand_cap,
+                                 &acc, launches));
     // pairs whose candidates did not fit: gather and rerun with a larger buffer
     for (int round = 0; round < 8 && n; round++) {
         FARM_TRY(s->d_counters.ensure(256));
@@ -826,8 +860,8 @@ int within(farm_store *s, const uint32_t *pairs, uint64_t n, double distance, in
         launches++;
         cand_cap *= 4;
         int rw = nwarps > 256 ? 256 : nwarps;
-        FARM_TRY(within_round(s, rpairs, hc[1], ro.as<uint8_t>(), distance, geography, tgt_base, cap, rw, cand_cap,
-                              &acc, launches));
+        FARM_TRY(within_round(s, rpairs, hc[1], ro.as<uint8_t>(), distance, geography, mode, tgt_base, cap, rw,
+                              cand_cap, &acc, launches));
         k_scatter_retry<<<gbw(hc[1]), 256, 0, stream>>>(ro.as<uint8_t>(), ridx, hc[1], dout);
         launches++;
     }
@@ -873,5 +907,16 @@ extern "C" int farm_within(farm_store *s, const uint32_t *pairs, uint64_t n, dou
         set_error("invalid arguments to farm_within");
         return FARM_EINVAL;
     }
-    return within(s, pairs, n, distance, geography, target_is_source, mem, out, found, st);
+    return within(s, pairs, n, distance, geography, target_is_source, FARM_MODE_EXACT, mem, out, found, st);
+}
+
+extern "C" int farm_within_mode(farm_store *s, const uint32_t *pairs, uint64_t n, double distance, int geography,
+                                int target_is_source, int mode, int mem, uint8_t *out, uint64_t *found,
+                                farm_stats *st) {
+    using namespace farm;
+    if (!s || (n && !pairs)) {
+        set_error("invalid arguments to farm_within_mode");
+        return FARM_EINVAL;
+    }
+    return within(s, pairs, n, distance, geography, target_is_source, mode, mem, out, found, st);
 }

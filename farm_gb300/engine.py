@@ -130,7 +130,9 @@ class Store:
         self.last_stats = stats_dict(st)
         return out, found.value
 
-    def within(self, pairs, distance: float = 10.0, geography: bool = True, self_join: bool = False, out=None):
+    def within(self, pairs, distance: float = 10.0, geography: bool = True, self_join: bool = False, out=None,
+               mode: int = MODE_EXACT):
+        """Ideal::within per pair; mode MODE_APPROX is the reference's within -a rule."""
         n = pairs.shape[0]
         pp, mem = _addr(pairs)
         if out is None:
@@ -138,8 +140,8 @@ class Store:
         po, mo = _addr(out)
         found = C.c_uint64(0)
         st = Stats()
-        check_gpu(self._lib.farm_within(self._h, pp, n, float(distance), int(geography), int(self_join), mem, po,
-                                        C.byref(found), C.byref(st)))
+        check_gpu(self._lib.farm_within_mode(self._h, pp, n, float(distance), int(geography), int(self_join),
+                                             int(mode), mem, po, C.byref(found), C.byref(st)))
         self.last_stats = stats_dict(st)
         return out, found.value
 

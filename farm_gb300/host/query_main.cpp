@@ -1,7 +1,7 @@
 // Drop-in query programs for FARM's polygon-join path on one GB300:
 //
 //   intersect       -s S.dt -t T.dt -r [-g] [-a] [-v vpr] [-w classes] [-b batch] [-n threads]
-//   within_polygon  -s S.dt -r -h [-g] [-d km] [-v vpr] [-w classes] [-b batch] [-n threads]
+//   within_polygon  -s S.dt -r -h [-g] [-a] [-d km] [-v vpr] [-w classes] [-b batch] [-n threads]
 //   intersection    -s S.dt -t T.dt -r [-g] [-v vpr] [-w classes] [-b batch] [-n threads]
 //
 // One binary; the program is chosen by the name it is invoked under (the
@@ -92,7 +92,8 @@ void usage() {
             "  --help                     produce help message\n"
             "  -r [ --rasterize ]         partition with rasterization\n"
             "  -g [ --gpu ]               query with gpu\n"
-            "  -a [ --approximation ]     use approximation (intersect: the fill-ratio heuristic)\n"
+            "  -a [ --approximation ]     use approximation (intersect: the fill-ratio heuristic;\n"
+            "                             within_polygon: the pixel-pair midpoint distance)\n"
             "  -h [ --hierachy ]          partition with hierarchical grid\n"
             "  -s [ --source ] arg        path to the source\n"
             "  -t [ --target ] arg        path to the target\n"
@@ -252,9 +253,10 @@ int main(int argc, char **argv) {
                   "farm_intersect");
         } else if (a.kind == K_WITHIN) {
             out.resize(n);
-            check(farm_within(st, pairs.data() + 2 * i, n, (double)a.within_distance, 1, 1, FARM_MEM_HOST,
-                              out.data(), &f, nullptr),
-                  "farm_within");
+            check(farm_within_mode(st, pairs.data() + 2 * i, n, (double)a.within_distance, 1, 1,
+                                   a.approximation ? FARM_MODE_APPROX : FARM_MODE_EXACT, FARM_MEM_HOST, out.data(),
+                                   &f, nullptr),
+                  "farm_within_mode");
         } else {
             area.resize(n);
             check(farm_intersection_area(st, pairs.data() + 2 * i, n, FARM_MEM_HOST, area.data(), nullptr),

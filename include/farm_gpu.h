@@ -120,6 +120,14 @@ int farm_intersect_filter(farm_store *s, const uint32_t *d_pairs, uint64_t n, ui
 int farm_within(farm_store *s, const uint32_t *pairs, uint64_t n, double distance, int geography,
                 int target_is_source, int mem, uint8_t *out, uint64_t *found, farm_stats *st);
 
+/* farm_within with a mode: FARM_MODE_EXACT (= farm_within) or FARM_MODE_APPROX,
+ * the reference's within "-a" rule (query_within_polygon.cu:332-375, :721-742):
+ * a pair the hierarchical descent leaves undecided is within when one of its
+ * finest surviving BORDER pixel pairs has min + 0.5 (max - min) <= distance
+ * (float), with no refinement. Other modes are FARM_EINVAL. */
+int farm_within_mode(farm_store *s, const uint32_t *pairs, uint64_t n, double distance, int geography,
+                     int target_is_source, int mode, int mem, uint8_t *out, uint64_t *found, farm_stats *st);
+
 /* FP64 area of source[p.s] ∩ target[p.t] for n pairs (out: n doubles). The
  * reference stops before computing it (Ideal.cpp:1683); this is the project's
  * boundary-integral formulation. */

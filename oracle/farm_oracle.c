@@ -1315,15 +1315,12 @@ static int wcand_cmp(const void *a, const void *b) {
 
 static uint8_t layer_status(const fo_raster *r, uint32_t li, int id) { return r->status[r->layers[li].offset + (uint32_t)id]; }
 
-/* Ideal.cpp:2475-2643 */
-int fo_within(const fo_raster *s, const float *sring, const fo_raster *t, const float *tring, double distance,
-              int geography, fo_counters *c) {
+/* The hierarchical descent of Ideal::within (Ideal.cpp:2478-2584): 1 or 0
+ * when it decides the pair, 2 with the finest surviving pixel pairs left in
+ * qa / qb (caller frees), or FO_ENOMEM. */
+static int within_descend(const fo_raster *s, const fo_raster *t, double distance, int geography, iv_t *qa_out,
+                          iv_t *qb_out) {
     const int cc = 16;
-    fo_counters local = {0};
-    if (!c) c = &local;
-    memset(c, 0, sizeof *c);
-    if (!s->num_layers || !t->num_layers) return FO_EINVAL; /* the reference needs -h here */
-    const pt *sp = (const pt *)sring, *tp = (const pt *)tring;
     uint32_t s_level = s->num_layers - 1, t_level = t->num_layers - 1;
     /* queue of pixel pairs, as two parallel arrays */
     iv_t qa = {0}, qb = {0};
@@ -1434,6 +1431,23 @@ int fo_within(const fo_raster *s, const float *sring, const fo_raster *t, const 
         free(qb.v);
         return err ? FO_ENOMEM : result;
     }
+    *qa_out = qa;
+    *qb_out = qb;
+    return 2;
+}
+
+/* Ideal.cpp:2475-2643 */
+int fo_within(const fo_raster *s, const float *sring, const fo_raster *t, const float *tring, double distance,
+              int geography, fo_counters *c) {
+    const int cc = 16;
+    fo_counters local = {0};
+    if (!c) c = &local;
+    memset(c, 0, sizeof *c);
+    if (!s->num_layers || !t->num_layers) return FO_EINVAL; /* the reference needs -h here */
+    const pt *sp = (const pt *)sring, *tp = (const pt *)tring;
+    iv_t qa = {0}, qb = {0};
+    int result = within_descend(s, t, distance, geography, &qa, &qb);
+    if (result != 2) return result;
     size_t nc = qa.n;
     wcand_t *cand = (wcand_t *)malloc((nc ? nc : 1) * sizeof(wcand_t));
     if (!cand) {
@@ -1499,6 +1513,32 @@ int fo_within(const fo_raster *s, const float *sring, const fo_raster *t, const 
     free(suffix);
     free(cand);
     return result == 1 ? 1 : 0;
+}
+
+/* The reference's within "-a" (query_within_polygon.cu:332-375, :721-742) on
+ * the descent above: an undecided pair is within when one of its finest
+ * surviving pixel pairs has apxDist = minDist + mean (maxDist - minDist) <=
+ * distance, all in float. mean = (1.0 - pf / category_count) * 0.5 divides two
+ * 8-bit integers (:352), so it is 0.5 for every pf. */
+int fo_within_heuristic(const fo_raster *s, const fo_raster *t, double distance, int geography) {
+    if (!s->num_layers || !t->num_layers) return FO_EINVAL;
+    iv_t qa = {0}, qb = {0};
+    int result = within_descend(s, t, distance, geography, &qa, &qb);
+    if (result != 2) return result;
+    const fo_layer *sl = &s->layers[s->num_layers - 1], *tl = &t->layers[t->num_layers - 1];
+    result = 0;
+    for (size_t k = 0; k < qa.n && !result; k++) {
+        double b1[4], b2[4];
+        layer_box(sl, qa.v[k], b1);
+        layer_box(tl, qb.v[k], b2);
+        const float lo = (float)box_distance(b1, b2, geography);
+        const float hi = (float)box_max_distance(b1, b2, geography);
+        const float apx = lo + 0.5f * (hi - lo); /* 0.5 (hi - lo) is exact: an FMA rounds the same */
+        if ((double)apx <= distance) result = 1;
+    }
+    free(qa.v);
+    free(qb.v);
+    return result;
 }
 
 /* ------------------------------------------------ point in polygon ------ */

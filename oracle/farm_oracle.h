@@ -88,6 +88,10 @@ int fo_intersect_heuristic(const fo_raster *s, const fo_raster *t);
 int fo_within(const fo_raster *s, const float *sring, const fo_raster *t, const float *tring,
               double distance, int geography, fo_counters *c);
 
+/* The reference's within "-a" rule (query_within_polygon.cu:332-375) on the
+ * descent of fo_within: 1 / 0, no refinement. */
+int fo_within_heuristic(const fo_raster *s, const fo_raster *t, double distance, int geography);
+
 /* Single segment predicates (geometry_computation.h:190-221, :49-89). */
 int fo_segment_intersect(const float *a, const float *b, const float *c, const float *d);
 double fo_point_to_segment_distance(const float *p, const float *p1, const float *p2, int geography);

@@ -57,6 +57,7 @@ def lib() -> C.CDLL:
         L.fo_intersect_heuristic.argtypes = [C.POINTER(FoRaster), C.POINTER(FoRaster)]
         L.fo_within.argtypes = [C.POINTER(FoRaster), fp, C.POINTER(FoRaster), fp, C.c_double, C.c_int,
                                 C.POINTER(FoCounters)]
+        L.fo_within_heuristic.argtypes = [C.POINTER(FoRaster), C.POINTER(FoRaster), C.c_double, C.c_int]
         L.fo_segment_intersect.argtypes = [fp, fp, fp, fp]
         L.fo_point_to_segment_distance.argtypes = [fp, fp, fp, C.c_int]
         L.fo_point_to_segment_distance.restype = C.c_double
@@ -149,6 +150,14 @@ def within(rs: Raster, rt: Raster, distance: float = 10.0, geography: bool = Tru
     if v < 0:
         raise RuntimeError(f"oracle within failed: {v}")
     return (bool(v), c) if counters else bool(v)
+
+
+def within_heuristic(rs: Raster, rt: Raster, distance: float = 10.0, geography: bool = True) -> bool:
+    """The reference's within -a rule on the hierarchical descent (no refinement)."""
+    v = lib().fo_within_heuristic(C.byref(rs.r), C.byref(rt.r), float(distance), int(geography))
+    if v < 0:
+        raise RuntimeError(f"oracle within heuristic failed: {v}")
+    return bool(v)
 
 
 def intersection_area(a: np.ndarray, b: np.ndarray) -> float:

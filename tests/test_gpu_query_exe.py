@@ -45,3 +45,19 @@ def test_query_program_batches_add_up(gpu_lib):
     s, t = str(GOLDEN / f"{case['name']}_S.dt"), str(GOLDEN / f"{case['name']}_T.dt")
     whole = run("intersect", "-s", s, "-t", t, "-r", "-g", "-v", str(case["vpr"]))
     assert run("intersect", "-s", s, "-t", t, "-r", "-g", "-v", str(case["vpr"]), "-b", "37") == whole
+
+
+def test_within_program_approximation(gpu_lib, tmp_path):
+    # within_polygon -a counts the pairs the within -a rule accepts
+    import numpy as np
+    from farm_gb300 import polygons as P
+    from oracle import oracle as O
+    S = P.generate(P.StarParams(dom_hi=2.0, r_lo=0.005, r_hi=0.06, n_hi=1500), 45, 220)
+    f = tmp_path / "s.dt"
+    S.write_dt(str(f))
+    pairs = P.mbr_join(S.mbrs(), S.mbrs(), expand=10.0, geography=True, skip_same=True)
+    RS = O.rasterize_set(S, 10, True)
+    expected = sum(O.within_heuristic(RS[s], RS[t]) for s, t in pairs)
+    assert run("within_polygon", "-s", str(f), "-r", "-h", "-g", "-a", "-v", "10") == expected
+    assert run("within_polygon", "-s", str(f), "-r", "-h", "-g", "-v", "10") == sum(
+        O.within(RS[s], RS[t]) for s, t in pairs)

@@ -77,3 +77,30 @@ def test_gpu_within_planar_large_coordinates(gpu_lib):
     assert np.array_equal(out, exp), f"{int((out != exp).sum())} of {len(exp)} differ"
     assert 0 < found < len(pairs)
     assert stats["fp64_rechecks"] > 0
+
+
+@pytest.mark.parametrize("vpr,seed,self_join", [(10, 45, True), (4, 46, False)])
+def test_gpu_within_approx_matches_oracle(gpu_lib, vpr, seed, self_join):
+    # the reference's within -a rule (no refinement) against the oracle's
+    # restatement of it on the same descent, pair for pair; pixels small
+    # against the 10 km distance, where the rule is informative
+    prm = P.StarParams(dom_hi=2.0, r_lo=0.005, r_hi=0.06, n_hi=1500)
+    S = P.generate(prm, seed, 220)
+    T = S if self_join else P.generate(prm, seed + 7, 260)
+    pairs = np.ascontiguousarray(P.mbr_join(S.mbrs(), T.mbrs(), expand=10.0, geography=True, skip_same=self_join),
+                                 dtype=np.uint32)
+    st = Store()
+    st.load_sets(S, None if self_join else T)
+    st.rasterize(vpr=vpr, hierarchy=True)
+    out, found = st.within(pairs, distance=10.0, self_join=self_join, mode=1)
+    stats = st.last_stats
+    exact, _ = st.within(pairs, distance=10.0, self_join=self_join)
+    st.close()
+    assert stats["segment_tests"] == 0
+    RS = O.rasterize_set(S, vpr, True)
+    RT = RS if self_join else O.rasterize_set(T, vpr, True)
+    exp = np.array([O.within_heuristic(RS[s], RT[t]) for s, t in pairs], np.uint8)
+    assert np.array_equal(out, exp), f"{int((out != exp).sum())} of {len(exp)} differ"
+    assert found == int(exp.sum()) and 0 < found < len(pairs)
+    # a heuristic: most pairs agree with the exact answer
+    assert (out == exact).mean() > 0.9

@@ -72,3 +72,27 @@ def test_segment_predicates_known_answers(host_built):
     p, a, b = (np.array(v, np.float32) for v in ((0, 1), (-1, 0), (1, 0)))
     d = L.fo_point_to_segment_distance(p.ctypes.data_as(fp), a.ctypes.data_as(fp), b.ctypes.data_as(fp), 0)
     assert d == 1.0
+
+
+
+def test_oracle_within_heuristic_small_pixels(host_built):
+    # The within -a rule has no CPU counterpart in the reference to pin it
+    # to. It judges a pixel pair by the midpoint of its box distance range, so
+    # it is only informative where pixels are small against the distance:
+    # polygons of 0.5-7 km radius and 10 km here, where it agrees with the
+    # exact answer on most pairs (with 40 km pixels it says false throughout).
+    from farm_gb300 import polygons as P
+    prm = P.StarParams(dom_hi=2.0, r_lo=0.005, r_hi=0.06, n_hi=1500)
+    S = P.generate(prm, 45, 220)
+    pairs = P.mbr_join(S.mbrs(), S.mbrs(), expand=10.0, geography=True, skip_same=True)
+    RS = O.rasterize_set(S, 10, True)
+    exact = np.array([O.within(RS[s], RS[t]) for s, t in pairs], np.int64)
+    apx = np.array([O.within_heuristic(RS[s], RS[t]) for s, t in pairs], np.int64)
+    assert (apx == exact).mean() > 0.9
+    assert 0 < apx.sum() < len(apx)
+    # far apart: the descent prunes every pixel pair; the same polygon: the
+    # descent decides it
+    sq = np.array([[0, 0], [0.01, 0], [0.01, 0.01], [0, 0.01], [0, 0]], np.float32)
+    a, b = O.Raster(sq, 10, True), O.Raster(sq + np.float32(1.0), 10, True)
+    assert not O.within_heuristic(a, b) and not O.within(a, b)
+    assert O.within_heuristic(a, a) and O.within(a, a)
