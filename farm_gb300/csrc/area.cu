@@ -59,12 +59,11 @@ struct AreaArgs {
     uint64_t cap_items;          // partial's capacity
     double *partial;             // per item
     const int8_t *orient;        // per polygon: +1 counter-clockwise, -1 clockwise
+    const uint64_t *ep_off;      // per ring position: first entry of the edge's pixel list
+    const uint32_t *ep_pix;      // pixels listing each edge (edge -> pixel CSR)
     unsigned long long *next;
-    unsigned long long *overflow;  // [0] crossings beyond the fast path, [1] items beyond cap_items
+    unsigned long long *overflow;  // [0] unused, [1] items beyond cap_items
 };
-
-constexpr int kMaxCross = 48;     // crossings per edge deduplicated in registers
-constexpr int kHashSlots = 1024;  // beyond that, a per-lane hash set (half full at most)
 
 __device__ __forceinline__ double cross2(double ax, double ay, double bx, double by) { return ax * by - ay * bx; }
 
@@ -101,59 +100,135 @@ __device__ bool pip_raster(const StoreView &sv, const PolyHdr &H, double px, dou
     return odd;  // past the raster: outside, so the crossings decide
 }
 
-// Edges of polygon O that may cross segment (P, Q): sequences of O's BORDER
-// pixels in a one-pixel-padded window around the segment. Calls f(edge index).
+// The pixels of polygon O searched for edges that may cross segment
+// (x0, y0) -> (x1, y1): rows sy..ey of a one-pixel-padded window, and in each
+// row the columns row_cols gives.
+struct SegWin {
+    double x0, y0, x1, y1;
+    int sx, ex, sy, ey;
+};
+
+__device__ __forceinline__ bool seg_window(const PolyHdr &O, double x0, double y0, double x1, double y1, SegWin &w) {
+    const double mnx = fmin(x0, x1), mxx = fmax(x0, x1), mny = fmin(y0, y1), mxy = fmax(y0, y1);
+    if (mxx < O.mbr[0] || mnx > O.mbr[2] || mxy < O.mbr[1] || mny > O.mbr[3]) return false;
+    w.x0 = x0;
+    w.y0 = y0;
+    w.x1 = x1;
+    w.y1 = y1;
+    w.sx = offset_x(O.mbr, O.step_x, O.dimx, mnx) - 1;
+    w.ex = offset_x(O.mbr, O.step_x, O.dimx, mxx) + 1;
+    w.sy = offset_y(O.mbr, O.step_y, O.dimy, mny) - 1;
+    w.ey = offset_y(O.mbr, O.step_y, O.dimy, mxy) + 1;
+    w.sx = w.sx < 0 ? 0 : w.sx;
+    w.sy = w.sy < 0 ? 0 : w.sy;
+    w.ex = w.ex >= O.dimx ? O.dimx - 1 : w.ex;
+    w.ey = w.ey >= O.dimy ? O.dimy - 1 : w.ey;
+    return true;
+}
+
+// Columns xa..xb of window row y; false when the row holds none. Only the
+// columns the segment spans within rows y-1 .. y+1, one more on either side:
+// every pixel within a pixel of the segment's path, which holds every edge of
+// O that the segment crosses (an edge is listed in each pixel it passes
+// through, or, where the reference's walk cuts a grid corner, in the diagonal
+// neighbours).
+// Both for_candidate_edges and first_listing call it, so its products and sums
+// are explicit roundings: no contraction may differ between the two.
+__device__ __forceinline__ bool row_cols(const PolyHdr &O, const SegWin &w, int y, int &xa, int &xb) {
+    xa = w.sx;
+    xb = w.ex;
+    if (w.y1 != w.y0) {
+        const double ylo = __dadd_rn(O.mbr[1], __dmul_rn((double)(y - 1), O.step_y));
+        const double yhi = __dadd_rn(O.mbr[1], __dmul_rn((double)(y + 2), O.step_y));
+        const double dy = __dsub_rn(w.y1, w.y0);
+        double ta = __ddiv_rn(__dsub_rn(ylo, w.y0), dy), tb = __ddiv_rn(__dsub_rn(yhi, w.y0), dy);
+        if (ta > tb) {
+            const double tmp = ta;
+            ta = tb;
+            tb = tmp;
+        }
+        ta = ta < 0 ? 0 : ta;
+        tb = tb > 1 ? 1 : tb;
+        if (ta > tb) return false;
+        const double dx = __dsub_rn(w.x1, w.x0);
+        double xa_ = __dadd_rn(w.x0, __dmul_rn(ta, dx)), xb_ = __dadd_rn(w.x0, __dmul_rn(tb, dx));
+        if (xa_ > xb_) {
+            const double tmp = xa_;
+            xa_ = xb_;
+            xb_ = tmp;
+        }
+        const int ca = offset_x(O.mbr, O.step_x, O.dimx, xa_) - 1, cb = offset_x(O.mbr, O.step_x, O.dimx, xb_) + 1;
+        xa = ca > w.sx ? ca : w.sx;
+        xb = cb < w.ex ? cb : w.ex;
+    }
+    return true;
+}
+
+// Edges of polygon O listed by the BORDER pixels of window w, row by row, left
+// to right, sequence by sequence. Calls f(pixel, first column of its row,
+// sequence index, edge index); an edge listed by several of these pixels (or
+// sequences) comes once per listing.
 template <typename F>
-__device__ void for_candidate_edges(const StoreView &sv, const PolyHdr &O, double x0, double y0, double x1, double y1,
-                                    int cc, F f) {
-    double mnx = fmin(x0, x1), mxx = fmax(x0, x1), mny = fmin(y0, y1), mxy = fmax(y0, y1);
-    if (mxx < O.mbr[0] || mnx > O.mbr[2] || mxy < O.mbr[1] || mny > O.mbr[3]) return;
-    int sx = offset_x(O.mbr, O.step_x, O.dimx, mnx) - 1, ex = offset_x(O.mbr, O.step_x, O.dimx, mxx) + 1;
-    int sy = offset_y(O.mbr, O.step_y, O.dimy, mny) - 1, ey = offset_y(O.mbr, O.step_y, O.dimy, mxy) + 1;
-    sx = sx < 0 ? 0 : sx;
-    sy = sy < 0 ? 0 : sy;
-    ex = ex >= O.dimx ? O.dimx - 1 : ex;
-    ey = ey >= O.dimy ? O.dimy - 1 : ey;
+__device__ void for_candidate_edges(const StoreView &sv, const PolyHdr &O, const SegWin &w, int cc, F f) {
     const uint8_t *st = sv.status + O.st;
     const uint32_t *off = sv.offset + O.off;
     const uint2 *seq = sv.seq + O.seq;
-    for (int y = sy; y <= ey; y++) {
-        // only the columns the segment spans within rows y-1 .. y+1, one more
-        // on either side: every pixel within a pixel of the segment's path,
-        // which holds every edge of O that the segment crosses (an edge is
-        // listed in each pixel it passes through, or, where the reference's
-        // walk cuts a grid corner, in the diagonal neighbours)
-        int xa = sx, xb = ex;
-        if (y1 != y0) {
-            const double ylo = O.mbr[1] + (double)(y - 1) * O.step_y, yhi = O.mbr[1] + (double)(y + 2) * O.step_y;
-            double ta = (ylo - y0) / (y1 - y0), tb = (yhi - y0) / (y1 - y0);
-            if (ta > tb) {
-                const double tmp = ta;
-                ta = tb;
-                tb = tmp;
-            }
-            ta = ta < 0 ? 0 : ta;
-            tb = tb > 1 ? 1 : tb;
-            if (ta > tb) continue;
-            double xa_ = x0 + ta * (x1 - x0), xb_ = x0 + tb * (x1 - x0);
-            if (xa_ > xb_) {
-                const double tmp = xa_;
-                xa_ = xb_;
-                xb_ = tmp;
-            }
-            const int ca = offset_x(O.mbr, O.step_x, O.dimx, xa_) - 1, cb = offset_x(O.mbr, O.step_x, O.dimx, xb_) + 1;
-            xa = ca > sx ? ca : sx;
-            xb = cb < ex ? cb : ex;
-        }
+    for (int y = w.sy; y <= w.ey; y++) {
+        int xa, xb;
+        if (!row_cols(O, w, y, xa, xb)) continue;
         for (int x = xa; x <= xb; x++) {
-            uint32_t pid = (uint32_t)(y * O.dimx + x);
+            const uint32_t pid = (uint32_t)(y * O.dimx + x);
             if (show_status(st[pid], cc) != 1) continue;
             for (uint32_t q = off[pid]; q < off[pid + 1]; q++) {
-                uint2 sq = seq[q];
-                for (uint32_t k = 0; k < sq.y; k++) f(sq.x + k);
+                const uint2 sq = seq[q];
+                for (uint32_t k = 0; k < sq.y; k++) f(pid, xa, q, sq.x + k);
             }
         }
     }
+}
+
+// Whether the listing of edge f met in pixel pid (sequence q, its row's first
+// column xa) is the first listing of f that for_candidate_edges meets: no
+// BORDER pixel of the window earlier in its order (an earlier row, or the same
+// row further left) lists f, and no earlier sequence of pid holds it. Each
+// edge that crosses the segment is then counted exactly once, whatever the
+// number of pixels listing it, with no per-edge memory. The other pixels
+// listing f come from the edge -> pixel index, and window membership from the
+// same row_cols the enumeration runs, so both agree to the bit.
+__device__ bool first_listing(const StoreView &sv, const PolyHdr &O, const SegWin &w, int cc, const uint64_t *ep_off,
+                              const uint32_t *ep_pix, uint32_t pid, int xa, uint32_t q, uint32_t f) {
+    const uint64_t g = O.ring + f;
+    const int py = (int)(pid / (uint32_t)O.dimx), px = (int)pid - py * O.dimx;
+    int cy = -1, cxa = 0, cxb = -1;
+    bool cok = false;
+    int self = 0;
+    for (uint64_t i = ep_off[g]; i < ep_off[g + 1]; i++) {
+        const uint32_t r = ep_pix[i];
+        if (r == pid) {
+            self++;
+            continue;
+        }
+        const int ry = (int)(r / (uint32_t)O.dimx), rx = (int)r - ry * O.dimx;
+        if (ry > py || (ry == py && rx > px) || ry < w.sy) continue;  // later, or above the window
+        if (show_status(sv.status[O.st + r], cc) != 1) continue;
+        if (ry == py) {
+            if (rx >= xa) return false;
+            continue;
+        }
+        if (ry != cy) {
+            cok = row_cols(O, w, ry, cxa, cxb);
+            cy = ry;
+        }
+        if (cok && rx >= cxa && rx <= cxb) return false;
+    }
+    if (self > 1) {  // pid holds f in more than one sequence: the first counts
+        const uint2 *seq = sv.seq + O.seq;
+        for (uint32_t p = sv.offset[O.off + pid]; p < q; p++) {
+            const uint2 sq = seq[p];
+            if (f >= sq.x && f - sq.x < sq.y) return false;
+        }
+    }
+    return true;
 }
 
 // Crossing parameter t of segment p -> p + d with edge e of ring r, in [0, 1)
@@ -244,77 +319,18 @@ __global__ void __launch_bounds__(256) k_area(const StoreView sv, AreaArgs a) {
                 py = (double)P.y - oy;
                 dx = (double)Q.x - P.x;
                 dy = (double)Q.y - P.y;
-                if (dx != 0 || dy != 0) {
-                    // an edge of O may be listed by several pixels: count it once
-                    uint32_t seen[kMaxCross];
-                    int ns = 0;
-                    bool slow = false;
-                    for_candidate_edges(sv, O, P.x, P.y, Q.x, Q.y, cc, [&](uint32_t f) {
+                SegWin w;
+                if ((dx != 0 || dy != 0) && seg_window(O, P.x, P.y, Q.x, Q.y, w)) {
+                    // an edge of O may be listed by several pixels: count it
+                    // at its first listing only
+                    for_candidate_edges(sv, O, w, cc, [&](uint32_t pid, int xa, uint32_t q, uint32_t f) {
                         double t, den;
-                        if (slow || apart32(P, Q, orr[f], orr[f + 1]) ||
-                            !crossing(px, py, dx, dy, orr, f, ox, oy, t, den))
+                        if (apart32(P, Q, orr[f], orr[f + 1]) || !crossing(px, py, dx, dy, orr, f, ox, oy, t, den))
                             return;
-                        for (int q = 0; q < ns; q++)
-                            if (seen[q] == f) return;
-                        if (ns == kMaxCross) {
-                            slow = true;
-                            return;
-                        }
-                        seen[ns++] = f;
+                        if (!first_listing(sv, O, w, cc, a.ep_off, a.ep_pix, pid, xa, q, f)) return;
                         nc++;
                         sum_t += (osign * den > 0) ? t : -t;
                     });
-                    if (slow) {
-                        // many crossings: an open-addressing set of the edges
-                        // already counted (per lane, local memory)
-                        nc = 0;
-                        sum_t = 0;
-                        uint32_t table[kHashSlots];
-                        for (int q = 0; q < kHashSlots; q++) table[q] = 0xFFFFFFFFu;
-                        int used = 0;
-                        bool full = false;
-                        for_candidate_edges(sv, O, P.x, P.y, Q.x, Q.y, cc, [&](uint32_t f) {
-                            double t, den;
-                            if (full || apart32(P, Q, orr[f], orr[f + 1]) ||
-                                !crossing(px, py, dx, dy, orr, f, ox, oy, t, den))
-                                return;
-                            uint32_t h = (f * 2654435761u) & (kHashSlots - 1);
-                            while (table[h] != 0xFFFFFFFFu) {
-                                if (table[h] == f) return;
-                                h = (h + 1) & (kHashSlots - 1);
-                            }
-                            if (++used > kHashSlots / 2) {
-                                full = true;
-                                return;
-                            }
-                            table[h] = f;
-                            nc++;
-                            sum_t += (osign * den > 0) ? t : -t;
-                        });
-                        slow = full;
-                    }
-                    if (slow) {
-                        // beyond the set's capacity: find earlier listings of the
-                        // same edge by re-enumeration
-                        nc = 0;
-                        sum_t = 0;
-                        uint64_t pos = 0;
-                        for_candidate_edges(sv, O, P.x, P.y, Q.x, Q.y, cc, [&](uint32_t f) {
-                            uint64_t mine = pos++;
-                            double t, den;
-                            if (apart32(P, Q, orr[f], orr[f + 1]) ||
-                                !crossing(px, py, dx, dy, orr, f, ox, oy, t, den))
-                                return;
-                            bool dup = false;
-                            uint64_t p2 = 0;
-                            for_candidate_edges(sv, O, P.x, P.y, Q.x, Q.y, cc, [&](uint32_t g) {
-                                if (p2++ < mine && g == f) dup = true;
-                            });
-                            if (dup) return;
-                            nc++;
-                            sum_t += (osign * den > 0) ? t : -t;
-                        });
-                    }
                 }
             }
             // parity of crossings of earlier edges of the chunk
@@ -343,6 +359,33 @@ __global__ void k_orient(const StoreView sv, uint32_t npoly, int8_t *__restrict_
             sa += cross2((double)r[k].x - ox, (double)r[k].y - oy, (double)r[k + 1].x - ox, (double)r[k + 1].y - oy);
         for (int o = 16; o; o >>= 1) sa += __shfl_xor_sync(0xffffffffu, sa, o);
         if (lane == 0) out[p] = sa >= 0 ? 1 : -1;
+    }
+}
+
+// Edge -> pixel index of every rasterized polygon, by ring position: pass 0
+// counts the pixels listing each edge, pass 1 writes them (in any order). One
+// warp per polygon, lanes over its pixels.
+template <bool kFill>
+__global__ void k_edge_pix(const StoreView sv, uint32_t npoly, const uint64_t *__restrict__ ep_off,
+                           unsigned long long *__restrict__ cnt, uint32_t *__restrict__ ep_pix) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t p = w0; p < npoly; p += nw) {
+        const PolyHdr &h = sv.hdr[p];
+        if (h.err) continue;
+        const uint32_t *off = sv.offset + h.off;
+        const uint2 *seq = sv.seq + h.seq;
+        for (uint32_t pid = lane; pid < h.P; pid += 32) {
+            for (uint32_t q = off[pid]; q < off[pid + 1]; q++) {
+                const uint2 sq = seq[q];
+                for (uint32_t k = 0; k < sq.y; k++) {
+                    if (sq.x + k > h.nv) break;  // past the polygon's ring slots (never, by construction)
+                    const uint64_t g = h.ring + sq.x + k;
+                    const unsigned long long at = atomicAdd(&cnt[g], 1ull);
+                    if (kFill) ep_pix[ep_off[g] + at] = pid;
+                }
+            }
+        }
     }
 }
 
@@ -409,6 +452,38 @@ static int ensure_orient(farm_store *s, cudaStream_t st) {
     return FARM_OK;
 }
 
+// The edge -> pixel index, built once per rasterization in scratch slots of
+// its own (a captured plan holds their addresses). Counts go through Q_SCR3.
+static int ensure_edge_pix(farm_store *s, cudaStream_t st) {
+    if (s->edgepix_epoch == s->raster_epoch) return FARM_OK;
+    const uint64_t nring = s->n_edges + 2 * s->n_poly;
+    DevBuf &off = s->s[Q_AREA_EPOFF], &pix = s->s[Q_AREA_EPPIX], &cnt = s->s[Q_SCR3];
+    FARM_TRY(off.ensure(8 * (nring + 1) + 64));
+    FARM_TRY(cnt.ensure(8 * (nring + 1) + 64));
+    unsigned long long *c = cnt.as<unsigned long long>();
+    uint64_t *o = off.as<uint64_t>();
+    unsigned blocks = (unsigned)((32ull * s->n_poly + 255) / 256);
+    if (blocks > 8192) blocks = 8192;
+    if (!blocks) blocks = 1;
+    FARM_CUDA(cudaMemsetAsync(c, 0, 8 * (nring + 1), st));
+    k_edge_pix<false><<<blocks, 256, 0, st>>>(s->view(), (uint32_t)s->n_poly, nullptr, c, nullptr);
+    FARM_CUDA(cudaGetLastError());
+    size_t bytes = 0;
+    FARM_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, bytes, (const uint64_t *)c, o, (int64_t)(nring + 1)));
+    FARM_TRY(s->cub_tmp.ensure(bytes + 64));
+    FARM_CUDA(cub::DeviceScan::ExclusiveSum(s->cub_tmp.p, bytes, (const uint64_t *)c, o, (int64_t)(nring + 1), st));
+    uint64_t total = 0;
+    FARM_CUDA(cudaMemcpyAsync(&total, o + nring, 8, cudaMemcpyDeviceToHost, st));
+    FARM_CUDA(cudaStreamSynchronize(st));
+    FARM_TRY(pix.ensure(4 * total + 64));
+    FARM_CUDA(cudaMemsetAsync(c, 0, 8 * (nring + 1), st));
+    k_edge_pix<true><<<blocks, 256, 0, st>>>(s->view(), (uint32_t)s->n_poly, o, c, pix.as<uint32_t>());
+    FARM_CUDA(cudaGetLastError());
+    s->launches += 3;
+    s->edgepix_epoch = s->raster_epoch;
+    return FARM_OK;
+}
+
 // Buffers of one area pass. Everything the kernels need to know about the
 // batch (pair count, item count) is read on the device, so the same sequence
 // can be captured once in a CUDA graph and replayed for any batch that fits.
@@ -444,8 +519,18 @@ static int area_items(farm_store *s, const AreaBufs &b, cudaStream_t st) {
 
 static int area_compute(farm_store *s, const AreaBufs &b, cudaStream_t st) {
     FARM_CUDA(cudaMemsetAsync(b.ctr, 0, 24, st));
-    AreaArgs aa{b.pairs, b.n, s->n_side[0], b.chunks, b.start, b.cap_items, b.partial, s->s[kOrientSlot].as<int8_t>(),
-                b.ctr, b.ctr + 1};
+    AreaArgs aa{b.pairs,
+                b.n,
+                s->n_side[0],
+                b.chunks,
+                b.start,
+                b.cap_items,
+                b.partial,
+                s->s[kOrientSlot].as<int8_t>(),
+                s->s[Q_AREA_EPOFF].as<uint64_t>(),
+                s->s[Q_AREA_EPPIX].as<uint32_t>(),
+                b.ctr,
+                b.ctr + 1};
     k_area<<<sm_count() * 8, 256, 0, st>>>(s->view(), aa);
     FARM_CUDA(cudaGetLastError());
     unsigned blocks = (unsigned)((b.cap_pairs + 255) / 256);
@@ -490,6 +575,7 @@ int intersection_area(farm_store *s, const uint32_t *pairs, uint64_t n, int mem,
     uint64_t *dn = reinterpret_cast<uint64_t *>(ctr + 8);
     FARM_CUDA(cudaMemcpyAsync(dn, &n, 8, cudaMemcpyHostToDevice, stream));
     FARM_TRY(ensure_orient(s, stream));
+    FARM_TRY(ensure_edge_pix(s, stream));
     AreaBufs b{};
     b.pairs = dpairs;
     b.n = dn;
@@ -574,6 +660,7 @@ extern "C" int farm_area_plan_create(farm_store *s, uint64_t max_pairs, uint64_t
     FARM_TRY(area_checks(s, "farm_area_plan_create"));
     cudaStream_t st = s->stream;
     FARM_TRY(ensure_orient(s, st));
+    FARM_TRY(ensure_edge_pix(s, st));
     farm_area_plan *p = new farm_area_plan();
     p->s = s;
     p->cap_pairs = max_pairs;

@@ -197,6 +197,8 @@ enum ScratchSlot : int {
     Q_SCR5 = 31,
     Q_WITHIN_SUF = 35,
     Q_AREA_ORIENT = 36,
+    Q_AREA_EPOFF = 37,  // area: edge -> pixel index offsets (per ring position)
+    Q_AREA_EPPIX = 38,  // area: edge -> pixel index entries
 };
 }  // namespace farm
 
@@ -227,6 +229,7 @@ struct farm_store {
     void *mlp = nullptr;    // learned scorer state (mlp.cu)
     uint64_t raster_epoch = 0;     // bumped by every rasterization (plans check it)
     uint64_t orient_epoch = ~0ull;  // raster_epoch the cached orientations belong to
+    uint64_t edgepix_epoch = ~0ull; // raster_epoch the area's edge -> pixel index belongs to
     int32_t area_chunk[32] = {};   // edges per area item by size bucket (0: the default 256)
     farm::StoreView view() const;
 };
