@@ -127,6 +127,9 @@ def log(msg: str) -> None:
 # every vertex of a generated polygon lies within this many mean radii of its
 # centre unless its lognormal factor exceeds exp(0.3 * 6.5) (probability ~4e-11)
 EXTENT_RADII = math.exp(0.3 * 6.5)
+# configuration-4 sample for the area block: polygons per pool and domain side
+AREA_POOL = 1500
+AREA_SIDE = 40.0
 
 
 def build_workload(seed: int, strip: int, n_strips: int, vpr: int):
@@ -518,9 +521,62 @@ def run_ours(args) -> dict:
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(W, args, budget_s=args.cpu_seconds, threads=1, gpu_out=h_out.numpy())
     store.close()
+    if rank == 0 and args.area_pairs > 0:
+        result["area"] = area_eval(args)
     if world > 1:
         dist.destroy_process_group()
     return result if rank == 0 else None
+
+
+def area_eval(args) -> dict:
+    """Intersection area (stage d) on a configuration-4 sample, through a captured area plan.
+
+    Configuration 4 mixes tiny and huge polygons (vertex counts log-uniform
+    8..200,000 on each side) in one launch. The sample draws two pools of
+    polygons from the star generator and takes args.area_pairs of their
+    MBR-overlapping pairs at random, in one batch: one CUDA-graph launch of
+    the persistent work-stealing kernel per pass. value = pairs / device time
+    of one pass, timed with CUDA events (median of three passes after one
+    warm-up pass)."""
+    from farm_gb300 import polygons as P
+    from farm_gb300.engine import Store
+
+    t0 = time.time()
+    prm = P.StarParams(dom_lo=0.0, dom_hi=AREA_SIDE, r_lo=0.05, r_hi=2.0, n_lo=8, n_hi=200_000, sigma=0.3)
+    S = P.generate(prm, args.seed + 400, AREA_POOL)
+    T = P.generate(prm, args.seed + 401, AREA_POOL)
+    pairs = P.mbr_join(S.mbrs(), T.mbrs())
+    rng = np.random.default_rng(args.seed + 402)
+    pairs = np.ascontiguousarray(pairs[rng.permutation(len(pairs))][:args.area_pairs])
+    es = np.diff(S.off.astype(np.int64))[pairs[:, 0]]
+    et = np.diff(T.off.astype(np.int64))[pairs[:, 1]]
+    st = Store()
+    st.load_sets(S, T)
+    st.rasterize(vpr=10, strict=False)
+    ras_s = st.raster_totals()["ms_total"] / 1000.0
+    # items per pair at the smallest chunk the autotuner may pick (32 edges)
+    plan = st.area_plan(max_pairs=len(pairs), max_items=int(((es + 31) // 32 + (et + 31) // 32).sum()) + 64)
+    plan.run(pairs)
+    warm_ms = plan.last_stats["ms_total"]
+    ms = []
+    for _ in range(3):
+        out = plan.run(pairs)
+        ms.append(plan.last_stats["ms_total"])
+    plan.close()
+    st.close()
+    med = float(np.median(ms))
+    log(f"area: {len(pairs)} pairs, {int(es.sum() + et.sum())} edges, {med:.1f} ms per pass "
+        f"(warm-up {warm_ms:.1f} ms), {time.time() - t0:.1f} s wall")
+    return {"metric": "intersection-area pairs/sec, configuration-4 sample", "value": len(pairs) / (med / 1000.0),
+            "unit": "pairs/s", "ms_per_pass": med, "passes": 3, "warmup_passes": 1, "dtype": "f64",
+            "edges_per_s": float(es.sum() + et.sum()) / (med / 1000.0),
+            "config": {"workload": f"{len(pairs)} MBR-overlapping pairs drawn at random from two pools of "
+                                   f"{AREA_POOL} star polygons, vertex counts log-uniform 8..200,000, radii "
+                                   f"0.05..2 in a {AREA_SIDE:g} x {AREA_SIDE:g} domain; one batch, one "
+                                   "graph launch per pass", "vpr": 10, "pairs": len(pairs),
+                       "edges_in_pairs": int(es.sum() + et.sum()), "largest_pair_edges": int((es + et).max()),
+                       "pool_vertices": int(S.total + T.total), "seed": args.seed + 400},
+            "nonzero_areas": int((out > 0).sum()), "rasterize_s": ras_s}
 
 
 def _oracle_chunk(job):
@@ -636,6 +692,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--ref-step-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--area-pairs", type=int, default=0,
+                    help="pairs of the configuration-4 area sample (0 = skip the area block; one pass over "
+                         "1,000 pairs takes ~47 s)")
     ap.add_argument("--no-learned", dest="learned", action="store_false",
                     help="skip training and evaluating the learned scorer")
     ap.add_argument("--learned-pairs", type=int, default=2_000_000, help="training + held-out pairs")

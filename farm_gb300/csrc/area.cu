@@ -164,18 +164,29 @@ __device__ __forceinline__ bool row_cols(const PolyHdr &O, const SegWin &w, int 
     return true;
 }
 
+// Column ranges of the first kRowCache rows of a window, kept as the
+// enumeration computes them (an empty row is stored as xa > xb), so that
+// first_listing reads them instead of recomputing.
+constexpr int kRowCache = 16;
+struct RowCache {
+    int2 r[kRowCache];
+};
+
 // Edges of polygon O listed by the BORDER pixels of window w, row by row, left
 // to right, sequence by sequence. Calls f(pixel, first column of its row,
 // sequence index, edge index); an edge listed by several of these pixels (or
-// sequences) comes once per listing.
+// sequences) comes once per listing. Pixel ids grow in this order (row-major).
 template <typename F>
-__device__ void for_candidate_edges(const StoreView &sv, const PolyHdr &O, const SegWin &w, int cc, F f) {
+__device__ void for_candidate_edges(const StoreView &sv, const PolyHdr &O, const SegWin &w, int cc, RowCache &rc,
+                                    F f) {
     const uint8_t *st = sv.status + O.st;
     const uint32_t *off = sv.offset + O.off;
     const uint2 *seq = sv.seq + O.seq;
     for (int y = w.sy; y <= w.ey; y++) {
         int xa, xb;
-        if (!row_cols(O, w, y, xa, xb)) continue;
+        const bool ok = row_cols(O, w, y, xa, xb);
+        if (y - w.sy < kRowCache) rc.r[y - w.sy] = ok ? make_int2(xa, xb) : make_int2(1, 0);
+        if (!ok) continue;
         for (int x = xa; x <= xb; x++) {
             const uint32_t pid = (uint32_t)(y * O.dimx + x);
             if (show_status(st[pid], cc) != 1) continue;
@@ -189,37 +200,43 @@ __device__ void for_candidate_edges(const StoreView &sv, const PolyHdr &O, const
 
 // Whether the listing of edge f met in pixel pid (sequence q, its row's first
 // column xa) is the first listing of f that for_candidate_edges meets: no
-// BORDER pixel of the window earlier in its order (an earlier row, or the same
+// BORDER pixel of the window with a smaller id (an earlier row, or the same
 // row further left) lists f, and no earlier sequence of pid holds it. Each
 // edge that crosses the segment is then counted exactly once, whatever the
-// number of pixels listing it, with no per-edge memory. The other pixels
-// listing f come from the edge -> pixel index, and window membership from the
-// same row_cols the enumeration runs, so both agree to the bit.
-__device__ bool first_listing(const StoreView &sv, const PolyHdr &O, const SegWin &w, int cc, const uint64_t *ep_off,
-                              const uint32_t *ep_pix, uint32_t pid, int xa, uint32_t q, uint32_t f) {
+// number of pixels listing it, with no per-edge memory. The pixels listing f
+// come from the edge -> pixel index (ascending ids, so the scan stops at pid),
+// and window membership from the rows the enumeration computed (or the same
+// row_cols for rows past the cache), so both agree to the bit.
+__device__ bool first_listing(const StoreView &sv, const PolyHdr &O, const SegWin &w, int cc, const RowCache &rc,
+                              const uint64_t *ep_off, const uint32_t *ep_pix, uint32_t pid, int xa, uint32_t q,
+                              uint32_t f) {
     const uint64_t g = O.ring + f;
-    const int py = (int)(pid / (uint32_t)O.dimx), px = (int)pid - py * O.dimx;
-    int cy = -1, cxa = 0, cxb = -1;
-    bool cok = false;
+    const uint32_t dimx = (uint32_t)O.dimx;
+    const int py = (int)(pid / dimx);
     int self = 0;
-    for (uint64_t i = ep_off[g]; i < ep_off[g + 1]; i++) {
+    for (uint64_t i = ep_off[g], e = ep_off[g + 1]; i < e; i++) {
         const uint32_t r = ep_pix[i];
+        if (r > pid) break;
         if (r == pid) {
             self++;
             continue;
         }
-        const int ry = (int)(r / (uint32_t)O.dimx), rx = (int)r - ry * O.dimx;
-        if (ry > py || (ry == py && rx > px) || ry < w.sy) continue;  // later, or above the window
+        const int ry = (int)(r / dimx), rx = (int)(r - (uint32_t)ry * dimx);
+        if (ry < w.sy) continue;  // above the window
         if (show_status(sv.status[O.st + r], cc) != 1) continue;
         if (ry == py) {
             if (rx >= xa) return false;
             continue;
         }
-        if (ry != cy) {
-            cok = row_cols(O, w, ry, cxa, cxb);
-            cy = ry;
+        int cxa, cxb;
+        if (ry - w.sy < kRowCache) {
+            const int2 c = rc.r[ry - w.sy];
+            cxa = c.x;
+            cxb = c.y;
+        } else if (!row_cols(O, w, ry, cxa, cxb)) {
+            continue;
         }
-        if (cok && rx >= cxa && rx <= cxb) return false;
+        if (rx >= cxa && rx <= cxb) return false;
     }
     if (self > 1) {  // pid holds f in more than one sequence: the first counts
         const uint2 *seq = sv.seq + O.seq;
@@ -322,12 +339,15 @@ __global__ void __launch_bounds__(256) k_area(const StoreView sv, AreaArgs a) {
                 SegWin w;
                 if ((dx != 0 || dy != 0) && seg_window(O, P.x, P.y, Q.x, Q.y, w)) {
                     // an edge of O may be listed by several pixels: count it
-                    // at its first listing only
-                    for_candidate_edges(sv, O, w, cc, [&](uint32_t pid, int xa, uint32_t q, uint32_t f) {
+                    // at its first listing only (tested before the FP64
+                    // crossing, which then runs once per edge pair)
+                    RowCache rc;
+                    for_candidate_edges(sv, O, w, cc, rc, [&](uint32_t pid, int xa, uint32_t q, uint32_t f) {
                         double t, den;
-                        if (apart32(P, Q, orr[f], orr[f + 1]) || !crossing(px, py, dx, dy, orr, f, ox, oy, t, den))
+                        if (apart32(P, Q, orr[f], orr[f + 1]) ||
+                            !first_listing(sv, O, w, cc, rc, a.ep_off, a.ep_pix, pid, xa, q, f) ||
+                            !crossing(px, py, dx, dy, orr, f, ox, oy, t, den))
                             return;
-                        if (!first_listing(sv, O, w, cc, a.ep_off, a.ep_pix, pid, xa, q, f)) return;
                         nc++;
                         sum_t += (osign * den > 0) ? t : -t;
                     });
@@ -385,6 +405,23 @@ __global__ void k_edge_pix(const StoreView sv, uint32_t npoly, const uint64_t *_
                     if (kFill) ep_pix[ep_off[g] + at] = pid;
                 }
             }
+        }
+    }
+}
+
+// Each edge's pixel list in ascending pixel id (insertion sort: an edge is
+// listed by at most dimx + dimy pixels, a few in the common case).
+__global__ void k_edge_pix_sort(const uint64_t *__restrict__ ep_off, uint64_t nring, uint32_t *__restrict__ ep_pix) {
+    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < nring; g += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t b = ep_off[g], e = ep_off[g + 1];
+        for (uint64_t i = b + 1; i < e; i++) {
+            const uint32_t v = ep_pix[i];
+            uint64_t j = i;
+            while (j > b && ep_pix[j - 1] > v) {
+                ep_pix[j] = ep_pix[j - 1];
+                j--;
+            }
+            ep_pix[j] = v;
         }
     }
 }
@@ -479,7 +516,11 @@ static int ensure_edge_pix(farm_store *s, cudaStream_t st) {
     FARM_CUDA(cudaMemsetAsync(c, 0, 8 * (nring + 1), st));
     k_edge_pix<true><<<blocks, 256, 0, st>>>(s->view(), (uint32_t)s->n_poly, o, c, pix.as<uint32_t>());
     FARM_CUDA(cudaGetLastError());
-    s->launches += 3;
+    unsigned sb = (unsigned)((nring + 255) / 256);
+    if (sb > 8192) sb = 8192;
+    k_edge_pix_sort<<<sb ? sb : 1, 256, 0, st>>>(o, nring, pix.as<uint32_t>());
+    FARM_CUDA(cudaGetLastError());
+    s->launches += 4;
     s->edgepix_epoch = s->raster_epoch;
     return FARM_OK;
 }

@@ -5,7 +5,7 @@
  * It replaces the reference's GPU offload entry points (src/include/Ideal.h:205-213):
  *   cuda_create_buffer / preprocess_for_gpu  -> farm_store_create + farm_store_load + farm_rasterize
  *   cuda_intersect                           -> farm_intersect
- *   cuda_within_polygon                      -> farm_within
+ *   cuda_within_polygon                      -> farm_within (farm_within_mode for -a)
  *   cuda_intersection                        -> farm_intersection_area
  *   ResetDevice                              -> (none: results are written to caller buffers)
  * and, for the CPU path it must agree with, Ideal::rasterization / Ideal::intersect /
