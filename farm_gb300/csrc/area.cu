@@ -16,7 +16,9 @@
 // Work: items are (pair, side, chunk of that side's edges), taken by persistent
 // warps from a global counter. A lane takes one edge: it finds its crossings
 // through the other polygon's raster (edge sequences of the BORDER pixels
-// around the edge), ranks them, and adds its signed inside length. Per-item
+// around the edge, each crossing edge counted at its first listing), and adds
+// its signed inside length: the leaving parameters minus the entering ones,
+// plus the tail when it ends inside. Per-item
 // partial sums are reduced per pair in a fixed order (deterministic results).
 // Coordinates are taken relative to the pair's source first vertex.
 // General position is assumed (no collinear overlaps, no crossing exactly at a
