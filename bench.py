@@ -694,7 +694,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--area-pairs", type=int, default=0,
                     help="pairs of the configuration-4 area sample (0 = skip the area block; one pass over "
-                         "1,000 pairs takes ~47 s)")
+                         "1,000 pairs takes ~13 s)")
     ap.add_argument("--no-learned", dest="learned", action="store_false",
                     help="skip training and evaluating the learned scorer")
     ap.add_argument("--learned-pairs", type=int, default=2_000_000, help="training + held-out pairs")

@@ -166,9 +166,11 @@ __device__ __forceinline__ bool row_cols(const PolyHdr &O, const SegWin &w, int 
     return true;
 }
 
-// Column ranges of the first kRowCache rows of a window, kept as the
-// enumeration computes them (an empty row is stored as xa > xb), so that
-// first_listing reads them instead of recomputing.
+// Column ranges of the last kRowCache window rows the enumeration computed,
+// in a ring indexed by row & (kRowCache - 1) (an empty row is stored as
+// xa > xb), so that first_listing reads them instead of recomputing: the
+// earlier listings of an edge that crosses the segment lie within a few rows
+// of the current one, even when the window spans hundreds of rows.
 constexpr int kRowCache = 16;
 struct RowCache {
     int2 r[kRowCache];
@@ -187,7 +189,7 @@ __device__ void for_candidate_edges(const StoreView &sv, const PolyHdr &O, const
     for (int y = w.sy; y <= w.ey; y++) {
         int xa, xb;
         const bool ok = row_cols(O, w, y, xa, xb);
-        if (y - w.sy < kRowCache) rc.r[y - w.sy] = ok ? make_int2(xa, xb) : make_int2(1, 0);
+        rc.r[y & (kRowCache - 1)] = ok ? make_int2(xa, xb) : make_int2(1, 0);
         if (!ok) continue;
         for (int x = xa; x <= xb; x++) {
             const uint32_t pid = (uint32_t)(y * O.dimx + x);
@@ -208,7 +210,7 @@ __device__ void for_candidate_edges(const StoreView &sv, const PolyHdr &O, const
 // number of pixels listing it, with no per-edge memory. The pixels listing f
 // come from the edge -> pixel index (ascending ids, so the scan stops at pid),
 // and window membership from the rows the enumeration computed (or the same
-// row_cols for rows past the cache), so both agree to the bit.
+// row_cols for rows older than the cache), so both agree to the bit.
 __device__ bool first_listing(const StoreView &sv, const PolyHdr &O, const SegWin &w, int cc, const RowCache &rc,
                               const uint64_t *ep_off, const uint32_t *ep_pix, uint32_t pid, int xa, uint32_t q,
                               uint32_t f) {
@@ -231,8 +233,8 @@ __device__ bool first_listing(const StoreView &sv, const PolyHdr &O, const SegWi
             continue;
         }
         int cxa, cxb;
-        if (ry - w.sy < kRowCache) {
-            const int2 c = rc.r[ry - w.sy];
+        if (ry > py - kRowCache) {  // still in the ring (rows sy .. py were enumerated in order)
+            const int2 c = rc.r[ry & (kRowCache - 1)];
             cxa = c.x;
             cxb = c.y;
         } else if (!row_cols(O, w, ry, cxa, cxb)) {

@@ -6,7 +6,7 @@ kernel counts a crossing only at the edge's first listing in the window's own
 enumeration order (farm_gb300/csrc/area.cu: seg_window, row_cols,
 for_candidate_edges, first_listing, k_edge_pix_sort). Here the same window
 arithmetic (IEEE double, as the kernel's explicit roundings) and the same rule,
-with a 16-row cache and row_cols past it, run over dense spiky rasters and
+with a ring of the last 16 rows and row_cols beyond it, run over dense spiky rasters and
 random segments; every edge listed in a window must be accepted exactly once.
 """
 import math
@@ -92,13 +92,13 @@ def row_cols(R, w, y):
 
 
 def enumerate_window(R, w):
-    """(pid, xa, q, f) in for_candidate_edges' order, and the row cache."""
+    """(pid, xa, q, f) in for_candidate_edges' order, each with the row ring
+    as it stood when that listing was met."""
     out, cache = [], {}
     _, _, _, _, sx, ex, sy, ey = w
     for y in range(sy, ey + 1):
         ok, xa, xb = row_cols(R, w, y)
-        if y - sy < K_ROW_CACHE:
-            cache[y - sy] = (xa, xb) if ok else (1, 0)
+        cache[y & (K_ROW_CACHE - 1)] = (xa, xb) if ok else (1, 0)
         if not ok:
             continue
         for x in range(xa, xb + 1):
@@ -108,8 +108,8 @@ def enumerate_window(R, w):
             for q in range(int(R.off[pid]), int(R.off[pid + 1])):
                 s0, ln = int(R.seq[q, 0]), int(R.seq[q, 1])
                 for k in range(ln):
-                    out.append((pid, xa, q, s0 + k))
-    return out, cache
+                    out.append((pid, xa, q, s0 + k, dict(cache)))
+    return out
 
 
 def first_listing(R, w, cache, pid, xa, q, f):
@@ -129,8 +129,8 @@ def first_listing(R, w, cache, pid, xa, q, f):
             if rx >= xa:
                 return False
             continue
-        if ry - sy < K_ROW_CACHE:
-            cxa, cxb = cache[ry - sy]
+        if ry > py - K_ROW_CACHE:
+            cxa, cxb = cache[ry & (K_ROW_CACHE - 1)]
         else:
             ok, cxa, cxb = row_cols(R, w, ry)
             if not ok:
@@ -172,12 +172,12 @@ def test_first_listing_accepts_each_listed_edge_once(host_built, seed, n_hi, vpr
             w = seg_window(R, x0, y0, x1, y1)
             if w is None:
                 continue
-            listed, cache = enumerate_window(R, w)
+            listed = enumerate_window(R, w)
             counts = {}
-            for pid, xa, q, f in listed:
+            for pid, xa, q, f, cache in listed:
                 if first_listing(R, w, cache, pid, xa, q, f):
                     counts[f] = counts.get(f, 0) + 1
-            edges = {f for _, _, _, f in listed}
+            edges = {f for _, _, _, f, _ in listed}
             assert set(counts) == edges and all(c == 1 for c in counts.values()), (k, i)
             checked += len(edges)
             multi += len(listed) - len(edges)
