@@ -44,6 +44,8 @@ RASTER_CASES = [
     ("r_cfg1_v4_h", StarParams(dom_hi=20.0), 102, 60, 4, 1),
     ("r_cfg1_v64", StarParams(dom_hi=20.0), 103, 60, 64, 0),
     ("r_small_v1", StarParams(dom_hi=5.0, r_lo=0.01, r_hi=0.5, n_lo=16, n_hi=200), 104, 60, 1, 1),
+    # the bench's -v 64 on polygons of 2k-20k vertices (below the 65,536-sequence assert)
+    ("r_big_v64", StarParams(dom_hi=30.0, n_lo=2000, n_hi=20000), 105, 10, 64, 0),
 ]
 # (name, params, seed, n_source, n_target (0 = self-join), vpr, mode)
 PAIR_CASES = [
@@ -51,6 +53,9 @@ PAIR_CASES = [
     ("p_intersect_v4", StarParams(dom_hi=20.0), 202, 50, 200, 4, "intersect"),
     ("p_within_v10", StarParams(dom_hi=20.0), 203, 260, 0, 10, "within"),
     ("p_within_v64", StarParams(dom_hi=30.0), 204, 260, 0, 64, "within"),
+    # -v 64 with configuration 2's heavy tail, cut at 20k vertices
+    ("p_intersect_v64_big", StarParams(dom_hi=12.0, n_lo=16, n_hi=20000), 205, 24, 90, 64, "intersect"),
+    ("p_within_v64_big", StarParams(dom_hi=12.0, n_lo=16, n_hi=5000), 206, 100, 0, 64, "within"),
 ]
 
 
