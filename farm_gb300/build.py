@@ -4,7 +4,7 @@
   compiled for sm_103a only.
 * ``farm_gb300/lib/libfarm_host.so`` — host services (include/farm_host.h).
 * ``farm_gb300/lib/farm_query``      — the drop-in query executable.
-* ``oracle/liboracle.so``            — the CPU restatement used as the test checker.
+* ``oracle/liboracle.so``            — the CPU restatement the tests verify results against.
 * ``oracle/_ref/*``                  — the reference's own CPU code, only where its
   source tree is present (never on a machine without it).
 

@@ -1,7 +1,7 @@
 /*
  * farm_oracle.c — CPU restatement of the FARM reference's polygon-join hot
- * path. TEST INFRASTRUCTURE ONLY (see farm_oracle.h): the checker for the
- * GPU engine, never part of it.
+ * path. TEST INFRASTRUCTURE ONLY (see farm_oracle.h): it verifies the GPU
+ * engine's results and is never part of it.
  *
  * Built with -ffp-contract=off: the reference is compiled for x86-64 without
  * -march (src/Makefile:11), so none of its multiply-adds are fused; every

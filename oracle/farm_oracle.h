@@ -1,8 +1,8 @@
 /*
  * farm_oracle.h — CPU restatement of the FARM reference's polygon-join hot
  * path, in plain C. TEST INFRASTRUCTURE ONLY: the parity tests, smoke() and
- * bench.py's CPU-baseline leg use it as the checker; the product never links,
- * loads or calls it.
+ * bench.py's CPU-baseline leg use it to verify results; the product never
+ * links, loads or calls it.
  *
  * Each function states the reference file:line it follows (paths relative to
  * the reference's src/). Behaviour is reproduced literally, including the

@@ -1,8 +1,8 @@
 """ctypes front end of the CPU oracle (oracle/farm_oracle.c).
 
 TEST INFRASTRUCTURE ONLY. Only tests/, __graft_entry__.smoke() and bench.py's
-CPU-baseline leg import this module, and only as the checker or the timed CPU
-baseline; the engine never routes through it.
+CPU-baseline leg import this module, and only to verify the engine's results or
+as the timed CPU baseline; the engine never routes through it.
 """
 from __future__ import annotations
 

@@ -2,7 +2,7 @@
 
 The fixtures were produced by compiling the reference's unmodified CPU code
 (tests/golden/make_golden.py); a match here pins the oracle that every GPU
-parity test then uses as its checker.
+parity test then compares the engine with.
 """
 import hashlib
 
