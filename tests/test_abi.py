@@ -48,3 +48,30 @@ def test_query_program_flags_without_gpu(host_built):
         assert flag in h.stderr, flag
     u = subprocess.run([str(exe), "--bogus"], capture_output=True, text=True, timeout=60)
     assert "Undefined Option!" in u.stdout
+
+
+def test_gpu_library_reports_errors_without_a_gpu(host_built):
+    """With no usable GPU the ABI returns an error code and a message; it never
+    exits, aborts or dereferences a null store."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    from farm_gb300 import build
+    build.build_cuda()
+    lib = C.CDLL(str(ROOT / "farm_gb300" / "lib" / "libfarm_gpu.so"))
+    lib.farm_last_error.restype = C.c_char_p
+    st = C.c_void_p(None)
+    rc = lib.farm_store_create(C.byref(st))
+    assert rc < 0 and not st.value
+    assert lib.farm_last_error()
+    # null stores are rejected before any device work
+    found = C.c_uint64(0)
+    for call in (lambda: lib.farm_intersect(None, None, C.c_uint64(0), 0, 0, None, C.byref(found), None),
+                 lambda: lib.farm_within_mode(None, None, C.c_uint64(0), C.c_double(10.0), 1, 1, 0, 0, None,
+                                              C.byref(found), None),
+                 lambda: lib.farm_intersection_area(None, None, C.c_uint64(0), 0, None, None)):
+        assert call() < 0
+        assert lib.farm_last_error()
