@@ -84,4 +84,6 @@ def declare(lib):
     lib.farm_event_elapsed.argtypes = [vp, C.c_int, C.c_int, f64p]
     lib.farm_store_launches.argtypes = [vp]
     lib.farm_store_launches.restype = C.c_uint64
+    lib.farm_store_device_bytes.argtypes = [vp, u64p]
+    lib.farm_probe_issue_rates.argtypes = [f64p, f64p]
 

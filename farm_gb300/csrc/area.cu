@@ -600,6 +600,7 @@ static int area_checks(farm_store *s, const char *who) {
 
 int intersection_area(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, double *out, farm_stats *st) {
     FARM_TRY(area_checks(s, "farm_intersection_area"));
+    FARM_TRY(check_pairs(s, pairs, n, mem, false, "farm_intersection_area"));
     cudaStream_t stream = s->stream;
     const uint32_t *dpairs = pairs;
     if (mem == FARM_MEM_HOST && n) {
@@ -780,6 +781,7 @@ extern "C" int farm_area_plan_run(farm_area_plan *p, const uint32_t *pairs, uint
         set_error("farm_area_plan_run: the store was reloaded or rasterized again since the plan was made");
         return FARM_EINVAL;
     }
+    FARM_TRY(check_pairs(s, pairs, n, mem, false, "farm_area_plan_run"));
     cudaStream_t st = s->stream;
     const cudaMemcpyKind k_in = mem == FARM_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
     const cudaMemcpyKind k_out = mem == FARM_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
@@ -838,6 +840,7 @@ extern "C" int farm_area_autotune(farm_store *s, const uint32_t *pairs, uint64_t
         return FARM_EINVAL;
     }
     FARM_TRY(area_checks(s, "farm_area_autotune"));
+    FARM_TRY(check_pairs(s, pairs, n, mem, false, "farm_area_autotune"));
     std::vector<uint32_t> hp(2 * n);
     if (n) {
         if (mem == FARM_MEM_HOST) {

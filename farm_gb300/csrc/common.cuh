@@ -181,6 +181,14 @@ int sm_count();
 
 }  // namespace farm
 
+struct farm_store;
+namespace farm {
+// FARM_EINVAL unless every pair's source index is below the source count and
+// its target index below the target count (the source count when self).
+// Device pairs are checked by a kernel (one synchronisation).
+int check_pairs(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, bool self, const char *who);
+}  // namespace farm
+
 // The store object behind the C ABI.
 namespace farm {
 // Scratch slots of farm_store::s. The rasterizer's pipeline uses slots 0-33
@@ -224,6 +232,7 @@ struct farm_store {
     farm::DevBuf s[40];
     farm::DevBuf cub_tmp;
     farm::DevBuf d_pairs, d_out, d_counters;
+    farm::DevBuf d_check;  // pair-index validation counter
     cudaEvent_t ev[8] = {};
     uint64_t launches = 0;  // engine kernels launched through this store
     void *mlp = nullptr;    // learned scorer state (mlp.cu)

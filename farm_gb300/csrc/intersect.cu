@@ -505,6 +505,7 @@ extern "C" int farm_intersect_filter(farm_store *s, const uint32_t *d_pairs, uin
         return FARM_EINVAL;
     }
     if (!n) return FARM_OK;
+    FARM_TRY(check_pairs(s, d_pairs, n, FARM_MEM_DEVICE, false, "farm_intersect_filter"));
     return intersect_filter(s, d_pairs, n, d_code, nullptr, reinterpret_cast<uint32_t *>(d_cost));
 }
 
@@ -515,6 +516,7 @@ extern "C" int farm_intersect(farm_store *s, const uint32_t *pairs, uint64_t n, 
         set_error("invalid arguments to farm_intersect");
         return FARM_EINVAL;
     }
+    if (s->rasterized && s->n_side[1]) FARM_TRY(check_pairs(s, pairs, n, mem, false, "farm_intersect"));
     if (mode == FARM_MODE_LEARNED) return intersect_learned(s, pairs, n, mem, out, found, st);
     if (mode == FARM_MODE_FILTER) {
         if (!s->rasterized) {
@@ -604,6 +606,8 @@ extern "C" int farm_intersect_static(farm_store *s, const uint32_t *pairs, uint6
         set_error("farm_intersect_static: no target side loaded");
         return FARM_EINVAL;
     }
+    // host-side range check of every pair before any device work
+    FARM_TRY(check_pairs(s, pairs, n, FARM_MEM_HOST, false, "farm_intersect_static"));
     int cur = 0;
     FARM_CUDA(cudaGetDevice(&cur));
     if (cur != s->device) FARM_CUDA(cudaSetDevice(s->device));

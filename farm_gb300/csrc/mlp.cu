@@ -488,6 +488,7 @@ int farm_mlp_init(farm_store *s, uint64_t seed) {
 /* Features of n candidate pairs into X (device, bf16 [n_pad x 576]). */
 int farm_mlp_features(farm_store *s, const uint32_t *d_pairs, uint64_t n, void *d_X, uint64_t rows) {
     if (!s || !s->rasterized || rows < n) return FARM_EINVAL;
+    FARM_TRY(check_pairs(s, d_pairs, n, FARM_MEM_DEVICE, false, "farm_mlp_features"));
     k_features<<<gbm(32 * rows), 256, 0, s->stream>>>(s->view(), d_pairs, n, rows, s->n_side[0],
                                                       static_cast<__nv_bfloat16 *>(d_X));
     FARM_CUDA(cudaGetLastError());
@@ -597,6 +598,7 @@ int farm_mlp_set(farm_store *s, const float *in) {
 int farm_mlp_train(farm_store *s, const uint32_t *d_pairs, const uint8_t *d_labels, uint64_t n, int epochs,
                    int batch, float lr, uint64_t seed, float *last_loss) {
     if (!s || !s->rasterized || !d_pairs || !d_labels || n == 0 || batch <= 0 || batch % 128) return FARM_EINVAL;
+    FARM_TRY(check_pairs(s, d_pairs, n, FARM_MEM_DEVICE, false, "farm_mlp_train"));
     Mlp *m = mlp_of(s);
     if (!m->ready) FARM_TRY(farm_mlp_init(s, seed));
     cudaStream_t st = s->stream;
@@ -658,6 +660,7 @@ int farm_mlp_predict(farm_store *s, const uint32_t *d_pairs, uint64_t n, float *
         set_error("no trained scorer in this store");
         return FARM_EINVAL;
     }
+    FARM_TRY(check_pairs(s, d_pairs, n, FARM_MEM_DEVICE, false, "farm_mlp_predict"));
     cudaStream_t st = s->stream;
     const uint64_t chunk = 1 << 16;
     FARM_CUDA(cudaMemsetAsync(m->err.p, 0, 4, st));

@@ -4,6 +4,7 @@
 // in a 64-bit-offset layout, and the store owns every device allocation.
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <string>
 
@@ -45,16 +46,71 @@ void DevBuf::release() {
     cap = 0;
 }
 
+// SM count of the current device, looked up once per device ordinal (hosts
+// may mix GPU models, and grids are sized from this).
 int sm_count() {
-    static int n = 0;
-    static std::once_flag once;
-    std::call_once(once, []() {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n <= 0) n = 1;
-    });
+    constexpr int kMaxDev = 64;
+    static std::atomic<int> cache[kMaxDev];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) {
+        cudaGetLastError();
+        dev = 0;
+    }
+    if (dev < kMaxDev) {
+        int c = cache[dev].load(std::memory_order_relaxed);
+        if (c > 0) return c;
+    }
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        n = 1;
+    }
+    if (dev < kMaxDev) cache[dev].store(n, std::memory_order_relaxed);
     return n;
+}
+
+// Pairs whose source index is >= n_src or target index >= n_tgt.
+__global__ void k_check_pairs(const uint32_t *__restrict__ pairs, uint64_t n, uint64_t n_src, uint64_t n_tgt,
+                              unsigned long long *__restrict__ bad) {
+    unsigned long long mine = 0;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint2 p = reinterpret_cast<const uint2 *>(pairs)[k];
+        mine += (p.x >= n_src) | (p.y >= n_tgt);
+    }
+    if (mine) atomicAdd(bad, mine);
+}
+
+int check_pairs(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, bool self, const char *who) {
+    if (!n) return FARM_OK;
+    const uint64_t n_src = s->n_side[0], n_tgt = self ? s->n_side[0] : s->n_side[1];
+    uint64_t bad = 0, first = ~0ull;
+    if (mem == FARM_MEM_HOST) {
+        for (uint64_t k = 0; k < n; k++)
+            if (pairs[2 * k] >= n_src || pairs[2 * k + 1] >= n_tgt) {
+                if (!bad) first = k;
+                bad++;
+            }
+    } else {
+        FARM_TRY(s->d_check.ensure(64));
+        unsigned long long *d = s->d_check.as<unsigned long long>();
+        FARM_CUDA(cudaMemsetAsync(d, 0, 8, s->stream));
+        unsigned blocks = grid_for(n, 256);
+        if (blocks > 8u * (unsigned)sm_count()) blocks = 8u * (unsigned)sm_count();
+        k_check_pairs<<<blocks, 256, 0, s->stream>>>(pairs, n, n_src, n_tgt, d);
+        FARM_CUDA(cudaGetLastError());
+        unsigned long long h = 0;
+        FARM_CUDA(cudaMemcpyAsync(&h, d, 8, cudaMemcpyDeviceToHost, s->stream));
+        FARM_CUDA(cudaStreamSynchronize(s->stream));
+        bad = h;
+    }
+    if (bad) {
+        std::string m = std::string(who) + ": " + std::to_string(bad) + " pair index(es) out of range (" +
+                        std::to_string(n_src) + " sources, " + std::to_string(n_tgt) + " targets)";
+        if (first != ~0ull) m += ", first at pair " + std::to_string(first);
+        set_error(m);
+        return FARM_EINVAL;
+    }
+    return FARM_OK;
 }
 
 // Copy stored rings into the padded layout: per polygon the stored vertices,
@@ -154,13 +210,28 @@ void farm_store_destroy(farm_store *s) {
     s->mlp = nullptr;
     DevBuf *bufs[] = {&s->d_xy_in, &s->d_off, &s->d_ring, &s->d_hdr, &s->d_status, &s->d_offset, &s->d_seq,
                       &s->d_hoff, &s->d_hnodes, &s->d_voff, &s->d_vnodes, &s->d_areas, &s->cub_tmp,
-                      &s->d_pairs, &s->d_out, &s->d_counters};
+                      &s->d_pairs, &s->d_out, &s->d_counters, &s->d_check};
     for (DevBuf *b : bufs) b->release();
     for (auto &b : s->s) b.release();
     for (auto &ev : s->ev)
         if (ev) cudaEventDestroy(ev);
     cudaStreamDestroy(s->stream);
     delete s;
+}
+
+int farm_store_device_bytes(farm_store *s, uint64_t *bytes) {
+    if (!s || !bytes) {
+        set_error("invalid arguments to farm_store_device_bytes");
+        return FARM_EINVAL;
+    }
+    const DevBuf *bufs[] = {&s->d_xy_in, &s->d_off, &s->d_ring, &s->d_hdr, &s->d_status, &s->d_offset, &s->d_seq,
+                            &s->d_hoff, &s->d_hnodes, &s->d_voff, &s->d_vnodes, &s->d_areas, &s->cub_tmp,
+                            &s->d_pairs, &s->d_out, &s->d_counters, &s->d_check};
+    uint64_t t = 0;
+    for (const DevBuf *b : bufs) t += b->cap;
+    for (const auto &b : s->s) t += b.cap;
+    *bytes = t;
+    return FARM_OK;
 }
 
 int farm_sync(farm_store *s) {

@@ -796,6 +796,7 @@ int within(farm_store *s, const uint32_t *pairs, uint64_t n, double distance, in
         set_error("farm_within: no target side loaded (or pass target_is_source)");
         return FARM_EINVAL;
     }
+    FARM_TRY(check_pairs(s, pairs, n, mem, self != 0, "farm_within"));
     FARM_TRY(ensure_tables(s->device));
     cudaStream_t stream = s->stream;
     const uint64_t tgt_base = self ? 0 : s->n_side[0];

@@ -238,6 +238,12 @@ class Store:
         """Engine kernels launched through this store so far."""
         return int(self._lib.farm_store_launches(self._h))
 
+    def device_bytes(self) -> int:
+        """Device bytes held by the store's own allocations."""
+        b = C.c_uint64(0)
+        check_gpu(self._lib.farm_store_device_bytes(self._h, C.byref(b)))
+        return int(b.value)
+
     def raster_totals(self) -> dict:
         """Sizes of the last rasterization (units processed, arrays written)."""
         t = RasterTotals()
@@ -305,6 +311,13 @@ def _torch_empty_u8(n, device):
 def _torch_empty_f64(n, device):
     import torch
     return torch.empty(n, dtype=torch.float64, device=device)
+
+
+def issue_rates() -> dict:
+    """Measured non-fused FP64 and FP32 operation rates of the current device (ops/s)."""
+    a, b = C.c_double(0), C.c_double(0)
+    check_gpu(gpu().farm_probe_issue_rates(C.byref(a), C.byref(b)))
+    return {"fp64_ops_per_s": a.value, "fp32_ops_per_s": b.value}
 
 
 def device_name() -> str:

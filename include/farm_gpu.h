@@ -162,7 +162,10 @@ int farm_raster_fetch(farm_store *s, int side, uint64_t index, farm_raster_view 
  * call before any stream capture. All calls share the array and it keeps the
  * last call's contents, so calls that overlap on the GPU (from different host
  * threads or stores) race; serialise them. The store itself must already be
- * loaded and rasterized (those steps allocate). */
+ * loaded and rasterized (those steps allocate). The looked-up address is kept
+ * for the life of the process: do not reset the device (cudaDeviceReset) or
+ * tear down its primary context while this entry point is in use. Pair
+ * indices are range-checked on the host before any device work. */
 int farm_intersect_static(farm_store *s, const uint32_t *pairs, uint64_t n, uint8_t *out, uint64_t *found);
 
 /* Diagnostics: the learned scorer's tcgen05 GEMM on its own, C[M x N] (fp32)
@@ -246,6 +249,14 @@ int farm_event_record(farm_store *s, int slot);
 int farm_event_elapsed(farm_store *s, int a, int b, double *ms);
 /* Engine kernels launched through this store so far. */
 uint64_t farm_store_launches(farm_store *s);
+/* Measured non-fused FP64 and FP32 arithmetic rates of the current device
+ * (multiplies or adds per second), the denominators of the FP64- and
+ * FP32-bound rooflines. No counterpart in the reference. */
+int farm_probe_issue_rates(double *fp64_ops_per_s, double *fp32_ops_per_s);
+/* Device bytes the store currently holds in its own allocations (rings,
+ * rasters, query scratch), the learned scorer's state excluded. No
+ * counterpart in the reference. */
+int farm_store_device_bytes(farm_store *s, uint64_t *bytes);
 
 #ifdef __cplusplus
 }

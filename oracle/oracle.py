@@ -127,6 +127,59 @@ def rasterize_set(ps, vpr: int, hierarchy: bool = False, category_count: int = 1
     return [Raster(ps.ring(k), vpr, hierarchy, category_count, merge_carry, grid_extent) for k in range(ps.n)]
 
 
+def _try_raster(args):
+    ring, vpr, hierarchy, category_count = args
+    try:
+        return Raster(ring, vpr, hierarchy, category_count)
+    except RuntimeError:  # the reference asserts or never terminates on this polygon
+        return None
+
+
+def rasterize_many(rings, vpr: int, hierarchy: bool = False, category_count: int = 16, threads: int = 0) -> list:
+    """Raster objects of many rings (None where the reference fails on one),
+    built on a thread pool: ctypes releases the GIL while the C code runs, so
+    the threads use every core. Largest rings are started first."""
+    import concurrent.futures as cf
+    import os
+    lib()
+    rings = list(rings)
+    order = sorted(range(len(rings)), key=lambda k: -len(rings[k]))
+    out = [None] * len(rings)
+    with cf.ThreadPoolExecutor(max_workers=threads or os.cpu_count() or 1) as ex:
+        futs = {ex.submit(_try_raster, (rings[k], vpr, hierarchy, category_count)): k for k in order}
+        for f in cf.as_completed(futs):
+            out[futs[f]] = f.result()
+    return out
+
+
+def intersect_many(rs: list, rt: list, pairs, threads: int = 0, counters: bool = False):
+    """Oracle intersect of (s, t) pairs over prebuilt rasters, on a thread
+    pool: 0/1 per pair, 2 where either raster is None; with counters, also the
+    reference-order segment tests per pair (uint64)."""
+    import concurrent.futures as cf
+    import os
+    pairs = np.asarray(pairs)
+    n = len(pairs)
+    res = np.zeros(n, np.uint8)
+    tests = np.zeros(n, np.uint64)
+    nt = threads or os.cpu_count() or 1
+    bounds = np.linspace(0, n, min(n, 4 * nt) + 1).astype(np.int64) if n else np.zeros(1, np.int64)
+
+    def run(lo_hi):
+        lo, hi = lo_hi
+        for k in range(lo, hi):
+            a, b = rs[int(pairs[k, 0])], rt[int(pairs[k, 1])]
+            if a is None or b is None:
+                res[k] = 2
+                continue
+            v, c = intersect(a, b, counters=True)
+            res[k] = int(v)
+            tests[k] = c.segment_tests
+    with cf.ThreadPoolExecutor(max_workers=nt) as ex:
+        list(ex.map(run, zip(bounds[:-1], bounds[1:])))
+    return (res, tests) if counters else res
+
+
 def intersect(rs: Raster, rt: Raster, counters: bool = False):
     c = FoCounters()
     fp = C.POINTER(C.c_float)
