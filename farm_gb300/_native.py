@@ -44,6 +44,7 @@ def host() -> C.CDLL:
         lib.farm_gen_counts.argtypes = [C.POINTER(GenParams), C.c_uint64, C.c_uint64, C.c_uint64, u32p]
         lib.farm_gen_fill.argtypes = [C.POINTER(GenParams), C.c_uint64, C.c_uint64, C.c_uint64, u64p, f32p, C.c_int]
         lib.farm_gen_centres.argtypes = [C.POINTER(GenParams), C.c_uint64, C.c_uint64, C.c_uint64, f64p]
+        lib.farm_gen_radii.argtypes = [C.POINTER(GenParams), C.c_uint64, C.c_uint64, C.c_uint64, f64p, C.c_int]
         lib.farm_gen_counts_idx.argtypes = [C.POINTER(GenParams), C.c_uint64, u64p, C.c_uint64, u32p]
         lib.farm_gen_fill_idx.argtypes = [C.POINTER(GenParams), C.c_uint64, u64p, C.c_uint64, u64p, f32p, C.c_int]
         lib.farm_dt_write.argtypes = [C.c_char_p, C.c_uint64, u64p, f32p]

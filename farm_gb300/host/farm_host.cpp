@@ -187,6 +187,40 @@ int farm_gen_fill(const farm_gen_params *gp, uint64_t seed, uint64_t first, uint
     return gen_fill(gp, seed, [first](uint64_t k) { return first + k; }, count, off, xy, threads);
 }
 
+int farm_gen_radii(const farm_gen_params *gp, uint64_t seed, uint64_t first, uint64_t count, double *rmax,
+                   int threads) {
+    if (!gp || (!rmax && count)) return fail(FARM_EINVAL, "null argument");
+    if (gp->n_lo < 3 || gp->n_hi < gp->n_lo) return fail(FARM_EINVAL, "vertex-count range must satisfy 3 <= n_lo <= n_hi");
+    if (!(gp->r_lo > 0) || gp->r_hi < gp->r_lo) return fail(FARM_EINVAL, "radius range must satisfy 0 < r_lo <= r_hi");
+    const double two_pi = 6.283185307179586476925286766559;
+    const double lr0 = std::log(gp->r_lo), lr1 = std::log(gp->r_hi);
+    parallel_chunks(count, threads, 64, [&](uint64_t b, uint64_t e) {
+        for (uint64_t k = b; k < e; k++) {
+            const uint64_t i = first + k;
+            const uint32_t n = gen_count(gp, seed, i) - 1;
+            const double rbar = std::exp(lr0 + rng_open01(seed, i, S_R, 0) * (lr1 - lr0));
+            // the same draws as gen_fill's per-vertex radius; every step from
+            // z to r is monotone, so the largest z gives the largest r. As
+            // z <= sqrt(-2 ln u), a vertex whose u lies above exp(-zmax^2 / 2)
+            // (with a relative margin far above the rounding of that bound)
+            // cannot raise zmax, and its logarithm and cosine are skipped.
+            double zmax = -1e300, ucut = 1.0;
+            for (uint32_t j = 0; j < n; j++) {
+                double u = rng_open01(seed, i, S_NRM_U, j);
+                if (u > ucut) continue;
+                double v = rng_open01(seed, i, S_NRM_V, j);
+                double z = std::sqrt(-2.0 * std::log(u)) * std::cos(two_pi * v);
+                if (z > zmax) {
+                    zmax = z;
+                    ucut = zmax > 0 ? std::exp(-0.5 * zmax * zmax) * (1.0 + 1e-9) : 1.0;
+                }
+            }
+            rmax[k] = rbar * std::exp(gp->sigma * zmax);
+        }
+    });
+    return FARM_OK;
+}
+
 int farm_gen_counts_idx(const farm_gen_params *gp, uint64_t seed, const uint64_t *idx, uint64_t count,
                         uint32_t *nverts_out) {
     if (!gp || (count && (!idx || !nverts_out))) return fail(FARM_EINVAL, "null argument");

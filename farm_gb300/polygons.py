@@ -94,6 +94,15 @@ def centres(params: StarParams, seed: int, count: int, first: int = 0) -> np.nda
     return out
 
 
+def radii(params: StarParams, seed: int, count: int, first: int = 0, threads: int = 0) -> np.ndarray:
+    """Largest vertex distance from the centre of generator polygons
+    first..first+count-1 (float64 [count]), without drawing their vertices."""
+    gp = params.c()
+    out = np.zeros(count, dtype=np.float64)
+    check_host(host().farm_gen_radii(C.byref(gp), seed, first, count, ptr(out, f64p), threads))
+    return out
+
+
 def generate_indices(params: StarParams, seed: int, idx, threads: int = 0, out_off=None, out_xy=None) -> PolygonSet:
     """Generator polygons idx[0], idx[1], ... (any order) as one set. out_off / out_xy
     may supply preallocated (e.g. pinned) arrays of the right sizes."""

@@ -7,13 +7,14 @@ target set T splits with no exchange on the data path:
 
 * the domain is cut into vertical strips by source centre; strip b holds the
   sources whose centre x lies in [b w, (b + 1) w), w = L / n_strips;
-* strip b takes every target whose extent (centre x +- extent radius) reaches
-  the x-range of the strip's source MBRs;
+* strip b takes every target whose x-extent (an interval that holds all its
+  vertices: the generator's exact largest radius about the centre, or the
+  MBR itself) reaches the x-range of the strip's source MBRs;
 * the strip's candidates are the MBR-overlapping pairs of those two sets.
 
 Each candidate pair (s, t) of the whole job falls in the strip of s, and t
-is in that strip's target set whenever its MBR lies within its extent
-radius, so the strips' pair sets partition the job's. Rank r runs strips
+is always in that strip's target set (its MBR lies inside its x-extent and
+overlaps the MBR of s), so the strips' pair sets partition the job's. Rank r runs strips
 r, r + N, r + 2N, ...; the only collective is the reduction of the ranks'
 pair counts and times at the end of a run.
 """
@@ -40,16 +41,27 @@ def strip_sources(src_centres: np.ndarray, strip: int, n_strips: int, side: floa
     return np.nonzero(lo & hi)[0].astype(np.uint64)
 
 
-def strip_targets(src_mbrs: np.ndarray, tgt_centres: np.ndarray, extent_radii: float) -> np.ndarray:
-    """Indices (uint64) of the targets whose extent reaches the x-range of the
-    strip's source MBRs; a target's extent is its centre x +- extent_radii x
-    its mean radius (tgt_centres columns: x, y, mean radius)."""
+def target_extents(tgt_centres: np.ndarray, tgt_rmax: np.ndarray) -> np.ndarray:
+    """Closed x-intervals [lo, hi] (float64 [n, 2]) that contain every vertex
+    of each target: centre x -+ its largest vertex distance from the centre,
+    widened by the float32 rounding of the stored coordinates (a relative
+    2^-24 of the coordinate, bounded here by 1e-6 of |x| + 1e-6)."""
+    cx = tgt_centres[:, 0]
+    r = np.asarray(tgt_rmax, dtype=np.float64) * (1.0 + 1e-6)
+    pad = 1e-6 * (np.abs(cx) + r + 1.0)
+    return np.stack([cx - r - pad, cx + r + pad], axis=1)
+
+
+def strip_targets(src_mbrs: np.ndarray, tgt_xext: np.ndarray) -> np.ndarray:
+    """Indices (uint64) of the targets whose x-extent (tgt_xext[k] = [lo, hi],
+    an interval holding every vertex of target k, e.g. target_extents() or the
+    exact MBRs) reaches the x-range of the strip's source MBRs. A target
+    outside that range has an MBR disjoint from every source MBR of the
+    strip, so no candidate pair of the strip is lost."""
     if len(src_mbrs) == 0:
         return np.zeros(0, np.uint64)
-    ext = extent_radii * tgt_centres[:, 2]
     xlo, xhi = src_mbrs[:, 0].min(), src_mbrs[:, 2].max()
-    cx = tgt_centres[:, 0]
-    return np.nonzero((cx + ext >= xlo) & (cx - ext <= xhi))[0].astype(np.uint64)
+    return np.nonzero((tgt_xext[:, 1] >= xlo) & (tgt_xext[:, 0] <= xhi))[0].astype(np.uint64)
 
 
 def reduce_job(t_dev: float, t_e2e: float, n_pairs: int, device=None) -> tuple[float, float, float]:

@@ -55,6 +55,12 @@ int farm_gen_counts(const farm_gen_params *gp, uint64_t seed, uint64_t first, ui
 /* Centre (cx, cy) and mean radius of each polygon, 3 doubles per polygon,
  * without drawing its vertices (the same counters as farm_gen_fill). */
 int farm_gen_centres(const farm_gen_params *gp, uint64_t seed, uint64_t first, uint64_t count, double *cxyr);
+/* Largest vertex distance from the centre of each polygon (the mean radius
+ * times its largest lognormal factor), from the same draws as farm_gen_fill
+ * without computing the vertices: every vertex of polygon i lies within
+ * rmax[i] of its centre, up to the float32 rounding of its coordinates. */
+int farm_gen_radii(const farm_gen_params *gp, uint64_t seed, uint64_t first, uint64_t count, double *rmax,
+                   int threads);
 /* Pass 2: fill rings; off (count+1 entries) must be the exclusive scan of the
  * counts from pass 1 (off[0] may be non-zero: it is an absolute offset into xy). */
 int farm_gen_fill(const farm_gen_params *gp, uint64_t seed, uint64_t first, uint64_t count,
