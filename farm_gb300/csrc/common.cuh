@@ -192,7 +192,7 @@ int check_pairs(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, bool 
 // The store object behind the C ABI.
 namespace farm {
 // Scratch slots of farm_store::s. The rasterizer's pipeline uses slots 0-33
-// (raster.cu) only while farm_rasterize runs; the queries reuse Q_SCR0-5
+// and 40-43 (raster.cu) only while farm_rasterize runs; the queries reuse Q_SCR0-5
 // within one call; Q_WITHIN_SUF and Q_AREA_ORIENT are theirs alone (the
 // area orientations stay valid across calls and a captured area plan holds
 // their address).
@@ -229,7 +229,7 @@ struct farm_store {
     uint64_t tot_P = 0, tot_status = 0, tot_seq = 0;
     farm_raster_totals rtot = {};
     // scratch for the rasterizer and the queries
-    farm::DevBuf s[40];
+    farm::DevBuf s[48];
     farm::DevBuf cub_tmp;
     farm::DevBuf d_pairs, d_out, d_counters;
     farm::DevBuf d_check;  // pair-index validation counter

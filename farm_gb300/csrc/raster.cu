@@ -23,6 +23,7 @@
 #include <cstring>
 
 #include "common.cuh"
+#include "dfloat.cuh"
 
 namespace farm {
 
@@ -67,6 +68,10 @@ enum Scratch {
     S_CPCOL,    // column of each column-polygon point
     S_COLPOLY,  // polygon of each fill column
     S_ECNT16,   // per-edge walk counts from phase 1 (u16 x 3), reused by phase 2
+    S_COLXF = 40,  // float forms of the sweep lines (LineF); slots 35-39 belong to the queries
+    S_ROWYF = 41,
+    S_WALKF = 42,  // per-polygon walk constants (WalkF)
+    S_LINEBIG = 43, // grid lines too long for the shared-memory node sort
 };
 
 // ------------------------------------------------------------ headers ----
@@ -211,8 +216,14 @@ __global__ void k_header(const float2 *__restrict__ ring, const uint64_t *__rest
 
 // Bases from the scanned sizes, and the fill sweep lines (Ideal.cpp:829-851,
 // :869-875): Xi accumulates by repeated addition, exactly as the loop does.
+// The line after the last column (row) is stored too, with each line's float
+// forms (LineF, declared with the fill kernels).
+struct LineF;
+__device__ inline void put_line(double *lines, LineF *lf, uint64_t at, double v);
+
 __global__ void k_bases(PolyHdr *__restrict__ hdr, uint32_t npoly, const uint64_t *__restrict__ scan,
-                        double *__restrict__ colx, double *__restrict__ rowy) {
+                        double *__restrict__ colx, double *__restrict__ rowy, LineF *__restrict__ colf,
+                        LineF *__restrict__ rowf) {
     uint64_t n1 = (uint64_t)npoly + 1;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npoly; p += gridDim.x * blockDim.x) {
         PolyHdr h = hdr[p];
@@ -232,11 +243,12 @@ __global__ void k_bases(PolyHdr *__restrict__ hdr, uint32_t npoly, const uint64_
                 h.err = FARM_EASSERT;
                 break;
             }
-            colx[h.col + c] = Xi;
+            put_line(colx, colf, h.col + c, Xi);
             Xi += h.step_x;
             Xi1 = Xi + h.step_x;
             c++;
         }
+        put_line(colx, colf, h.col + c, Xi);  // c <= dimx + 1 < dimx + 2 entries
         if (c > h.dimx) h.err = FARM_EASSERT;
         h.ncols = c;
         double Yi = h.mbr[1];
@@ -248,11 +260,12 @@ __global__ void k_bases(PolyHdr *__restrict__ hdr, uint32_t npoly, const uint64_
                 h.err = FARM_EASSERT;
                 break;
             }
-            rowy[h.row + r] = Yi;
+            put_line(rowy, rowf, h.row + r, Yi);
             Yi += h.step_y;
             Yi1 = Yi + h.step_y;
             r++;
         }
+        put_line(rowy, rowf, h.row + r, Yi);
         if (r > h.dimy) h.err = FARM_EASSERT;
         h.nrows = r;
         hdr[p] = h;
@@ -263,37 +276,78 @@ __global__ void k_bases(PolyHdr *__restrict__ hdr, uint32_t npoly, const uint64_
 // Ideal.cpp:259-521 for one edge. Sink receives: border(x, y), cross(from,
 // to) (a LEAVE/ENTER pair), hnode(line, value), vnode(line, value).
 //
-// FP64 is GB300's scarcest pipe, and the reference's walk divides three times
-// per step. Every one of those quotients only feeds an integer decision —
-// truncation, the 1e-8 snap of double_to_int, or the 1e-9 grid-corner test —
-// except the h-node abscissa, which is emitted. So each quotient t / d is
-// first taken as t * fl(1/d), which differs from the reference's fl(t / d) by
-// at most ~3 units in the last place of |q| <= grid size (a few 1e-16 * dim);
-// the decision is read off that value unless it lies within a 1e-15 * (dim + 4)
-// band of a decision threshold, where the exact quotient is taken instead.
-// Outside the band both values fall on the same side of every threshold, so
-// the decisions are the reference's. Emitted values (v-node ordinates, h-node
-// abscissae) are always the reference's exact expressions.
+// FP64 is GB300's scarcest pipe (2 lanes per clock per SM against 128 for
+// FP32), and every quotient of the reference's walk only feeds an integer
+// decision: the truncation and 1e-8 snap of double_to_int for the endpoint
+// cells, the 1e-9 grid-corner test and the truncation of the x-branch, the
+// truncation of the y-branch. Each is evaluated in double-float arithmetic
+// on the FP32 pipe with a bound on its distance from the reference's double
+// (cval, dfloat.cuh); when no decision threshold lies within that bound the
+// decision is the reference's, and otherwise the reference's FP64 expression
+// decides. Only the emitted node values (the v-node ordinates and h-node
+// abscissae, doubles) are computed in FP64, and only by the fill pass.
+
+// Per polygon: start, step and 1 / step of both axes split into
+// double-floats (k_bases), the walk's constants.
+struct WalkF {
+    dflt sx, sy, tx, ty, ix, iy;
+};
+
+__device__ inline dflt split_d(double v) {
+    const float hi = __double2float_rn(v);
+    return {hi, __double2float_rn(v - (double)hi)};
+}
+
+// Where a quotient q (within e of the reference's double Q) sits between
+// integers: fi = floor, d0 = q - fi, d1 = fi + 1 - q, each accurate to a
+// rounding of itself when small. false when q is out of the float range used.
+__device__ inline bool frac_parts(dflt q, float &fi, float &d0, float &d1) {
+    if (!(fabsf(q.hi) < 4194304.f)) return false;
+    fi = floorf(q.hi);
+    if (q.hi == fi) {
+        if (q.lo < 0.f) {
+            fi = __fsub_rn(fi, 1.f);
+            d0 = __fadd_rn(1.f, q.lo);
+            d1 = -q.lo;
+        } else {
+            d0 = q.lo;
+            d1 = __fsub_rn(1.f, q.lo);
+        }
+    } else {
+        d0 = __fadd_rn(__fsub_rn(q.hi, fi), q.lo);
+        d1 = __fsub_rn(__fsub_rn(__fadd_rn(fi, 1.f), q.hi), q.lo);
+    }
+    return true;
+}
+
+// double_to_int(Q) (util.h:98-106) for the reference's quotient Q within e
+// of q, Q >= 0: the integer part, plus one when the next integer is less
+// than 1e-8 away. -1 when undecided.
+__device__ inline int d2i_cert(const cval &q) {
+    float fi, d0, d1;
+    if (!frac_parts(q.v, fi, d0, d1) || fi < 0.f) return -1;
+    const float m = __fadd_rn(__fadd_rn(q.e, __fmul_rn(2.f * kU, d1)), 1e-15f);
+    if (fabsf(__fsub_rn(d1, 1e-8f)) <= m) return -1;
+    return (int)fi + (d1 < 1e-8f ? 1 : 0);
+}
+
+// double_to_int((v - start) / step) for a vertex coordinate v
+__device__ inline int cell_of(float v, const dflt &s, const dflt &is, double start, double step) {
+    const cval q = cv_mul(cv_add(cv_f(v), cv_neg(cv_d(s))), cv_d(is));
+    const int r = d2i_cert(q);
+    return r >= 0 ? r : double_to_int(((double)v - start) / step);
+}
+
 template <typename Sink>
-__device__ void walk_edge(const PolyHdr &h, float2 A, float2 B, Sink &s) {
+__device__ void walk_edge(const PolyHdr &h, const WalkF &g, float2 A, float2 B, Sink &s) {
     const double start_x = h.mbr[0], start_y = h.mbr[1];
     const double step_x = h.step_x, step_y = h.step_y;
-    const double isx = __drcp_rn(step_x), isy = __drcp_rn(step_y);
     const int dimx = h.dimx, dimy = h.dimy;
-    const double qlim = (double)(dimx > dimy ? dimx : dimy) + 2.0;
-    const double band = 1e-15 * (qlim + 2.0);
-    // double_to_int(t / d) for t / d >= 0 (a vertex is never left of or
-    // below its MBR): its only thresholds there sit 1e-8 below each integer
-    auto d2i = [&](double t, double d, double inv) -> int {
-        double v = t * inv;
-        if (!(v >= -0.5 && v <= qlim) || fabs(fabs(v - rint(v)) - 1e-8) <= band) v = t / d;
-        return double_to_int(v);
-    };
-    double x1 = A.x, y1 = A.y, x2 = B.x, y2 = B.y;
-    int cur_startx = d2i(x1 - start_x, step_x, isx);
-    int cur_endx = d2i(x2 - start_x, step_x, isx);
-    int cur_starty = d2i(y1 - start_y, step_y, isy);
-    int cur_endy = d2i(y2 - start_y, step_y, isy);
+    const float x1 = A.x, y1 = A.y, x2 = B.x, y2 = B.y;
+    int cur_startx = cell_of(x1, g.sx, g.ix, start_x, step_x);
+    int cur_endx = cell_of(x2, g.sx, g.ix, start_x, step_x);
+    int cur_starty = cell_of(y1, g.sy, g.iy, start_y, step_y);
+    int cur_endy = cell_of(y2, g.sy, g.iy, start_y, step_y);
     if (cur_startx == dimx) cur_startx--;
     if (cur_endx == dimx) cur_endx--;
     if (cur_starty == dimy) cur_starty--;
@@ -308,12 +362,12 @@ __device__ void walk_edge(const PolyHdr &h, float2 A, float2 B, Sink &s) {
     if (y1 == y2) {
         if (cur_startx < cur_endx) {
             for (int x = cur_startx; x < cur_endx; x++) {
-                s.vnode(x + 1, y1);
+                s.vnode(x + 1, (double)y1);
                 s.cross(x, cur_starty, x + 1, cur_starty);
             }
         } else {
             for (int x = cur_startx; x > cur_endx; x--) {
-                s.vnode(x, y1);
+                s.vnode(x, (double)y1);
                 s.cross(x, cur_starty, x - 1, cur_starty);
             }
         }
@@ -322,24 +376,42 @@ __device__ void walk_edge(const PolyHdr &h, float2 A, float2 B, Sink &s) {
     if (x1 == x2) {
         if (cur_starty < cur_endy) {
             for (int y = cur_starty; y < cur_endy; y++) {
-                s.hnode(y + 1, x1);
+                s.hnode(y + 1, (double)x1);
                 s.cross(cur_startx, y, cur_startx, y + 1);
             }
         } else {
             for (int y = cur_starty; y > cur_endy; y--) {
-                s.hnode(y, x1);
+                s.hnode(y, (double)x1);
                 s.cross(cur_startx, y, cur_startx, y - 1);
             }
         }
         return;
     }
-    const double a = (y1 - y2) / (x1 - x2);
-    const double b = (x1 * y2 - x2 * y1) / (x1 - x2);
-    const double ia = __drcp_rn(a);
-    // band for the y-branch quotient ((yv - b) / a - start_x) / step_x: the
-    // abscissa's ~3 ulp error, carried through the subtraction and the scaling
-    const double mx = fmax(fabs(x1), fabs(x2));
-    const double band2 = 1e-15 * ((2.0 * mx + fabs(start_x)) * isx + qlim + 2.0);
+    // the line y = a x + b of the reference (Ideal.cpp:371-372), tracked:
+    // a = (y1 - y2) / (x1 - x2), b = (x1 y2 - x2 y1) / (x1 - x2); the
+    // products of floats are exact in double, so the numerator of b is the
+    // exact difference rounded once
+    const cval cdy = cv_add(cv_f(y1), cv_f(-y2));
+    const cval cdx = cv_add(cv_f(x1), cv_f(-x2));
+    const cval ca = cv_div(cdy, cdx);
+    const cval cia = cv_div(cdx, cdy);  // 1 / a: a's own rounding is one more 2^-52 relative
+    const cval cia2 = {cia.v, __fadd_rn(cia.e, __fmul_rn(kRef, fabsf(cia.v.hi)))};
+    const dflt p1 = two_prod(x1, y2), p2 = two_prod(x2, y1);
+    const cval cnum = cv_add({p1, 0.f}, {{-p2.hi, -p2.lo}, 0.f});
+    const cval cb = cv_div(cnum, cdx);
+    const cval csx = cv_d(g.sx), csy = cv_d(g.sy), ctx = cv_d(g.tx), cty = cv_d(g.ty);
+    const cval cix = cv_d(g.ix), ciy = cv_d(g.iy);
+    // the reference's doubles, computed on first use (fill pass values and
+    // undecided steps only)
+    double a = 0.0, b = 0.0;
+    bool have_ab = false;
+    auto need_ab = [&]() {
+        if (!have_ab) {
+            a = ((double)y1 - (double)y2) / ((double)x1 - (double)x2);
+            b = ((double)x1 * (double)y2 - (double)x2 * (double)y1) / ((double)x1 - (double)x2);
+            have_ab = true;
+        }
+    };
     const int ymax = cur_endy > cur_starty ? cur_endy : cur_starty;
     const int ymin = cur_endy < cur_starty ? cur_endy : cur_starty;
     const int xmax = cur_endx > cur_startx ? cur_endx : cur_startx;
@@ -353,21 +425,35 @@ __device__ void walk_edge(const PolyHdr &h, float2 A, float2 B, Sink &s) {
         }
         bool passed = false;
         if (x != cur_endx) {
-            double xval;
-            if (cur_startx < cur_endx)
-                xval = ((double)x + 1) * step_x + start_x;
-            else
-                xval = (double)x * step_x + start_x;
-            const double yval = xval * a + b;
-            const double t = yval - start_y;
-            double q = t * isy;
-            double d = fabs(q - rint(q));
-            if (!(fabs(q) <= qlim) || fabs(d - 1e-9) <= band) {
-                q = t / step_y;
-                d = fabs(q - round(q));
+            const int xl = cur_startx < cur_endx ? x + 1 : x;  // the vertical line crossed
+            // xval = xl * step_x + start_x; Q = (xval * a + b - start_y) / step_y
+            const cval cxv = cv_add(cv_mul(cv_f((float)xl), ctx), csx);
+            const cval cq = cv_mul(cv_add(cv_add(cv_mul(cxv, ca), cb), cv_neg(csy)), ciy);
+            float fi, d0, d1;
+            int corner = -1, cur_y = 0;
+            if (frac_parts(cq.v, fi, d0, d1)) {
+                const float dist = fminf(d0, d1);
+                const float m = __fadd_rn(__fadd_rn(cq.e, __fmul_rn(2.f * kU, dist)), 1e-15f);
+                if (fabsf(__fsub_rn(dist, 1e-9f)) > m) {
+                    corner = dist < 1e-9f ? 1 : 0;
+                    cur_y = (int)fi;  // floor; equal to the truncation after the clamp below
+                }
             }
-            if (d < 1e-9) {
+            if (corner < 0) {  // undecided: the reference's FP64 expression
+                need_ab();
+                const double xval = (double)xl * step_x + start_x;
+                const double yval = xval * a + b;
+                const double q = (yval - start_y) / step_y;
+                corner = fabs(q - round(q)) < 1e-9 ? 1 : 0;
+                cur_y = (int)q;
+            }
+            if (corner) {
                 // Ideal.cpp:396-422: through a grid corner
+                double yval = 0.0;
+                if (Sink::kValues && cur_startx < cur_endx) {
+                    need_ab();
+                    yval = ((double)xl * step_x + start_x) * a + b;
+                }
                 if (cur_startx < cur_endx && cur_starty < cur_endy) {
                     s.vnode(x + 1, yval);
                     s.cross(x, y, x + 1, y + 1);
@@ -389,11 +475,15 @@ __device__ void walk_edge(const PolyHdr &h, float2 A, float2 B, Sink &s) {
                 }
                 continue;
             }
-            int cur_y = (int)q;
             if (cur_y > ymax) cur_y = ymax;
             if (cur_y < ymin) cur_y = ymin;
             if (cur_y == y) {
                 passed = true;
+                double yval = 0.0;
+                if (Sink::kValues) {
+                    need_ab();
+                    yval = ((double)xl * step_x + start_x) * a + b;
+                }
                 if (cur_startx < cur_endx) {
                     s.vnode(x + 1, yval);
                     s.cross(x, y, x + 1, y);
@@ -406,26 +496,32 @@ __device__ void walk_edge(const PolyHdr &h, float2 A, float2 B, Sink &s) {
             }
         }
         if (y != cur_endy) {
-            double yval;
-            if (cur_starty < cur_endy)
-                yval = (double)(y + 1) * step_y + start_y;
-            else
-                yval = (double)y * step_y + start_y;
-            const double t2 = yval - b;
-            double xv = t2 * ia;
-            double q2 = (xv - start_x) * isx;
-            bool exact = false;
-            if (!(fabs(q2) <= qlim) || fabs(q2 - rint(q2)) <= band2) {
-                xv = t2 / a;
-                q2 = (xv - start_x) / step_x;
-                exact = true;
+            const int yl = cur_starty < cur_endy ? y + 1 : y;  // the horizontal line crossed
+            // yval = yl * step_y + start_y; xval = (yval - b) / a; Q = (xval - start_x) / step_x
+            const cval cyv = cv_add(cv_mul(cv_f((float)yl), cty), csy);
+            const cval cxv = cv_mul(cv_add(cyv, cv_neg(cb)), cia2);
+            const cval cq = cv_mul(cv_add(cxv, cv_neg(csx)), cix);
+            float fi, d0, d1;
+            int cur_x = 0;
+            bool ok = false;
+            if (frac_parts(cq.v, fi, d0, d1)) {
+                const float dist = fminf(d0, d1);
+                if (dist > __fadd_rn(__fadd_rn(cq.e, __fmul_rn(2.f * kU, dist)), 1e-15f)) {
+                    cur_x = (int)fi;
+                    ok = true;
+                }
             }
-            int cur_x = (int)q2;
+            double xval = 0.0;
+            if (!ok || Sink::kValues) {
+                need_ab();
+                const double yval = (double)yl * step_y + start_y;
+                xval = (yval - b) / a;
+                if (!ok) cur_x = (int)((xval - start_x) / step_x);
+            }
             if (cur_x > xmax) cur_x = xmax;
             if (cur_x < xmin) cur_x = xmin;
             if (cur_x == x) {
                 passed = true;
-                const double xval = (Sink::kValues && !exact) ? t2 / a : xv;
                 if (cur_starty < cur_endy) {
                     s.hnode(y + 1, xval);
                     s.cross(x, y, x, y + 1);
@@ -441,6 +537,20 @@ __device__ void walk_edge(const PolyHdr &h, float2 A, float2 B, Sink &s) {
             s.fail();
             return;
         }
+    }
+}
+
+__global__ void k_walkf(const PolyHdr *__restrict__ hdr, uint32_t npoly, WalkF *__restrict__ wf) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npoly; p += gridDim.x * blockDim.x) {
+        const PolyHdr &h = hdr[p];
+        WalkF g;
+        g.sx = split_d(h.mbr[0]);
+        g.sy = split_d(h.mbr[1]);
+        g.tx = split_d(h.step_x);
+        g.ty = split_d(h.step_y);
+        g.ix = split_d(1.0 / h.step_x);
+        g.iy = split_d(1.0 / h.step_y);
+        wf[p] = g;
     }
 }
 
@@ -522,8 +632,48 @@ struct FillSink {
 };
 
 // ------------------------------------------------------------ fill ----
+//
+// The fill sweep's column and row lines are doubles built by repeated
+// addition (Ideal.cpp:829-851); each is kept with its float forms (LineF):
+// rn = the float nearest to it (the clip points' coordinate on that line),
+// up / dn = the smallest float >= it and the largest float <= it (so that a
+// float v satisfies v >= line iff v >= up, and v <= line iff v <= dn: the
+// reference's float-vs-double range tests become float compares), and
+// lo = rn(line - rn), with which rn + lo carries the line to ~2^-48.
+//
+// The clip points' other coordinate is an FP64 expression of the reference
+// rounded to float. It is evaluated in double-float arithmetic on the FP32
+// pipe with an error bound that covers both this evaluation and the
+// reference's own FP64 roundings (dfloat.cuh); only when a float rounding
+// midpoint lies inside that bound is the reference's FP64 expression itself
+// evaluated. Both paths give the reference's float, so the clip is
+// bit-identical either way; FARM_RASTER_EXACT=1 forces the FP64 path.
 
-__device__ inline bool in_rng(double lo, double hi, double v) { return !(v < lo || v > hi); }
+struct LineF {
+    float rn, up, dn, lo;
+};
+
+__device__ inline LineF line_f(double L) {
+    LineF f;
+    f.rn = __double2float_rn(L);
+    const double r = (double)f.rn;
+    if (r == L) {
+        f.up = f.dn = f.rn;
+    } else if (r > L) {
+        f.up = f.rn;
+        f.dn = nextafterf(f.rn, -INFINITY);
+    } else {
+        f.dn = f.rn;
+        f.up = nextafterf(f.rn, INFINITY);
+    }
+    f.lo = __double2float_rn(L - r);
+    return f;
+}
+
+__device__ inline void put_line(double *lines, LineF *lf, uint64_t at, double v) {
+    lines[at] = v;
+    lf[at] = line_f(v);
+}
 
 __device__ inline float2 mk(double x, double y) { return make_float2((float)x, (float)y); }
 
@@ -531,6 +681,9 @@ __device__ inline float2 mk(double x, double y) { return make_float2((float)x, (
 // the promotion is exact, so comparing in float gives the same answer without
 // the FP64 pipe
 __device__ inline bool in_rngf(float lo, float hi, float v) { return !(v < lo || v > hi); }
+
+// !(v < L0 || v > L1) for a float v and double lines L0, L1 (in_rng of the reference)
+__device__ inline bool in_lines(const LineF &L0, const LineF &L1, float v) { return v >= L0.up && v <= L1.dn; }
 
 // Points one edge contributes to column c's clip (Ideal.cpp:575-678), in order.
 // pi, pi1 are the float points (Xi, yi), (Xi1, yi1) on the column lines, yi and
@@ -541,12 +694,12 @@ __device__ inline bool in_rngf(float lo, float hi, float v) { return !(v < lo ||
 // under the same range test, so A would follow its own bit-identical copy in
 // the column's stream — a point the dedup rule always drops (a later copy of
 // a kept point, or of a point dropped for equalling a kept one).
-__device__ inline int clip_x_points(float2 A, float2 B, double Xi, double Xi1, float2 pi, float2 pi1, bool emitA,
-                                    float2 *out) {
+__device__ inline int clip_x_points(float2 A, float2 B, const LineF &X0, const LineF &X1, float2 pi, float2 pi1,
+                                    bool emitA, float2 *out) {
     int n = 0;
     const float mny = A.y < B.y ? A.y : B.y, mxy = A.y < B.y ? B.y : A.y;
     const float mnx = A.x < B.x ? A.x : B.x, mxx = A.x < B.x ? B.x : A.x;
-    if (emitA && in_rng(Xi, Xi1, A.x)) {
+    if (emitA && in_lines(X0, X1, A.x)) {
         if (out) out[n] = A;
         n++;
     }
@@ -559,38 +712,68 @@ __device__ inline int clip_x_points(float2 A, float2 B, double Xi, double Xi1, f
         if (c1) { if (out) out[n] = pi1; n++; }
         if (c0) { if (out) out[n] = pi; n++; }
     }
-    if (in_rng(Xi, Xi1, B.x)) {
+    if (in_lines(X0, X1, B.x)) {
         if (out) out[n] = B;
         n++;
     }
     return n;
 }
 
-// The edge's ordinate at column line X (Ideal.cpp:575-600). The reference
-// computes the slope per column and both lines' ordinates per column; the
-// slope depends only on the edge, and the ordinate at Xi1 is the one the next
-// column needs at its Xi (both lines come from the same repeated addition), so
-// callers compute the slope once and carry the ordinate: same doubles, half
-// the FP64 work.
+// The edge's ordinate at column line X (Ideal.cpp:575-600): the reference
+// computes slope = ((double)B.y - A.y) / (double)(B.x - A.x) (the x difference
+// taken in float) and ord = slope * (X - B.x) + B.y in FP64, then stores it as
+// a float. ordf(X) returns that float.
 struct ClipXEdge {
     float2 A, B;
     bool vert;
-    double slope, ymin;
+    float ymin, dxf;
+    dflt slope;      // double-float slope
+    float slope_err; // bound on |slope - the reference's double slope|
     __device__ ClipXEdge(float2 a, float2 b) : A(a), B(b) {
         vert = A.x == B.x;
         ymin = A.y < B.y ? A.y : B.y;
-        slope = vert ? 0.0 : ((double)B.y - A.y) / (double)(B.x - A.x);
+        dxf = __fsub_rn(B.x, A.x);
+        slope = {0.f, 0.f};
+        slope_err = 0.f;
+        if (!vert) {
+            const dflt dy = two_sum(B.y, -A.y);  // exact
+            slope = df_div_f(dy, dxf, &slope_err);
+            // the reference rounds dy and the quotient to double: 2 x 2^-53 relative
+            slope_err = __fadd_rn(slope_err, __fmul_rn(kU2 * 0.125f, fabsf(slope.hi)));
+        }
     }
-    __device__ double ord(double X) const { return vert ? ymin : slope * (X - B.x) + B.y; }
+    __device__ float ord_exact(double X) const {
+        if (vert) return ymin;
+        const double sl = ((double)B.y - A.y) / (double)(B.x - A.x);
+        return (float)(sl * (X - B.x) + B.y);
+    }
+    __device__ float ordf(double X, const LineF &L, bool cert) const {
+        if (vert) return ymin;
+        if (cert) {
+            float err = __fmul_rn(kU2, fabsf(L.rn));  // the line's own split (rn + lo)
+            const dflt d = df_add({L.rn, L.lo}, {-B.x, 0.f}, &err);
+            const float ed = err;  // |d - exact X - B.x|
+            float em = 0.f;
+            const dflt p = df_mul(slope, d, &em);
+            float e = __fadd_rn(__fadd_rn(__fmul_rn(fabsf(slope.hi), ed), __fmul_rn(fabsf(d.hi), slope_err)), em);
+            const dflt o = df_add(p, {B.y, 0.f}, &e);
+            // the reference's own roundings of X - B.x, the product and the sum
+            e = __fadd_rn(e, __fmul_rn(kU2 * 0.125f, __fadd_rn(__fadd_rn(__fmul_rn(fabsf(slope.hi), fabsf(d.hi)),
+                                                                           fabsf(p.hi)), fabsf(o.hi))) * 2.f);
+            float y;
+            if (round_certified(o, e, &y)) return y;
+        }
+        return ord_exact(X);
+    }
 };
 
 // Points one column-polygon edge contributes to row r's clip (Ideal.cpp:680-818),
 // given the float points (xi, Yi), (xi1, Yi1) on the row lines and the
 // parallel flag (ClipYEdge).
-__device__ inline int clip_y_points(float2 A, float2 B, double Yi, double Yi1, float2 pi, float2 pi1, bool parallels,
-                                    float2 *out) {
+__device__ inline int clip_y_points(float2 A, float2 B, const LineF &Y0, const LineF &Y1, float2 pi, float2 pi1,
+                                    bool parallels, float2 *out) {
     int n = 0;
-    if (in_rng(Yi, Yi1, A.y)) {
+    if (in_lines(Y0, Y1, A.y)) {
         if (out) out[n] = A;
         n++;
     }
@@ -613,73 +796,58 @@ __device__ inline int clip_y_points(float2 A, float2 B, double Yi, double Yi1, f
 // Ideal.cpp:680-730 per edge: vertical edges cut every row line at A.x;
 // horizontal edges touch only a row line they lie on (the other abscissa is
 // -DBL_MAX, which converts to -inf in float) and are otherwise parallel; the
-// rest cut at ((Y - B.y) / slope) + B.x, carried from Yi1 to the next row's Yi
-// as in ClipXEdge.
+// rest cut at ((Y - B.y) / slope) + B.x with the slope of ClipXEdge, and the
+// abscissa is used only rounded to float (abscf).
 struct ClipYEdge {
     float2 A, B;
     bool vert, horiz;
-    double slope;
+    dflt inv;      // double-float dxf / dy, the reciprocal of the reference's slope
+    float inv_err; // bound on |inv - 1 / the reference's double slope|
     __device__ ClipYEdge(float2 a, float2 b) : A(a), B(b) {
         vert = A.x == B.x;
         horiz = !vert && A.y == B.y;
-        slope = (vert || horiz) ? 0.0 : ((double)B.y - A.y) / (double)(B.x - A.x);
+        inv = {0.f, 0.f};
+        inv_err = 0.f;
+        if (!vert && !horiz) {
+            const dflt dy = two_sum(B.y, -A.y);  // exact
+            inv = df_rdiv(__fsub_rn(B.x, A.x), dy, &inv_err);
+            // the reference's slope carries two double roundings: 2 x 2^-53 relative
+            inv_err = __fadd_rn(inv_err, __fmul_rn(kU2 * 0.125f, fabsf(inv.hi)));
+        }
     }
     __device__ bool general() const { return !vert && !horiz; }
-    __device__ double absc(double Y) const { return ((Y - B.y) / slope) + B.x; }
-    // (float)absc(Y), the only form in which the abscissa is used. With
-    // isl = fl(1 / slope), s' = fl(fl((Y - B.y) * isl) + B.x) is within
-    // 3.02 u |q| + 1.01 ulp(s') of absc(Y) (q the quotient), i.e. within
-    // 2^(k+1) + 1.01 units of s''s last place for k = exp(q) - exp(s') + 1.
-    // Rounding to float changes only at float midpoints — where the 29 bits
-    // of s' below float precision read 2^28 — so when those bits are more
-    // than 2^(k+2) + 2 units from 2^28, (float)s' is (float)absc(Y); else
-    // the exact expression is taken.
-    __device__ float absc_f(double Y, double isl) const {
-        const double t = Y - B.y;
-        const double q = t * isl;
-        const double sx = q + B.x;
-        const long long bs = __double_as_longlong(sx), bq = __double_as_longlong(q);
-        const int es = (int)((bs >> 52) & 0x7FF), eq = (int)((bq >> 52) & 0x7FF);
-        const int k = eq - es + 1;
-        const int low = (int)(bs & 0x1FFFFFFFll);
-        const int dist = low > (1 << 28) ? low - (1 << 28) : (1 << 28) - low;
-        const int thr = (k < 0 ? 4 : (k > 24 ? (1 << 30) : (4 << k))) + 2;
-        // a normal float's exponent range, away from overflow and subnormals
-        if (es >= 1023 - 125 && es <= 1023 + 126 && dist > thr) return (float)sx;
-        return (float)(((Y - B.y) / slope) + B.x);
+    __device__ float absc_exact(double Y) const {
+        const double sl = ((double)B.y - A.y) / (double)(B.x - A.x);
+        return (float)(((Y - B.y) / sl) + B.x);
     }
-    // abscissae for row lines Yi, Yi1; g0, g1 are absc(Yi), absc(Yi1) for general edges
-    __device__ void row(double Yi, double Yi1, double g0, double g1, double &xi, double &xi1, bool &par) const {
-        par = false;
-        if (vert) {
-            xi = A.x;
-            xi1 = A.x;
-        } else if (horiz) {
-            xi = 0;
-            xi1 = 0;
-            if (A.y == Yi) {
-                xi = A.x;
-                xi1 = -INFINITY;
-            } else if (A.y == Yi1) {
-                xi = -INFINITY;
-                xi1 = A.x;
-            } else {
-                par = true;
-            }
-        } else {
-            xi = g0;
-            xi1 = g1;
+    __device__ float abscf(double Y, const LineF &L, bool cert) const {
+        if (cert) {
+            float et = __fmul_rn(kU2, fabsf(L.rn));  // the line's own split
+            const dflt t = df_add({L.rn, L.lo}, {-B.y, 0.f}, &et);
+            float e = 0.f;
+            const dflt q = df_mul(t, inv, &e);
+            e = __fadd_rn(e, __fadd_rn(__fmul_rn(fabsf(inv.hi), et), __fmul_rn(fabsf(t.hi), inv_err)));
+            const dflt x = df_add(q, {B.x, 0.f}, &e);
+            // the reference's own roundings of Y - B.y, the quotient and the sum
+            e = __fadd_rn(e, __fmul_rn(kU2 * 0.125f,
+                                       __fadd_rn(__fadd_rn(__fmul_rn(fabsf(t.hi), fabsf(inv.hi)), fabsf(q.hi)),
+                                                 fabsf(x.hi))) * 2.f);
+            float v;
+            if (round_certified(x, e, &v)) return v;
         }
+        return absc_exact(Y);
     }
 };
 
-// first index i in [0, n) with lines[i] + step >= v, scanning down from a
-// binary-search guess (lines ascending)
-__device__ int first_line(const double *lines, int n, double step, double v) {
+// first index i in [0, n) whose far line lines[i + 1] could reach v, on the
+// lines' float forms: up(lines[i + 1]) >= vf with vf <= v. It never lies past
+// the reference's first line (lines[i] + step >= v); the lines skipped before
+// that one contribute no point.
+__device__ int first_line_f(const LineF *lines, int n, float vf) {
     int lo = 0, hi = n;
     while (lo < hi) {
         int mid = (lo + hi) >> 1;
-        if (lines[mid] + step < v)
+        if (lines[mid + 1].up < vf)
             lo = mid + 1;
         else
             hi = mid;
@@ -687,8 +855,9 @@ __device__ int first_line(const double *lines, int n, double step, double v) {
     return lo;
 }
 
-// margin covering the float rounding of a clip line coordinate
-__device__ inline double fmargin(double a, double b) { return (fabs(a) + fabs(b)) * 1.2e-7 + 1e-30; }
+// float margin covering the float rounding of a clip line coordinate: at least
+// twice the reference's (|a| + |b|) * 1.2e-7 after its own rounding
+__device__ inline float fmargin_f(float a, float b) { return (fabsf(a) + fabsf(b)) * 2.5e-7f + 1e-30f; }
 
 // "Small" points: a coordinate below 2^-5 in magnitude, where two distinct
 // floats can be closer than the 1e-9 of Point::operator==. Elsewhere that
@@ -742,8 +911,8 @@ __global__ void k_edge_cost(const StoreView sv, const PolyHdr *__restrict__ hdr,
 // Phase 1's walk: per-polygon totals, and each edge's counts kept (u16, for
 // phase 2's chunks, which would otherwise walk every edge a second time only
 // to count); a count above 65535 sets *ovf and phase 2 counts by walking.
-__global__ void k_walk_tot(const StoreView sv, PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off,
-                           uint32_t npoly, uint64_t e0, uint64_t nedges, const uint32_t *__restrict__ perm,
+__global__ void k_walk_tot(const StoreView sv, PolyHdr *__restrict__ hdr, const WalkF *__restrict__ wf,
+                           const uint64_t *__restrict__ off, uint32_t npoly, uint64_t e0, uint64_t nedges, const uint32_t *__restrict__ perm,
                            unsigned long long *__restrict__ tot, uint16_t *__restrict__ c16, uint64_t ne_all,
                            int *__restrict__ ovf) {
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nedges;
@@ -758,7 +927,7 @@ __global__ void k_walk_tot(const StoreView sv, PolyHdr *__restrict__ hdr, const 
         s.status = sv.status + h.st;
         s.dimx = h.dimx;
         s.dimy = h.dimy;
-        walk_edge(h, r[i], r[i + 1], s);
+        walk_edge(h, wf[p], r[i], r[i + 1], s);
         if (s.bad) atomicMin(&hdr[p].err, FARM_EASSERT);
         if (s.nc > 0xFFFFu || s.nh > 0xFFFFu || s.nv > 0xFFFFu) atomicOr(ovf, 1);
         c16[e] = (uint16_t)s.nc;
@@ -799,8 +968,8 @@ __global__ void k_set_node_bases(PolyHdr *__restrict__ hdr, uint32_t npoly, cons
     }
 }
 
-__global__ void k_walk_count(const StoreView sv, PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off,
-                             Chunk ch, const uint32_t *__restrict__ perm, uint32_t *__restrict__ cnt) {
+__global__ void k_walk_count(const StoreView sv, PolyHdr *__restrict__ hdr, const WalkF *__restrict__ wf,
+                             const uint64_t *__restrict__ off, Chunk ch, const uint32_t *__restrict__ perm, uint32_t *__restrict__ cnt) {
     uint64_t n1 = ch.ne + 1;
     for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < ch.ne;
          j += (uint64_t)gridDim.x * blockDim.x) {
@@ -815,7 +984,7 @@ __global__ void k_walk_count(const StoreView sv, PolyHdr *__restrict__ hdr, cons
         if (h.err == 0) {
             uint32_t i = (uint32_t)(e - h.edge);
             const float2 *r = sv.ring + h.ring;
-            walk_edge(h, r[i], r[i + 1], s);
+            walk_edge(h, wf[p], r[i], r[i + 1], s);
         }
         if (s.bad) atomicMin(&hdr[p].err, FARM_EASSERT);
         cnt[k] = s.nc;
@@ -840,8 +1009,8 @@ __global__ void k_load_counts(const PolyHdr *__restrict__ hdr, const uint64_t *_
     }
 }
 
-__global__ void k_walk_fill(const StoreView sv, const PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off,
-                            Chunk ch, const uint32_t *__restrict__ perm, const uint64_t *__restrict__ scan,
+__global__ void k_walk_fill(const StoreView sv, const PolyHdr *__restrict__ hdr, const WalkF *__restrict__ wf,
+                            const uint64_t *__restrict__ off, Chunk ch, const uint32_t *__restrict__ perm, const uint64_t *__restrict__ scan,
                             uint32_t *from, uint32_t *to, uint32_t *cedge, uint64_t *hkey, double *hval,
                             uint64_t *vkey, double *vval) {
     uint64_t n1 = ch.ne + 1;
@@ -872,7 +1041,7 @@ __global__ void k_walk_fill(const StoreView sv, const PolyHdr *__restrict__ hdr,
         s.vval = vval;
         s.hline = h.hline - ch.h0;
         s.vline = h.vline - ch.v0;
-        walk_edge(h, r[i], r[i + 1], s);
+        walk_edge(h, wf[p], r[i], r[i + 1], s);
     }
 }
 
@@ -983,6 +1152,63 @@ __global__ void k_line_scatter(const uint64_t *__restrict__ key, const double *_
     }
 }
 
+// Grid-line node values sorted per line (Grid_line sorts each line's
+// crossings, Ideal.cpp:185-238). Each line's values are a few to a few
+// thousand doubles: one block sorts one line in shared memory by a bitonic
+// network on order-preserving 64-bit integer keys (the integer pipe, not
+// FP64 compares). Equal keys are equal doubles, so the network's lack of
+// stability is invisible; -0.0 sorts before +0.0. Lines longer than
+// kLineSortMax are listed for a library segmented sort.
+constexpr int kLineSortMax = 4096;
+
+__device__ inline uint64_t dkey(double v) {
+    const uint64_t b = (uint64_t)__double_as_longlong(v);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ inline double dval(uint64_t k) {
+    const uint64_t b = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
+    return __longlong_as_double((long long)b);
+}
+
+__global__ void __launch_bounds__(256) k_line_sort(const double *__restrict__ in, double *__restrict__ out,
+                                                   const uint64_t *__restrict__ start, uint64_t nseg,
+                                                   uint64_t *__restrict__ big_b, uint64_t *__restrict__ big_e,
+                                                   unsigned long long *__restrict__ nbig) {
+    __shared__ uint64_t sk[kLineSortMax];
+    for (uint64_t l = blockIdx.x; l < nseg; l += gridDim.x) {
+        const uint64_t b = start[l], n = start[l + 1] - b;
+        if (n == 0) continue;
+        if (n > (uint64_t)kLineSortMax) {
+            if (threadIdx.x == 0) {
+                const unsigned long long at = atomicAdd(nbig, 1ull);
+                big_b[at] = b;
+                big_e[at] = b + n;
+            }
+            continue;
+        }
+        uint32_t N = 1;
+        while (N < n) N <<= 1;
+        for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) sk[i] = i < n ? dkey(in[b + i]) : ~0ull;
+        __syncthreads();
+        for (uint32_t k = 2; k <= N; k <<= 1)
+            for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) {
+                    const uint32_t ixj = i ^ j;
+                    if (ixj > i) {
+                        const uint64_t x = sk[i], y = sk[ixj];
+                        if ((x > y) == ((i & k) == 0)) {
+                            sk[i] = y;
+                            sk[ixj] = x;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) out[b + i] = dval(sk[i]);
+        __syncthreads();
+    }
+}
+
 // Grid-line offsets (Ideal.cpp:185-238): lines with nodes get their start,
 // others keep 0; the end entries get the node count.
 __global__ void k_line_offsets(PolyHdr *__restrict__ hdr, Chunk ch, int vertical, const uint32_t *__restrict__ cnt,
@@ -1034,10 +1260,11 @@ __global__ void k_scanline(const PolyHdr *__restrict__ hdr, const uint64_t *__re
 }
 
 // Per edge: points contributed to every column (count pass or emit pass).
+// Both passes run the same arithmetic, so they agree point for point.
 __global__ void k_clipx(const StoreView sv, const PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off,
                         Chunk ch, const uint32_t *__restrict__ perm, const double *__restrict__ colx,
-                        uint32_t *__restrict__ cnt, const uint64_t *__restrict__ scan, uint64_t *__restrict__ okey,
-                        float2 *__restrict__ opt) {
+                        const LineF *__restrict__ colf, int cert, uint32_t *__restrict__ cnt,
+                        const uint64_t *__restrict__ scan, uint64_t *__restrict__ okey, float2 *__restrict__ opt) {
     for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < ch.ne;
          j += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t k = perm[j];
@@ -1051,20 +1278,22 @@ __global__ void k_clipx(const StoreView sv, const PolyHdr *__restrict__ hdr, con
         uint32_t i = (uint32_t)(e - h.edge);
         const float2 *r = sv.ring + h.ring;
         float2 A = r[i], B = r[i + 1];
-        double mnx = A.x < B.x ? A.x : B.x, mxx = A.x < B.x ? B.x : A.x;
-        double mg = fmargin(mnx, mxx);
+        const float mnx = A.x < B.x ? A.x : B.x, mxx = A.x < B.x ? B.x : A.x;
+        const float mg = fmargin_f(mnx, mxx);
+        const float vstart = __fsub_rn(mnx, mg), vend = __fadd_rn(mxx, mg);
         const double *lines = colx + h.col;
-        int c = first_line(lines, h.ncols, h.step_x, mnx - mg);
+        const LineF *lf = colf + h.col;
+        int c = first_line_f(lf, h.ncols, vstart);
         uint32_t total = 0;
         uint64_t at = scan ? scan[k] : 0;
         float2 buf[4];
         const ClipXEdge E(A, B);
-        double Xi = c < h.ncols ? lines[c] : 0.0;
-        float2 pi = mk(Xi, E.ord(Xi));
-        for (; c < h.ncols && Xi <= mxx + mg; c++) {
-            const double Xi1 = Xi + h.step_x;  // == lines[c + 1]
-            const float2 pi1 = mk(Xi1, E.ord(Xi1));
-            int m = clip_x_points(A, B, Xi, Xi1, pi, pi1, i == 0, okey ? buf : nullptr);
+        LineF L0 = lf[c];
+        float2 pi = make_float2(L0.rn, c < h.ncols ? E.ordf(lines[c], L0, cert) : 0.f);
+        for (; c < h.ncols && L0.dn <= vend; c++) {
+            const LineF L1 = lf[c + 1];  // the line Xi + step_x
+            const float2 pi1 = make_float2(L1.rn, E.ordf(lines[c + 1], L1, cert));
+            int m = clip_x_points(A, B, L0, L1, pi, pi1, i == 0, okey ? buf : nullptr);
             if (okey) {
                 for (int q = 0; q < m; q++) {
                     okey[at] = (h.col - ch.col0) + (uint64_t)c;
@@ -1073,7 +1302,7 @@ __global__ void k_clipx(const StoreView sv, const PolyHdr *__restrict__ hdr, con
                 }
             }
             total += (uint32_t)m;
-            Xi = Xi1;
+            L0 = L1;
             pi = pi1;
         }
         if (cnt) cnt[k] = total;
@@ -1306,11 +1535,13 @@ __global__ void k_cp_cost(const PolyHdr *__restrict__ hdr, const uint64_t *__res
 }
 
 // Per column-polygon edge: points contributed to each row (count or emit).
+// Both passes run the same arithmetic, so they agree point for point.
 __global__ void k_clipy(const PolyHdr *__restrict__ hdr, Chunk ch, const uint32_t *__restrict__ perm,
                         const uint64_t *__restrict__ cpstart, const float2 *__restrict__ cpoly,
                         const uint32_t *__restrict__ cpcol, const uint32_t *__restrict__ colpoly, uint64_t ncp,
-                        const double *__restrict__ rowy, uint32_t *__restrict__ cnt, const uint64_t *__restrict__ scan,
-                        uint64_t *__restrict__ okey, float2 *__restrict__ opt) {
+                        const double *__restrict__ rowy, const LineF *__restrict__ rowf, int cert,
+                        uint32_t *__restrict__ cnt, const uint64_t *__restrict__ scan, uint64_t *__restrict__ okey,
+                        float2 *__restrict__ opt) {
     for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < ncp; t += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t j = perm[t];
         const uint64_t c = cpcol[j];
@@ -1319,33 +1550,36 @@ __global__ void k_clipy(const PolyHdr *__restrict__ hdr, Chunk ch, const uint32_
             const PolyHdr &h = hdr[colpoly[c]];
             int x = (int)(c + ch.col0 - h.col);
             float2 A = cpoly[j], B = cpoly[j + 1];
-            double mny = A.y < B.y ? A.y : B.y, mxy = A.y < B.y ? B.y : A.y;
-            double mg = fmargin(mny, mxy);
+            const float mny = A.y < B.y ? A.y : B.y, mxy = A.y < B.y ? B.y : A.y;
+            const float mg = fmargin_f(mny, mxy);
+            const float vstart = __fsub_rn(mny, mg), vend = __fadd_rn(mxy, mg);
             const double *lines = rowy + h.row;
-            int r = first_line(lines, h.nrows, h.step_y, mny - mg);
+            const LineF *lf = rowf + h.row;
+            int r = first_line_f(lf, h.nrows, vstart);
             uint64_t at = scan ? scan[j] : 0;
             float2 buf[4];
             const ClipYEdge E(A, B);
-            const double isl = E.general() ? __drcp_rn(E.slope) : 0.0;
-            double Yi = r < h.nrows ? lines[r] : 0.0;
+            LineF L0 = lf[r];
             // the point on line Yi, carried from the previous row's Yi1
             // (horizontal edges take per-row abscissae instead)
-            float2 pc = make_float2(E.vert ? A.x : E.absc_f(Yi, isl), (float)Yi);
-            for (; r < h.nrows && Yi <= mxy + mg; r++) {
-                const double Yi1 = Yi + h.step_y;  // == lines[r + 1]
+            float2 pc = make_float2(E.vert ? A.x : (E.general() && r < h.nrows ? E.abscf(lines[r], L0, cert) : 0.f),
+                                    L0.rn);
+            for (; r < h.nrows && L0.dn <= vend; r++) {
+                const LineF L1 = lf[r + 1];  // the line Yi + step_y
                 float2 pi, pi1;
                 bool par = false;
                 if (E.horiz) {
-                    double xi, xi1;
-                    E.row(Yi, Yi1, 0.0, 0.0, xi, xi1, par);
-                    pi = mk(xi, Yi);
-                    pi1 = mk(xi1, Yi1);
+                    // the edge lies on a row line only if A.y equals that double exactly
+                    const bool on0 = L0.up == L0.dn && A.y == L0.rn, on1 = L1.up == L1.dn && A.y == L1.rn;
+                    pi = make_float2(on0 ? A.x : (on1 ? -INFINITY : 0.f), L0.rn);
+                    pi1 = make_float2(on0 ? -INFINITY : (on1 ? A.x : 0.f), L1.rn);
+                    par = !on0 && !on1;
                 } else {
                     pi = pc;
-                    pi1 = make_float2(E.vert ? A.x : E.absc_f(Yi1, isl), (float)Yi1);
+                    pi1 = make_float2(E.vert ? A.x : E.abscf(lines[r + 1], L1, cert), L1.rn);
                     pc = pi1;
                 }
-                int k = clip_y_points(A, B, Yi, Yi1, pi, pi1, par, okey ? buf : nullptr);
+                int k = clip_y_points(A, B, L0, L1, pi, pi1, par, okey ? buf : nullptr);
                 if (okey && k) {
                     uint64_t cell = (h.pix - ch.pix0) + (uint64_t)r * h.dimx + x;
                     for (int q = 0; q < k; q++) {
@@ -1355,21 +1589,62 @@ __global__ void k_clipy(const PolyHdr *__restrict__ hdr, Chunk ch, const uint32_
                     }
                 }
                 total += (uint32_t)k;
-                Yi = Yi1;
+                L0 = L1;
             }
         }
         if (cnt) cnt[j] = total;
     }
 }
 
+// The exact double value of the product of two finite floats, built on the
+// integer pipe: a 24 x 24-bit significand product fits a double's 53 bits, so
+// (double)a * (double)b is this value with no rounding, and it is assembled
+// from the significand product and the exponents instead of two conversions
+// and an FP64 multiply (GB300's FP64 pipe issues 2 lanes per clock per SM, its
+// integer pipe 64). Subnormal floats (exponent field 0) carry no implicit bit
+// and the exponent of 1; the result is always a normal double.
+__device__ __forceinline__ double exact_fmul(float a, float b) {
+    const uint32_t ua = __float_as_uint(a), ub = __float_as_uint(b);
+    uint32_t ea = (ua >> 23) & 0xFFu, eb = (ub >> 23) & 0xFFu;
+    if (ea == 0xFFu || eb == 0xFFu) return (double)a * (double)b;  // inf / nan: the FP64 rules
+    uint32_t ma = ua & 0x7FFFFFu, mb = ub & 0x7FFFFFu;
+    if (ea) ma |= 0x800000u; else ea = 1;
+    if (eb) mb |= 0x800000u; else eb = 1;
+    const uint64_t sign = (uint64_t)((ua ^ ub) & 0x80000000u) << 32;
+    const uint64_t m = (uint64_t)ma * mb;  // value = m * 2^(ea + eb - 300)
+    if (m == 0) return __longlong_as_double((long long)sign);
+    const int top = 63 - __clzll((long long)m);  // m in [2^top, 2^(top + 1)), top <= 47
+    const uint64_t frac = (m << (52 - top)) & 0xFFFFFFFFFFFFFull;
+    const uint64_t ex = (uint64_t)(top + (int)ea + (int)eb - 300 + 1023);
+    return __longlong_as_double((long long)(sign | (ex << 52) | frac));
+}
+
+// Cell-area schedule: pixels in order of their clip-point counts, heaviest
+// first (8-bit key, finer below 64 points), so that the lanes of a warp sum
+// runs of similar length. The order only schedules the sums.
+__global__ void k_cell_cost(const uint64_t *__restrict__ cellstart, uint64_t npix, uint8_t *__restrict__ key,
+                            uint32_t *__restrict__ idx) {
+    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < npix;
+         g += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t n = cellstart[g + 1] - cellstart[g];
+        const uint64_t k = n < 64 ? n : 64 + (n - 64) / 16;
+        key[g] = (uint8_t)(255 - (k < 255 ? k : 255));
+        idx[g] = (uint32_t)g;
+    }
+}
+
 // Per pixel: cell area (geometry_computation.h:275-297 over the cell's clip,
 // closed as Ideal.cpp:805-808 does) and the fill class (Ideal.cpp:880-914).
+// Each term is (double)p1.x * p2.y - (double)p2.x * p1.y: the two exact
+// products come from exact_fmul, so the FP64 pipe only takes the difference and
+// the running sum, in the reference's order.
 __global__ void k_cells(PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ pixbase, Chunk ch,
-                        const uint64_t *__restrict__ cellstart, const float2 *__restrict__ cpt,
-                        const uint64_t *__restrict__ cpstart, uint8_t *__restrict__ status,
-                        double *__restrict__ areas, int cc) {
-    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ch.npix;
-         g += (uint64_t)gridDim.x * blockDim.x) {
+                        const uint32_t *__restrict__ order, const uint64_t *__restrict__ cellstart,
+                        const float2 *__restrict__ cpt, const uint64_t *__restrict__ cpstart,
+                        uint8_t *__restrict__ status, double *__restrict__ areas, int cc) {
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < ch.npix;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t g = order ? order[t] : t;
         uint32_t p = ch.p0 + find_segment(pixbase + ch.p0, ch.np, g + ch.pix0);
         const PolyHdr &h = hdr[p];
         if (h.err) continue;
@@ -1384,10 +1659,11 @@ __global__ void k_cells(PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ 
         uint64_t m = n + (close ? 1 : 0);
         double area = 0.0;
         if (m >= 3) {
+            float2 p1 = cpt[b];
             for (uint64_t k = 0; k + 1 < m; k++) {
-                float2 p1 = cpt[b + k];
-                float2 p2 = (k + 1 < n) ? cpt[b + k + 1] : cpt[b];
-                area += ((double)p1.x * p2.y - (double)p2.x * p1.y);
+                const float2 p2 = (k + 1 < n) ? cpt[b + k + 1] : cpt[b];
+                area += exact_fmul(p1.x, p2.y) - exact_fmul(p2.x, p1.y);
+                p1 = p2;
             }
             area = fabs(area) / 2.0;
         }
@@ -1396,8 +1672,8 @@ __global__ void k_cells(PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ 
         uint8_t *st = status + h.st + id;
         uint8_t raw = *st;
         if (raw == 1) {
-            int t = type < cc - 2 ? type : cc - 2;
-            *st = (uint8_t)(t > 1 ? t : 1);
+            int t2 = type < cc - 2 ? type : cc - 2;
+            *st = (uint8_t)(t2 > 1 ? t2 : 1);
             areas[h.pix + id] = area;
         } else if (raw == 2) {
             *st = (uint8_t)(cc - 1);
@@ -1577,6 +1853,9 @@ struct RasterCtx {
     const uint64_t *doff;
     const uint64_t *scan;  // per polygon bases (pix, st, off, hline, vline, col, row, scanrow)
     double *colx, *rowy;
+    LineF *colf, *rowf;
+    WalkF *wf;  // per polygon: the walk's constants as double-floats
+    int cert = 1;  // clip points by certified double-float (0: FP64 throughout)
     int cc;
     int launches = 0;
     KTimer timer;
@@ -1620,7 +1899,7 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     if (R.counts_kept) {
         k_load_counts<<<gb(ne), 256, 0, st>>>(R.hdr, R.doff, ch, s->s[S_ECNT16].as<uint16_t>(), s->n_edges, ecnt);
     } else {
-        R.timer.time(T_WALK, st, [&] { k_walk_count<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, perm, ecnt); });
+        R.timer.time(T_WALK, st, [&] { k_walk_count<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.wf, R.doff, ch, perm, ecnt); });
     }
     uint64_t *ecnt64 = s->s[S_TMP_A].as<uint64_t>(), *escan = s->s[S_SCAN_E].as<uint64_t>();
     k_u32_to_u64<<<gb(3 * ne1), 256, 0, st>>>(ecnt, 3 * ne1, ecnt64);
@@ -1641,7 +1920,7 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     FARM_TRY(s->s[S_VNVAL].ensure(8 * nV + 16));
     uint32_t *cfrom = s->s[S_CFROM].as<uint32_t>(), *cto = s->s[S_CTO].as<uint32_t>(),
              *cedge = s->s[S_CEDGE].as<uint32_t>();
-    R.timer.time(T_WALK, st, [&] { k_walk_fill<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, perm, escan, cfrom, cto, cedge, s->s[S_HKEY].as<uint64_t>(),
+    R.timer.time(T_WALK, st, [&] { k_walk_fill<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.wf, R.doff, ch, perm, escan, cfrom, cto, cedge, s->s[S_HKEY].as<uint64_t>(),
                                         s->s[S_HVAL].as<double>(), s->s[S_VNKEY].as<uint64_t>(),
                                         s->s[S_VNVAL].as<double>()); });
     L++;
@@ -1712,10 +1991,21 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
         if (nn) {
             k_line_scatter<<<gb(nn), 256, 0, st>>>(key, val, nn, lstart, lfill, unsorted);
             L++;
-            FARM_TRY(cub_call(s, [&](void *t, size_t &b) {
-                return cub::DeviceSegmentedSort::SortKeys(t, b, unsorted, nodes_out, (int64_t)nn, (int64_t)nl, lstart,
-                                                          lstart + 1, st);
-            }));
+            FARM_TRY(s->s[S_LINEBIG].ensure(16 * (nl + 1) + 64));
+            uint64_t *big_b = s->s[S_LINEBIG].as<uint64_t>(), *big_e = big_b + (nl + 1);
+            unsigned long long *nbig = reinterpret_cast<unsigned long long *>(big_e + (nl + 1));
+            FARM_CUDA(cudaMemsetAsync(nbig, 0, 8, st));
+            unsigned lb = (unsigned)std::min<uint64_t>(nl, 8ull * sm_count());
+            k_line_sort<<<lb ? lb : 1, 256, 0, st>>>(unsorted, nodes_out, lstart, nl, big_b, big_e, nbig);
+            L++;
+            unsigned long long hbig = 0;
+            FARM_TRY(d2h(s, &hbig, nbig, 8));
+            if (hbig) {
+                FARM_TRY(cub_call(s, [&](void *t, size_t &b) {
+                    return cub::DeviceSegmentedSort::SortKeys(t, b, unsorted, nodes_out, (int64_t)nn, (int64_t)hbig,
+                                                              big_b, big_e, st);
+                }));
+            }
         }
         k_line_offsets<<<gb(ch.np), 256, 0, st>>>(R.hdr, ch, vert, lcnt, lstart,
                                                   vert ? s->d_voff.as<uint32_t>() : s->d_hoff.as<uint32_t>());
@@ -1733,7 +2023,7 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     FARM_CUDA(cudaMemsetAsync(xcnt, 0, 4 * ne1, st));
     const uint32_t *xperm = nullptr;
     FARM_TRY(edge_order(R, ch.p0, ch.np, ch.e0, ne, &xperm, 1));
-    R.timer.time(T_CLIPX, st, [&] { k_clipx<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, xperm, R.colx, xcnt, nullptr, nullptr, nullptr); });
+    R.timer.time(T_CLIPX, st, [&] { k_clipx<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, xperm, R.colx, R.colf, R.cert, xcnt, nullptr, nullptr, nullptr); });
     FARM_TRY(s->s[S_TMP_A].ensure(8 * ne1 + 16));
     uint64_t *x64 = s->s[S_TMP_A].as<uint64_t>();
     k_u32_to_u64<<<gb(ne1), 256, 0, st>>>(xcnt, ne1, x64);
@@ -1752,7 +2042,7 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     float2 *xpt = s->s[S_VVAL].as<float2>(), *xpt_s = s->s[S_VVAL2].as<float2>();
     const int colbits = key_bits(ch.ncol);
     if (nX) {
-        R.timer.time(T_CLIPX, st, [&] { k_clipx<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, xperm, R.colx, nullptr, xscan, xkey, xpt); });
+        R.timer.time(T_CLIPX, st, [&] { k_clipx<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, xperm, R.colx, R.colf, R.cert, nullptr, xscan, xkey, xpt); });
         L++;
         FARM_TRY(sort_pairs(s, xkey, xkey_s, reinterpret_cast<uint64_t *>(xpt), reinterpret_cast<uint64_t *>(xpt_s),
                             nX, colbits));
@@ -1880,7 +2170,7 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     uint32_t *ycnt = s->s[S_CNT_E].as<uint32_t>();
     FARM_CUDA(cudaMemsetAsync(ycnt, 0, 4 * (nCP + 1), st));
     if (nCP) {
-        R.timer.time(T_CLIPY, st, [&] { k_clipy<<<gb(nCP), 256, 0, st>>>(R.hdr, ch, yperm, cpstart, cpoly, cpcol, colpoly, nCP, R.rowy, ycnt,
+        R.timer.time(T_CLIPY, st, [&] { k_clipy<<<gb(nCP), 256, 0, st>>>(R.hdr, ch, yperm, cpstart, cpoly, cpcol, colpoly, nCP, R.rowy, R.rowf, R.cert, ycnt,
                                          nullptr, nullptr, nullptr); });
         L++;
     }
@@ -1901,8 +2191,8 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     uint64_t *ykb = s->s[S_VKEY].as<uint64_t>(), *yks = s->s[S_HKEY].as<uint64_t>();
     float2 *ypb = s->s[S_VVAL].as<float2>(), *yps = s->s[S_HVAL].as<float2>();
     if (nY) {
-        R.timer.time(T_CLIPY, st, [&] { k_clipy<<<gb(nCP), 256, 0, st>>>(R.hdr, ch, yperm, cpstart, cpoly, cpcol, colpoly, nCP, R.rowy,
-                                         nullptr, yscan, ykb, ypb); });
+        R.timer.time(T_CLIPY, st, [&] { k_clipy<<<gb(nCP), 256, 0, st>>>(R.hdr, ch, yperm, cpstart, cpoly, cpcol, colpoly, nCP, R.rowy, R.rowf,
+                                         R.cert, nullptr, yscan, ykb, ypb); });
         L++;
         FARM_TRY(sort_pairs(s, ykb, yks, reinterpret_cast<uint64_t *>(ypb), reinterpret_cast<uint64_t *>(yps), nY,
                             key_bits(ch.npix)));
@@ -1912,8 +2202,20 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     uint64_t *cellstart = s->s[S_TMP_A].as<uint64_t>();
     k_seg_starts<<<gb(nY + 1), 256, 0, st>>>(yks, nY, ch.npix, cellstart);
     L++;
-    R.timer.time(T_CELLS, st, [&] { k_cells<<<gb(ch.npix), 256, 0, st>>>(R.hdr, pixbase, ch, cellstart, yps, cpstart, s->d_status.as<uint8_t>(),
-                                         s->d_areas.as<double>(), R.cc); });
+    // cells heaviest first (the clip-point sort's buffers are free again)
+    uint32_t *corder = nullptr;
+    if (ch.npix) {
+        FARM_TRY(s->s[S_PERM_K].ensure(2 * ch.npix + 16));
+        FARM_TRY(s->s[S_PERM].ensure(8 * ch.npix + 16));
+        uint8_t *key = s->s[S_PERM_K].as<uint8_t>(), *key_s = key + ch.npix;
+        uint32_t *idx = s->s[S_PERM].as<uint32_t>(), *idx_s = idx + ch.npix;
+        k_cell_cost<<<gb(ch.npix), 256, 0, st>>>(cellstart, ch.npix, key, idx);
+        L++;
+        FARM_TRY(sort_pairs(s, key, key_s, idx, idx_s, ch.npix, 8));
+        corder = idx_s;
+    }
+    R.timer.time(T_CELLS, st, [&] { k_cells<<<gb(ch.npix), 256, 0, st>>>(R.hdr, pixbase, ch, corder, cellstart, yps, cpstart,
+                                         s->d_status.as<uint8_t>(), s->d_areas.as<double>(), R.cc); });
     L++;
 
     // ---- hierarchy
@@ -1988,6 +2290,8 @@ int rasterize(farm_store *s, const farm_raster_opts *o, int *launches) {
     FARM_TRY(s->d_voff.ensure(4 * totV + 16));
     FARM_TRY(s->s[S_COLX].ensure(8 * totCol + 16));
     FARM_TRY(s->s[S_ROWY].ensure(8 * totRow + 16));
+    FARM_TRY(s->s[S_COLXF].ensure(16 * totCol + 16));
+    FARM_TRY(s->s[S_ROWYF].ensure(16 * totRow + 16));
     FARM_CUDA(cudaMemsetAsync(s->d_status.p, 0, totStatus + 16, st));
     FARM_CUDA(cudaMemsetAsync(s->d_areas.p, 0, 8 * totP + 16, st));
     FARM_CUDA(cudaMemsetAsync(s->d_offset.p, 0, 4 * totOff + 16, st));
@@ -1995,7 +2299,17 @@ int rasterize(farm_store *s, const farm_raster_opts *o, int *launches) {
     FARM_CUDA(cudaMemsetAsync(s->d_voff.p, 0, 4 * totV + 16, st));
     R.colx = s->s[S_COLX].as<double>();
     R.rowy = s->s[S_ROWY].as<double>();
-    k_bases<<<gb(np), 256, 0, st>>>(R.hdr, np, scan, R.colx, R.rowy);
+    R.colf = s->s[S_COLXF].as<LineF>();
+    R.rowf = s->s[S_ROWYF].as<LineF>();
+    {
+        const char *ex = getenv("FARM_RASTER_EXACT");
+        R.cert = (ex && *ex && *ex != '0') ? 0 : 1;
+    }
+    k_bases<<<gb(np), 256, 0, st>>>(R.hdr, np, scan, R.colx, R.rowy, R.colf, R.rowf);
+    FARM_TRY(s->s[S_WALKF].ensure(sizeof(WalkF) * (uint64_t)np + 16));
+    R.wf = s->s[S_WALKF].as<WalkF>();
+    k_walkf<<<gb(np), 256, 0, st>>>(R.hdr, np, R.wf);
+    R.launches++;
     R.launches++;
 
     memset(&s->rtot, 0, sizeof s->rtot);
@@ -2028,7 +2342,7 @@ int rasterize(farm_store *s, const farm_raster_opts *o, int *launches) {
             const uint32_t *perm = nullptr;
             FARM_TRY(edge_order(R, pa, pb - pa, e0, n, &perm));
             R.timer.time(T_WALK, st,
-                         [&] { k_walk_tot<<<gb(n), 256, 0, st>>>(sv, R.hdr, R.doff, np, e0, n, perm, tot3,
+                         [&] { k_walk_tot<<<gb(n), 256, 0, st>>>(sv, R.hdr, R.wf, R.doff, np, e0, n, perm, tot3,
                                                                    c16, ne, ovf); });
             R.launches++;
         }

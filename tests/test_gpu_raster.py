@@ -150,3 +150,24 @@ def test_gpu_raster_small_point_tolerance(gpu_lib, vpr, seed):
         checked += 1
     st.close()
     assert checked >= ps.n // 2
+
+
+@pytest.mark.parametrize("scale,vpr", [(1.0, 10), (1.0, 64), (2500.0, 16), (0.01, 4)])
+def test_gpu_raster_certified_clip_equals_fp64_clip(gpu_lib, monkeypatch, scale, vpr):
+    """The fill clip's points come from certified double-float arithmetic, with
+    the reference's FP64 expression only where a float rounding midpoint lies
+    within the error bound. FARM_RASTER_EXACT=1 takes the FP64 expression for
+    every point: both give the same rasters, bit for bit, at coordinate scales
+    from 0.01 to 1e5 (and the oracle agrees with the certified path)."""
+    prm = P.StarParams(dom_lo=0.0, dom_hi=30.0 * scale, r_lo=0.05 * scale, r_hi=2.0 * scale, n_hi=4000)
+    ps = P.generate(prm, 70 + vpr, 120)
+    st_c, got_c = gpu_rasters(ps, vpr, False)
+    st_c.close()
+    monkeypatch.setenv("FARM_RASTER_EXACT", "1")
+    st_e, got_e = gpu_rasters(ps, vpr, False)
+    st_e.close()
+    for k in range(ps.n):
+        assert not raster_mismatches(got_c[k], got_e[k]), k
+    for k in range(0, ps.n, 7):
+        r = O.Raster(ps.ring(k), vpr, False).arrays()
+        assert not raster_mismatches(got_c[k], r), k
