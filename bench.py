@@ -4,24 +4,28 @@ Workload (configuration 2): seeded star polygons, 100,000 sources x
 1,000,000 targets, vertex count log-uniform 16..100,000, mean radius
 log-uniform 0.05..2.0, per-vertex radius x lognormal(0, 0.3); the domain side
 is calibrated so the MBR join yields ~20M candidate pairs. The job is cut into
-spatial strips by source centre: strip b holds the sources centred in it and
-the targets that reach them, and all of its candidate pairs. One "step" is
-one strip through the whole hot path — ring upload into the store's layout,
-rasterization of every polygon of the strip (stage a), pixel-pair filter +
-border refinement of every candidate (stages b, c), result bytes. Steps repeat
-the strip of this rank (the inputs are GBs, far larger than the 129 MB L2, so
-no L2 flush is needed).
+spatial strips by source centre: strip b holds the sources centred in it, the
+targets whose vertices reach the x-range of those sources' MBRs (an exact
+bound from the generator), and all of the strip's candidate pairs, so the
+strips partition the job's pairs. One "step" is one strip through the whole
+hot path — ring upload into the store's layout, rasterization of every
+polygon of the strip (stage a), pixel-pair filter + border refinement of every
+candidate (stages b, c), result bytes. Steps cycle through the rank's strips,
+so K >= the strip count covers the whole job; every strip's rings are
+resident in HBM before the timed region (the inputs are GBs, far larger than
+the 129 MB L2, so no L2 flush is needed).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Under torchrun each rank takes its own strip (weak scaling, no collective on
-the data path); value = all ranks' pairs / max rank time.
+Under torchrun each rank takes strips r, r + N, ... (weak scaling, no
+collective on the data path); value = all ranks' pairs / max rank time.
 --impl reference times the reference's CPU algorithm (the oracle port under
-oracle/, all host cores) on a bounded sample of the same workload.
+oracle/, all host cores) on bounded samples of the same job.
 """
 from __future__ import annotations
 
 import argparse
+import concurrent.futures as cf
 import json
 import math
 import os
@@ -43,6 +47,9 @@ UNIT = "pairs/s"
 # configuration 2
 N_SRC, N_TGT = 100_000, 1_000_000
 TARGET_PAIRS = 20_000_000
+# configuration-4 sample for the area block: polygons per pool and domain side
+AREA_POOL = 1500
+AREA_SIDE = 40.0
 
 
 def star_params(dom_hi):
@@ -58,7 +65,6 @@ def calibrate_domain(seed: int) -> float:
     unit-domain sample (sizes do not depend on the domain)."""
     from farm_gb300 import polygons as P
     prm = star_params(1.0)
-    prm.n_hi = 100_000
     a = P.generate(prm, seed + 7, 4000).mbrs()
     b = P.generate(prm, seed + 8, 4000).mbrs()
     wa, ha = a[:, 2] - a[:, 0], a[:, 3] - a[:, 1]
@@ -124,51 +130,42 @@ def log(msg: str) -> None:
     print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
 
 
-# every vertex of a generated polygon lies within this many mean radii of its
-# centre unless its lognormal factor exceeds exp(0.3 * 6.5) (probability ~4e-11)
-EXTENT_RADII = math.exp(0.3 * 6.5)
-# configuration-4 sample for the area block: polygons per pool and domain side
-AREA_POOL = 1500
-AREA_SIDE = 40.0
+# ------------------------------------------------------------------ job ----
+class Job:
+    """Configuration 2 cut into strips. Only centres and exact extents are held
+    for the whole job; a strip's rings are generated on demand."""
 
+    def __init__(self, seed: int, n_strips: int):
+        from farm_gb300 import polygons as P
+        from farm_gb300 import shard
+        self.seed, self.n_strips = seed, n_strips
+        self.L = calibrate_domain(seed)
+        self.prm = star_params(self.L)
+        t0 = time.time()
+        self.src_c = P.centres(self.prm, seed, N_SRC)
+        self.tgt_c = P.centres(self.prm, seed + 1, N_TGT)
+        # an interval that holds every vertex of each target (the generator's
+        # largest radius about the centre, widened by float rounding)
+        self.tgt_ext = shard.target_extents(self.tgt_c, P.radii(self.prm, seed + 1, N_TGT))
+        log(f"domain side {self.L:.2f}; exact target extents in {time.time() - t0:.1f} s")
 
-def build_workload(seed: int, strip: int, n_strips: int, vpr: int):
-    """Host (pinned) rings and candidate pairs of one strip of the job.
-
-    The domain is cut into n_strips vertical strips by source centre. Strip b
-    holds the sources centred in it and every target whose extent (centre +-
-    EXTENT_RADII x mean radius) reaches the x-range of the strip's source MBRs;
-    its pairs are the MBR-overlapping (source, target) pairs of those sets, so
-    every candidate pair of the job belongs to exactly one strip, and only
-    targets straddling a strip boundary are rasterized in two steps."""
-    import torch
-    from farm_gb300 import polygons as P
-    from farm_gb300 import shard
-
-    L = calibrate_domain(seed)
-    prm = star_params(L)
-    log(f"domain side {L:.2f}")
-    s_idx = shard.strip_sources(P.centres(prm, seed, N_SRC), strip, n_strips, L)
-
-    def gen_pinned(seed_, idx):
-        counts = P.vertex_counts(prm, seed_, idx)
-        off = torch.zeros(len(idx) + 1, dtype=torch.int64).pin_memory()
-        offn = off.numpy().view(np.uint64)
-        total = int(counts.sum(dtype=np.uint64))
-        xy = torch.empty((total, 2), dtype=torch.float32).pin_memory()
-        ps = P.generate_indices(prm, seed_, idx, out_off=offn, out_xy=xy.numpy())
-        return ps, off, xy
-
-    S, S_off_t, S_xy_t = gen_pinned(seed, s_idx)
-    ms = S.mbrs()
-    log(f"strip {strip}/{n_strips}: {S.n} sources, {S.total} vertices")
-    t_idx = shard.strip_targets(ms, P.centres(prm, seed + 1, N_TGT), EXTENT_RADII)
-    T, T_off_t, T_xy_t = gen_pinned(seed + 1, t_idx)
-    pairs = P.mbr_join(ms, T.mbrs())
-    log(f"targets: {T.n} ({T.total} vertices, {len(np.unique(pairs[:, 1]))} with candidates); "
-        f"candidates: {len(pairs)}")
-    return {"L": L, "S": S, "T": T, "pairs": pairs, "strip": strip, "n_strips": n_strips,
-            "pinned": (S_off_t, S_xy_t, T_off_t, T_xy_t)}
+    def strip(self, b: int, rings: bool = True) -> dict:
+        """Strip b: source and target generator indices, their rings (optional)
+        and the strip's candidate pairs (local indices, sorted by source)."""
+        from farm_gb300 import polygons as P
+        from farm_gb300 import shard
+        s_idx = shard.strip_sources(self.src_c, b, self.n_strips, self.L)
+        S = P.generate_indices(self.prm, self.seed, s_idx)
+        ms = S.mbrs()
+        t_idx = shard.strip_targets(ms, self.tgt_ext)
+        T = P.generate_indices(self.prm, self.seed + 1, t_idx)
+        pairs = P.mbr_join(ms, T.mbrs())
+        d = {"strip": b, "s_idx": s_idx, "t_idx": t_idx, "pairs": pairs,
+             "s_nv": np.diff(S.off.astype(np.int64)), "t_nv": np.diff(T.off.astype(np.int64)),
+             "vertices": int(S.total + T.total)}
+        if rings:
+            d["S"], d["T"] = S, T
+        return d
 
 
 def filter_bytes(stats: dict, n_pairs: int, bits: int) -> float:
@@ -178,65 +175,107 @@ def filter_bytes(stats: dict, n_pairs: int, bits: int) -> float:
     return n_pairs * (8 + 128 + 0.125) + bits / 8.0 * (stats["src_window_pixels"] + stats["tgt_window_pixels"])
 
 
-# Peaks. HBM: MEASURED_PEAKS.json (a STREAM-style copy on this GPU model).
-# FP64 / FP32: nominal issue rates, as no measured figure exists for them —
-# GB300 issues FP64 at 2 lanes/clock/SM (1.25 TFLOP/s counts an FMA as two
-# flops; these kernels cannot fuse, so every flop is one instruction) and FP32
-# at 128 lanes/clock/SM; 152 SMs at 2.07 GHz.
-FP64_PEAK = 2 * 152 * 2.07e9
-FP32_PEAK = 128 * 152 * 2.07e9
+# Fallback denominators when the device's own rates cannot be measured:
+# nominal issue rates, GB300 FP64 at 2 lanes/clock/SM and FP32 at 128, 152
+# SMs at 2.07 GHz (no kernel here fuses, so one flop is one instruction).
+FP64_NOMINAL = 2 * 152 * 2.07e9
+FP32_NOMINAL = 128 * 152 * 2.07e9
+
+# DRAM traffic per unit of the rasterizer's heavy kernels, from one ncu
+# capture each (dram__bytes_read.sum + dram__bytes_write.sum per launch, divided
+# by the units that launch processed); the capture command and the figures are
+# in profiles/k_walk_k_clip_small_strip.md. Per launch here = per unit x the
+# units of the measured launches.
+TRAFFIC_PER_UNIT = {
+    "edge_walk": None,   # bytes per edge (k_walk_tot + k_walk_fill)
+}
 
 
-def rooflines(rt: dict, qs: dict, n_pairs: int, stage: dict, steps: int) -> dict:
+def measured_peaks() -> dict:
+    """HBM from MEASURED_PEAKS.json; FP64 and FP32 measured now on this GPU
+    (farm_probe_issue_rates), else nominal."""
+    out = {}
+    try:
+        pk = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+        out["hbm"], out["hbm_src"] = float(pk["hbm_gbs"]) * 1e9, "MEASURED_PEAKS.json hbm_gbs (of measured)"
+    except Exception:
+        out["hbm"], out["hbm_src"] = 6.8e12, "fallback 6.8 TB/s (of fallback)"
+    try:
+        from farm_gb300.engine import issue_rates
+        r = max((issue_rates() for _ in range(2)), key=lambda d: d["fp64_ops_per_s"])
+        out["fp64"], out["fp32"] = r["fp64_ops_per_s"], r["fp32_ops_per_s"]
+        out["fp_src"] = "measured on this GPU by farm_probe_issue_rates (non-fused multiply/add chains; of measured)"
+    except Exception as e:
+        out["fp64"], out["fp32"] = FP64_NOMINAL, FP32_NOMINAL
+        out["fp_src"] = f"nominal issue rate (measurement failed: {e})"
+    return out
+
+
+def rooflines(rt: dict, qs: dict, n_pairs: float, stage: dict, steps: int, peaks: dict,
+              ref_tests: float | None) -> dict:
     """Roofline of each measured stage from its algorithmic work per unit
-    (counts of the last step; times are the per-step means of the timed steps).
+    (work summed over the timed steps; times are per-step means).
 
-    edge walk (2 launches per edge: totals + counts, then fill): FP64, 16 flops per edge
-      (endpoint cells, slope and intercept) + 16 per pixel-boundary crossing
-      (both branches of one walk step), the reference's arithmetic for ONE walk;
-    cell clip (count + emit): FP64, 4 flops per emitted clip point (slope and
-      the two line abscissae, shared by ~2 points per edge-row);
+    edge walk (k_walk_tot + k_walk_fill): FP64, 16 flops per edge (endpoint
+      cells, slope and intercept) + 16 per pixel-boundary crossing (both
+      branches of one walk step), the reference's arithmetic for ONE walk;
+    cell clip (count + emit): FP64, 4 flops per emitted clip point;
     column clip: FP64, 2 flops per emitted point;
     cell areas: FP64, 4 flops per clip point (shoelace term + accumulation);
-    filter + refine (k_intersect): FP32, 28 flops per segment-pair test
-      (4 cross products x 7); its HBM bytes per filter_bytes();
+    filter + refine (k_intersect): FP32, 28 flops per segment-pair test in the
+      reference's order with its early exit (counted by the oracle on the
+      parity sample and scaled to the step; the GPU's own test count is
+      reported beside it); its HBM bytes per filter_bytes();
     whole raster stage, HBM view: 8 B per vertex read + the raster written
       (w P / 8 + 4 (P + n) + 8 sequences + 8 nodes).
+    The whole path: sum over the two stages of max(bytes / HBM, flops64 /
+    FP64, flops32 / FP32), over the measured step time.
     """
-    peaks = {}
-    try:
-        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
-    except Exception:
-        pass
-    hbm = float(peaks.get("hbm_gbs", 6800.0)) * 1e9
+    hbm, p64, p32 = peaks["hbm"], peaks["fp64"], peaks["fp32"]
     per = lambda k: stage[k] / steps
-    walk_ms = rt["ms_walk"]
     st = {}
 
-    def fp(name, flops, ms, peak, kind, peak_src):
+    def fp(name, flops, ms, peak, kind):
         ach = flops / (ms * 1e-3) if ms > 0 else None
-        st[name] = {"bound": kind, "algorithmic_flops": flops, "kernel_ms": ms,
+        st[name] = {"bound": kind, "algorithmic_flops_per_step": flops, "kernel_ms": ms,
                     "achieved": ach / 1e12 if ach else None, "peak": peak / 1e12, "unit": "TFLOP/s",
-                    "frac": ach / peak if ach else None, "peak_source": peak_src}
+                    "frac": ach / peak if ach else None, "peak_source": peaks["fp_src"]}
 
-    src64 = "nominal FP64 issue rate (no measured FP64 figure in MEASURED_PEAKS.json)"
-    fp("edge_walk", 16.0 * rt["vertices"] + 16.0 * rt["crossings"], walk_ms, FP64_PEAK, "fp64", src64)
-    fp("cell_clip", 4.0 * rt["clip_y_points"], rt["ms_clip_y"], FP64_PEAK, "fp64", src64)
-    fp("column_clip", 2.0 * rt["clip_x_points"], rt["ms_clip_x"], FP64_PEAK, "fp64", src64)
-    fp("cell_area", 4.0 * rt["clip_y_points"], rt["ms_cells"], FP64_PEAK, "fp64", src64)
-    fp("refine", 28.0 * qs["segment_tests"], per("query_ms"), FP32_PEAK, "fp32",
-       "nominal FP32 issue rate (no measured FP32 figure in MEASURED_PEAKS.json)")
-    fb = filter_bytes(qs, n_pairs, 4)
-    rb = 8.0 * rt["vertices"] + 0.5 * rt["pixels"] + 4.0 * (rt["pixels"] + rt["polygons"]) + \
-        8.0 * rt["sequences"] + 8.0 * (rt["hnodes"] + rt["vnodes"])
-    rms = per("raster_ms")
-    st["raster_hbm_view"] = {"bound": "hbm", "algorithmic_bytes": rb, "kernel_ms": rms,
+    f_walk = (16.0 * rt["vertices"] + 16.0 * rt["crossings"]) / steps
+    f_clipy = 4.0 * rt["clip_y_points"] / steps
+    f_clipx = 2.0 * rt["clip_x_points"] / steps
+    f_cells = 4.0 * rt["clip_y_points"] / steps
+    fp("edge_walk", f_walk, rt["ms_walk"] / steps, p64, "fp64")
+    fp("cell_clip", f_clipy, rt["ms_clip_y"] / steps, p64, "fp64")
+    fp("column_clip", f_clipx, rt["ms_clip_x"] / steps, p64, "fp64")
+    fp("cell_area", f_cells, rt["ms_cells"] / steps, p64, "fp64")
+    gpu_tests = qs["segment_tests"] / steps
+    tests = ref_tests / steps if ref_tests else gpu_tests
+    fp("refine", 28.0 * tests, per("query_ms"), p32, "fp32")
+    st["refine"]["segment_tests_reference_order"] = tests if ref_tests else None
+    st["refine"]["segment_tests_gpu"] = gpu_tests
+    if ref_tests:
+        st["refine"]["gpu_tests_over_reference_order"] = gpu_tests / tests
+    fb = filter_bytes(qs, n_pairs, 4) / steps
+    rb = (8.0 * rt["vertices"] + 0.5 * rt["pixels"] + 4.0 * (rt["pixels"] + rt["polygons"]) +
+          8.0 * rt["sequences"] + 8.0 * (rt["hnodes"] + rt["vnodes"])) / steps
+    rms, qms = per("raster_ms"), per("query_ms")
+    st["raster_hbm_view"] = {"bound": "hbm", "algorithmic_bytes_per_step": rb, "kernel_ms": rms,
                              "achieved": rb / (rms * 1e-3) / 1e9 if rms > 0 else None, "peak": hbm / 1e9,
                              "unit": "GB/s", "frac": rb / (rms * 1e-3) / hbm if rms > 0 else None,
-                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
-    st["filter_hbm_view"] = {"bound": "hbm", "algorithmic_bytes": fb, "kernel_ms": per("query_ms"),
-                             "achieved": fb / (per("query_ms") * 1e-3) / 1e9 if per("query_ms") > 0 else None,
-                             "peak": hbm / 1e9, "unit": "GB/s", "peak_source": "MEASURED_PEAKS.json hbm_gbs"}
+                             "peak_source": peaks["hbm_src"]}
+    st["filter_hbm_view"] = {"bound": "hbm", "algorithmic_bytes_per_step": fb, "kernel_ms": qms,
+                             "achieved": fb / (qms * 1e-3) / 1e9 if qms > 0 else None,
+                             "peak": hbm / 1e9, "unit": "GB/s", "frac": fb / (qms * 1e-3) / hbm if qms > 0 else None,
+                             "peak_source": peaks["hbm_src"]}
+    raster_floor = max(rb / hbm, (f_walk + f_clipy + f_clipx + f_cells) / p64)
+    query_floor = max(fb / hbm, 28.0 * tests / p32)
+    step_s = per("step_ms") * 1e-3
+    st["whole_path"] = {"roofline_ms": (raster_floor + query_floor) * 1e3, "step_ms": step_s * 1e3,
+                        "frac": (raster_floor + query_floor) / step_s if step_s > 0 else None,
+                        "stages": {"raster": {"roofline_ms": raster_floor * 1e3, "measured_ms": rms},
+                                   "filter_refine": {"roofline_ms": query_floor * 1e3, "measured_ms": qms}},
+                        "formula": "sum over stages of max(bytes/HBM, flops64/FP64, flops32/FP32) / step time"}
     # the dominant kernel: the stage with the most device time
     cand = {k: v for k, v in st.items() if k in ("edge_walk", "cell_clip", "column_clip", "cell_area", "refine")}
     name = max(cand, key=lambda k: cand[k]["kernel_ms"] or 0.0)
@@ -244,11 +283,15 @@ def rooflines(rt: dict, qs: dict, n_pairs: int, stage: dict, steps: int) -> dict
     dom["kernel"] = {"edge_walk": "k_walk_tot + k_walk_fill", "cell_clip": "k_clipy (count + emit)",
                      "column_clip": "k_clipx (count + emit)", "cell_area": "k_cells",
                      "refine": "k_intersect (filter + refine)"}[name]
-    dom["traffic"] = None
-    dom["peak"] = dom["peak"]
+    units = {"edge_walk": rt["vertices"] / steps}
+    tpu = TRAFFIC_PER_UNIT.get(name)
+    dom["traffic"] = tpu * units[name] if tpu and name in units else None
+    dom["traffic_note"] = ("ncu dram bytes per unit x units per step (profiles/)" if dom["traffic"] else
+                           "no ncu capture of this kernel's DRAM bytes")
     return {"dominant": dom, "stages": st}
 
 
+# ------------------------------------------------------- learned scorer ----
 def choose_band(prob: np.ndarray, y: np.ndarray, budget: float, positives: int = 0) -> tuple:
     """Narrowest band (lo, hi) whose decided pairs stay within the error
     budget on held-out pairs: at most budget x positives false positives above
@@ -302,13 +345,12 @@ def train_scorer(args, store, dev) -> dict:
     """Train the learned scorer on pairs of a strip drawn with a separate seed,
     labelled by the exact path, and set its band from held-out pairs."""
     import torch
-    Wt = build_workload(args.seed + 1000, 0, args.strips, args.vpr)
-    so, sx, to, tx = (t.to(dev) for t in Wt["pinned"])
-    pairs = Wt["pairs"]
-    store.load(0, so, sx)
-    store.load(1, to, tx)
+    Jt = Job(args.seed + 1000, args.strips)
+    sd = Jt.strip(0)
+    S, T, pairs = sd["S"], sd["T"], sd["pairs"]
+    store.load_sets(S, T)
     store.rasterize(vpr=args.vpr, category_count=16, strict=False)
-    from farm_gb300.engine import MODE_FILTER
+    del S, T, sd
     dp = torch.from_numpy(pairs.view(np.int32)).to(dev).view(len(pairs), 2)
     lab, _ = store.intersect(dp)
     code, cost = store.filter_costs(dp)  # the scorer only sees pairs the filter leaves (3)
@@ -342,7 +384,7 @@ def train_scorer(args, store, dev) -> dict:
         inband = float(((prob > lo) & (prob < hi)).mean()) if len(prob) else 0.0
         log(f"scorer trained on {len(tr)} pairs in {train_s:.1f}s (loss {loss:.4f}); band ({lo:.4f}, {hi:.4f}) "
             f"from {len(val)} held-out pairs, {inband:.3f} of them inside it")
-    del so, sx, to, tx, dp, lab, code, cost
+    del dp, lab, code, cost
     torch.cuda.empty_cache()
     return {"train_pairs": int(len(tr)), "heldout_pairs": int(len(val)), "epochs": args.learned_epochs,
             "heldout_inside_band": inband, "band_kind": args.learned_band, "cost_lambda": lam,
@@ -363,7 +405,7 @@ def pr(out, ref):
 
 
 def learned_eval(store, d_pairs, exact_out, exact_query_ms: float, raster_ms: float, reps: int) -> dict:
-    """Learned mode and the -a heuristic on the step's pairs, against exact."""
+    """Learned mode and the -a heuristic on one strip's pairs, against exact."""
     import torch
     from farm_gb300.engine import MODE_APPROX, MODE_LEARNED
     res = {}
@@ -400,6 +442,18 @@ def learned_eval(store, d_pairs, exact_out, exact_query_ms: float, raster_ms: fl
     return res
 
 
+# ------------------------------------------------------------ GPU arm ----
+def workload_config(job: Job, args, strips: list, n_pairs: int, vertices: int) -> dict:
+    cfg = {"workload": "intersect, configuration 2: 100k sources x 1M targets, nv log-uniform 16..100000, "
+                       f"~20M MBR candidates, -v {args.vpr}, -w 16 (category_count 16); the job is cut into "
+                       f"{job.n_strips} strips by source centre, one step = one strip (sources centred in it + "
+                       "every target reaching them), steps cycle through the rank's strips",
+           "domain_side": job.L, "vpr": args.vpr, "category_count": 16, "n_source": N_SRC, "n_target": N_TGT,
+           "strips": job.n_strips, "strips_timed": strips, "candidate_pairs_in_strips": n_pairs,
+           "vertices_in_strips": vertices, "l2": "inputs larger than L2 (no flush needed)", "seed": args.seed}
+    return cfg
+
+
 def run_ours(args) -> dict:
     import torch
     import torch.distributed as dist
@@ -414,50 +468,71 @@ def run_ours(args) -> dict:
     from farm_gb300.engine import Store
 
     dev = torch.device("cuda", local)
+    peaks = measured_peaks()
     store = Store()
     learned_train = train_scorer(args, store, dev) if args.learned else None
     mine = shard.strips_of_rank(rank, world, args.strips)
     if not mine:
         raise SystemExit(f"{world} ranks need at least {world} strips (--strips {args.strips})")
-    W = build_workload(args.seed, mine[0], args.strips, args.vpr)
-    S, T, pairs = W["S"], W["T"], W["pairs"]
-    S_off_t, S_xy_t, T_off_t, T_xy_t = W["pinned"]
-    d = {k: v.to(dev) for k, v in (("so", S_off_t), ("sx", S_xy_t), ("to", T_off_t), ("tx", T_xy_t))}
-    d_pairs = torch.from_numpy(pairs.view(np.int32)).to(dev)
-    d_out = torch.empty(len(pairs), dtype=torch.uint8, device=dev)
-    h_out = torch.empty(len(pairs), dtype=torch.uint8).pin_memory()
-    h_pairs = torch.from_numpy(pairs.view(np.int32)).pin_memory()
+    job = Job(args.seed, args.strips)
+    # the strips the warm-up and timed steps visit (all of this rank's once
+    # K >= their count), resident in HBM: rings, offsets, pairs, results
+    n_used = min(len(mine), max(args.steps, args.warmup, 1))
+    strips = []
+    t0 = time.time()
+    for b in mine[:n_used]:
+        sd = job.strip(b)
+        S, T = sd.pop("S"), sd.pop("T")
+        sd["so"], sd["to"] = S.off, T.off
+        sd["d_so"] = torch.from_numpy(S.off.view(np.int64)).to(dev)
+        sd["d_sx"] = torch.from_numpy(S.xy).to(dev)
+        sd["d_to"] = torch.from_numpy(T.off.view(np.int64)).to(dev)
+        sd["d_tx"] = torch.from_numpy(T.xy).to(dev)
+        sd["d_pairs"] = torch.from_numpy(sd["pairs"].view(np.int32)).to(dev).view(len(sd["pairs"]), 2)
+        sd["d_out"] = torch.empty(len(sd["pairs"]), dtype=torch.uint8, device=dev)
+        sd["xy_bytes"] = (S.total + T.total) * 8
+        del S, T
+        strips.append(sd)
+        log(f"strip {b}: {len(sd['s_idx'])} sources, {len(sd['t_idx'])} targets, {sd['vertices']} vertices, "
+            f"{len(sd['pairs'])} candidates")
+    log(f"{len(strips)} strips resident in HBM after {time.time() - t0:.1f} s")
+    order = [strips[i % len(strips)] for i in range(max(args.steps, 1))]
+    warm = [strips[i % len(strips)] for i in range(args.warmup)]
 
     stage = {"load_ms": 0.0, "raster_ms": 0.0, "query_ms": 0.0}
+    rsum, qsum = {}, {}
 
-    def step_device(timed=False):
+    def acc(dst, src):
+        for k, v in src.items():
+            if isinstance(v, (int, float)):
+                dst[k] = dst.get(k, 0) + v
+
+    def step_device(sd, timed=False):
         store.event_record(4)
-        store.load(0, d["so"], d["sx"])
-        store.load(1, d["to"], d["tx"])
+        store.load(0, sd["d_so"], sd["d_sx"])
+        store.load(1, sd["d_to"], sd["d_tx"])
         store.event_record(5)
         store.rasterize(vpr=args.vpr, category_count=16, strict=False)
-        if timed:
-            stage["load_ms"] += store.event_elapsed(4, 5)
+        load_ms = store.event_elapsed(4, 5)
         store.event_record(4)
-        _, found = store.intersect(d_pairs.view(len(pairs), 2), out=d_out)
+        _, found = store.intersect(sd["d_pairs"], out=sd["d_out"])
+        sd["raster_ms"] = store.event_elapsed(5, 4)
+        sd["query_ms"] = store.last_stats["ms_total"]
         if timed:
-            stage["raster_ms"] += store.event_elapsed(5, 4)
-            stage["query_ms"] += store.last_stats["ms_total"]
+            stage["load_ms"] += load_ms
+            stage["raster_ms"] += sd["raster_ms"]
+            stage["query_ms"] += sd["query_ms"]
+            acc(rsum, store.raster_totals())
+            acc(qsum, store.last_stats)
+        sd["found"] = found
         return found
 
-    def step_e2e():
-        store.load(0, S_off_t.numpy().view(np.uint64), S_xy_t.numpy())
-        store.load(1, T_off_t.numpy().view(np.uint64), T_xy_t.numpy())
-        store.rasterize(vpr=args.vpr, category_count=16, strict=False)
-        _, found = store.intersect(h_pairs.numpy().view(np.uint32).reshape(-1, 2), out=h_out.numpy())
-        return found
-
-    for i in range(args.warmup):
+    for i, sd in enumerate(warm):
         t = time.time()
-        step_device()
+        step_device(sd)
         free, total = torch.cuda.mem_get_info(dev)
-        log(f"warmup step {i}: {time.time() - t:.2f}s, device memory in use {(total - free) / 2**30:.1f} GiB, "
-            f"raster {store.raster_totals()}, stats {store.last_stats}")
+        log(f"warmup step {i} (strip {sd['strip']}): {time.time() - t:.2f}s, device memory in use "
+            f"{(total - free) / 2**30:.1f} GiB, raster {store.raster_totals()}, stats {store.last_stats}")
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
@@ -465,67 +540,133 @@ def run_ours(args) -> dict:
     clocks.start()
     launches0 = store.launches
     store.event_record(0)
-    founds = []
-    for _ in range(args.steps):
-        founds.append(step_device(timed=True))
+    for sd in order:
+        step_device(sd, timed=True)
     store.event_record(1)
     ms = store.event_elapsed(0, 1)
     torch.cuda.synchronize()
     launches = store.launches - launches0
-    last = dict(store.last_stats)
     if world > 1:
         dist.barrier()
     clk = clocks.stop()
+    stage["step_ms"] = ms
     t_dev = ms / 1000.0
-    # end to end through the C ABI with host buffers
-    step_e2e()
+    pairs_timed = sum(len(sd["pairs"]) for sd in order)
+
+    # end to end through the C ABI with host buffers: the step's rings come
+    # from pinned host memory (two buffers; the next step's is refilled from
+    # HBM during the current step, inside the timed region) and the result
+    # bytes go back to pinned host memory
+    cap = max(sd["xy_bytes"] for sd in strips) // 4
+    hbuf = [torch.empty(cap, dtype=torch.float32).pin_memory() for _ in range(2)]
+    hout = torch.empty(max(len(sd["pairs"]) for sd in strips), dtype=torch.uint8).pin_memory()
+    hpairs = {sd["strip"]: torch.from_numpy(sd["pairs"].view(np.int32)).pin_memory() for sd in strips}
+    side = torch.cuda.Stream(dev)
+
+    def refill(buf, sd):
+        ns = sd["d_sx"].numel()
+        with torch.cuda.stream(side):
+            buf[:ns].copy_(sd["d_sx"].view(-1), non_blocking=True)
+            buf[ns:ns + sd["d_tx"].numel()].copy_(sd["d_tx"].view(-1), non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(side)
+        return ev
+
+    def step_e2e(sd, buf):
+        ns, nt = sd["d_sx"].numel(), sd["d_tx"].numel()
+        store.load(0, sd["so"], buf[:ns].numpy().reshape(-1, 2))
+        store.load(1, sd["to"], buf[ns:ns + nt].numpy().reshape(-1, 2))
+        store.rasterize(vpr=args.vpr, category_count=16, strict=False)
+        n = len(sd["pairs"])
+        _, found = store.intersect(hpairs[sd["strip"]].numpy().view(np.uint32).reshape(-1, 2), out=hout[:n].numpy())
+        return found
+
+    refill(hbuf[0], order[0]).synchronize()
+    step_e2e(order[0], hbuf[0])  # warm-up of the host path
+    refill(hbuf[0], order[0]).synchronize()
     torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
     store.event_record(2)
-    for _ in range(args.steps):
-        step_e2e()
+    t_e2e0 = time.perf_counter()
+    for i, sd in enumerate(order):
+        ev = refill(hbuf[(i + 1) % 2], order[(i + 1) % len(order)]) if i + 1 < len(order) else None
+        step_e2e(sd, hbuf[i % 2])
+        if ev is not None:
+            ev.synchronize()
     store.event_record(3)
     ms_e2e = store.event_elapsed(2, 3)
-    t_e2e = ms_e2e / 1000.0
-    t_dev, t_e2e, total_pairs = shard.reduce_job(t_dev, t_e2e, len(pairs), device=dev)
-    value = total_pairs * args.steps / t_dev
-    e2e_value = total_pairs * args.steps / t_e2e
-    rl = rooflines(store.raster_totals(), last, len(pairs), stage, args.steps)
-    h2d = int(S_xy_t.numel() * 4 + T_xy_t.numel() * 4 + S_off_t.numel() * 8 + T_off_t.numel() * 8 + pairs.nbytes)
+    wall_e2e = time.perf_counter() - t_e2e0
+    t_e2e = max(ms_e2e / 1000.0, wall_e2e)
+    if world > 1:
+        dist.barrier()
+    t_dev, t_e2e, total_pairs = shard.reduce_job(t_dev, t_e2e, pairs_timed, device=dev)
+    value = total_pairs / t_dev
+    e2e_value = total_pairs / t_e2e
+    h2d = int(sum(sd["xy_bytes"] + 8 * (len(sd["so"]) + len(sd["to"])) + sd["pairs"].nbytes for sd in order)
+              / len(order))
+    d2h = int(sum(len(sd["pairs"]) for sd in order) / len(order))
+    del hbuf
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64", "data": "synthetic (seeded star polygons, configuration 2 generator)",
-        "config": {"workload": "intersect, configuration 2: 100k sources x 1M targets, nv log-uniform 16..100000, "
-                               f"~20M MBR candidates, -v {args.vpr}, -w 16; one step = strip {W['strip']} of "
-                               f"{W['n_strips']} (sources centred in it + the targets reaching them)",
-                   "domain_side": W["L"], "vpr": args.vpr, "category_count": 16, "n_source": N_SRC,
-                   "n_target": N_TGT, "strips": W["n_strips"], "sources_per_step": int(S.n),
-                   "targets_per_step": int(T.n), "candidate_pairs_per_step": len(pairs), "found_per_step": founds[-1],
-                   "vertices_per_step": int(S.total + T.total), "l2": "inputs larger than L2 (no flush needed)",
-                   "seed": args.seed, "parallelism": f"weak-dp{world}"},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": int(len(pairs))},
+        "config": workload_config(job, args, [sd["strip"] for sd in order], pairs_timed,
+                                  sum(sd["vertices"] for sd in order)),
+        "found_in_timed_steps": int(sum(sd.get("found", 0) for sd in order)),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "note": "rings + pairs H2D from pinned host memory and result bytes D2H, every step; the next "
+                        "step's pinned rings are refilled from HBM during the step (inside the timed region)"},
         "gpu_launches": int(launches),
         "clocks": clk,
-        "roofline": rl["dominant"],
-        "stages": rl["stages"],
         "stage_ms": {"load": stage["load_ms"] / args.steps, "raster": stage["raster_ms"] / args.steps,
                      "filter_refine": stage["query_ms"] / args.steps, "step": ms / args.steps},
+        "peaks": {"hbm_gbs": peaks["hbm"] / 1e9, "fp64_tops": peaks["fp64"] / 1e12, "fp32_tops": peaks["fp32"] / 1e12,
+                  "fp_source": peaks["fp_src"]},
     }
+    # learned mode on the first strip (rasterized again, outside the timed region)
+    sd0 = strips[0]
+    step_device(sd0)
+    heavy = None
+    if rank == 0:
+        code, cost = store.filter_costs(sd0["d_pairs"])
+        heavy = heavy_pairs(cost.cpu().numpy(), args.seed)
     if learned_train is not None and rank == 0:
-        lr_ = learned_eval(store, d_pairs.view(len(pairs), 2), d_out, stage["query_ms"] / args.steps,
-                           stage["raster_ms"] / args.steps, reps=3)
+        lr_ = learned_eval(store, sd0["d_pairs"], sd0["d_out"], sd0["query_ms"], sd0["raster_ms"], reps=3)
+        lr_["strip"] = sd0["strip"]
         lr_["train"] = learned_train
-        lr_["note"] = ("query = stages b-c on the rasterized strip (learned: predict + band + exact refinement of "
+        lr_["note"] = ("query = stages b-c on one rasterized strip (learned: predict + band + exact refinement of "
                        "abstentions); step adds the strip's rasterization, which both modes need")
         result["learned"] = lr_
+    ref_tests = None
     if rank == 0 and not args.no_cpu_baseline:
-        result["cpu_baseline"] = cpu_baseline(W, args, budget_s=args.cpu_seconds, threads=1, gpu_out=h_out.numpy())
+        gpu_out = {sd["strip"]: sd["d_out"].cpu().numpy() for sd in strips}
+        cb = cpu_baseline(job, strips, args, threads=os.cpu_count() or 1, gpu_out=gpu_out,
+                          heavy=(sd0["strip"], heavy))
+        # reference-order segment tests per pair (the oracle's count, early exit) scaled to the timed steps
+        if cb.get("ref_tests_per_pair"):
+            ref_tests = cb["ref_tests_per_pair"] * pairs_timed
+        result["cpu_baseline"] = cb
+    rl = rooflines(rsum, qsum, pairs_timed, stage, args.steps, peaks, ref_tests)
+    result["roofline"] = rl["dominant"]
+    result["stages"] = rl["stages"]
     store.close()
+    del strips
+    torch.cuda.empty_cache()
     if rank == 0 and args.area_pairs > 0:
         result["area"] = area_eval(args)
     if world > 1:
         dist.destroy_process_group()
     return result if rank == 0 else None
+
+
+def heavy_pairs(cost: np.ndarray, seed: int, frac: float = 0.01, take: int = 100) -> np.ndarray:
+    """`take` pairs drawn at random from the heaviest `frac` of a strip's pairs
+    by the filter's refinement cost proxy (local pair indices)."""
+    n = len(cost)
+    top = np.argsort(-cost, kind="stable")[:max(int(frac * n), 1)]
+    rng = np.random.default_rng(seed + 98)
+    return np.sort(rng.permutation(top)[:take])
 
 
 def area_eval(args) -> dict:
@@ -579,103 +720,251 @@ def area_eval(args) -> dict:
             "nonzero_areas": int((out > 0).sum()), "rasterize_s": ras_s}
 
 
-def _oracle_chunk(job):
-    """Worker: oracle rasterization + intersect over a list of sampled pairs."""
-    import time as _t
-    sys.path.insert(0, str(ROOT))
-    from oracle import oracle as O
-    rings_s, rings_t, pairs, vpr = job
+# ------------------------------------------------------- CPU baseline ----
+# The CPU side runs the oracle (a C port of the reference's algorithm) on
+# threads: ctypes releases the GIL, so T threads use T cores at once.
+class CpuSample:
+    """Bounded samples of the job for the CPU oracle.
 
-    def ras(r):
-        try:
-            return O.Raster(r, vpr)
-        except RuntimeError:  # the reference aborts on this polygon
-            return None
+    * raster sample: a systematic sample of the strips' polygons (sources and
+      targets of every strip, a target counted once per strip that holds it,
+      as the job rasterizes it) in order of vertex count, so every size class
+      is represented; each sampled polygon stands for `k` polygons;
+    * query sample: sources drawn uniformly at random from the strips, with
+      all of their candidate pairs (a cluster sample of the pairs), until at
+      least `min_pairs` pairs; plus optional extra pairs (the heavy stratum),
+      which are checked for parity but not used in the rate.
+    """
 
-    t0 = _t.perf_counter()
-    rs = {k: ras(r) for k, r in rings_s.items()}
-    rt = {k: ras(r) for k, r in rings_t.items()}
-    t1 = _t.perf_counter()
-    res = [2 if rs[s] is None or rt[t] is None else int(O.intersect(rs[s], rt[t])) for s, t in pairs]
-    t2 = _t.perf_counter()
-    verts = sum(len(r) for r in rings_s.values()) + sum(len(r) for r in rings_t.values())
-    return t1 - t0, t2 - t1, verts, len(pairs), sum(v == 1 for v in res), [(s, t, int(v)) for (s, t), v in zip(pairs, res)]
+    def __init__(self, job: Job, strips: list, seed: int):
+        self.job, self.strips = job, strips
+        self.rng = np.random.default_rng(seed + 99)
+        # every (strip position, side, local index) with its vertex count
+        self.poly = np.concatenate([
+            np.stack([np.full(len(sd[key]), i), np.full(len(sd[key]), side), np.arange(len(sd[key])), sd[key]], 1)
+            for i, sd in enumerate(strips) for side, key in ((0, "s_nv"), (1, "t_nv"))]).astype(np.int64)
+        self.poly_sorted = self.poly[np.argsort(self.poly[:, 3], kind="stable")]
+        self.n_pairs = sum(len(sd["pairs"]) for sd in strips)
 
+    def raster_sample(self, n: int, offset_seed: int) -> tuple[np.ndarray, int]:
+        N = len(self.poly_sorted)
+        k = max(N // max(n, 1), 1)
+        off = int(np.random.default_rng(offset_seed).integers(k))
+        return self.poly_sorted[off::k], k
 
-def cpu_baseline(W, args, budget_s: float, threads: int, gpu_out=None) -> dict:
-    """The CPU oracle (a port of the reference's algorithm) on a bounded uniform
-    sample of the step's candidate pairs. Raster time is charged per vertex and
-    query time per pair, then scaled to the whole step."""
-    import multiprocessing as mp
-    S, T, pairs = W["S"], W["T"], W["pairs"]
-    rng = np.random.default_rng(args.seed + 99)
-    order = rng.permutation(len(pairs))
-    chunk = 8
-
-    def job(k):
-        sel = pairs[order[k:k + chunk]]
-        rs = {int(s): np.ascontiguousarray(S.ring(int(s))) for s in set(sel[:, 0].tolist())}
-        rt = {int(t): np.ascontiguousarray(T.ring(int(t))) for t in set(sel[:, 1].tolist())}
-        return (rs, rt, [(int(a), int(b)) for a, b in sel], args.vpr)
-
-    t_r = t_q = 0.0
-    verts = npairs = found = 0
-    checked = []
-    t0 = time.perf_counter()
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(threads) as pool:
-        pending, k = [], 0
-        while True:
-            while len(pending) < 2 * threads and k < len(order) and time.perf_counter() - t0 < budget_s:
-                pending.append(pool.apply_async(_oracle_chunk, (job(k),)))
-                k += chunk
-            if not pending:
+    def query_sample(self, min_pairs: int) -> np.ndarray:
+        """(strip position, local pair index) of the cluster sample."""
+        srcs = [(i, s) for i, sd in enumerate(self.strips) for s in range(len(sd["s_idx"]))]
+        order = self.rng.permutation(len(srcs))
+        out = []
+        got = 0
+        for o in order:
+            i, s = srcs[o]
+            pr_ = self.strips[i]["pairs"]
+            lo, hi = np.searchsorted(pr_[:, 0], s, "left"), np.searchsorted(pr_[:, 0], s, "right")
+            if hi > lo:
+                out.append(np.stack([np.full(hi - lo, i), np.arange(lo, hi)], 1))
+                got += hi - lo
+            if got >= min_pairs:
                 break
-            r = pending.pop(0).get()
-            t_r += r[0]
-            t_q += r[1]
-            verts += r[2]
-            npairs += r[3]
-            found += r[4]
-            checked.extend(r[5])
-    total_verts = S.total + T.total
-    raster_s = t_r / max(verts, 1) * total_verts
-    query_s = t_q / max(npairs, 1) * len(pairs)
-    value = len(pairs) / (raster_s + query_s) * 1.0
-    extra = {}
-    if gpu_out is not None and checked:
-        # the same oracle doubles as a full-size parity spot check of the GPU results
-        index = {(int(a), int(b)): i for i, (a, b) in enumerate(pairs)}
-        bad = sum(1 for s_, t_, v in checked if int(gpu_out[index[(s_, t_)]]) != v)
-        extra = {"parity_sample_pairs": len(checked), "parity_sample_mismatches": bad}
-    return {**extra, "value": value, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{npairs} uniformly sampled candidate pairs of the step ({verts} vertices rasterized), "
-                      f"{time.perf_counter() - t0:.1f} s wall on {threads} core(s); raster time scaled per vertex "
-                      f"to the step's {total_verts} vertices, query time per pair to its {len(pairs)} pairs",
-            "raster_s_per_step": raster_s, "query_s_per_step": query_s}
+        return np.concatenate(out).astype(np.int64) if out else np.zeros((0, 2), np.int64)
+
+    def rings(self, entries) -> list:
+        """Rings (float32 [nv, 2]) of (strip position, side, local index) entries."""
+        from farm_gb300 import polygons as P
+        out = [None] * len(entries)
+        for side, seed in ((0, self.job.seed), (1, self.job.seed + 1)):
+            sel = [j for j, e in enumerate(entries) if e[1] == side]
+            if not sel:
+                continue
+            key = "s_idx" if side == 0 else "t_idx"
+            gids = np.array([self.strips[entries[j][0]][key][entries[j][2]] for j in sel], np.uint64)
+            ps = P.generate_indices(self.job.prm, seed, gids)
+            for m, j in enumerate(sel):
+                out[j] = ps.ring(m)
+        return out
+
+
+def timed_rasters(rings: list, vpr: int, threads: int) -> tuple[list, list, float]:
+    """Oracle rasters of the rings on `threads` threads, largest first: the
+    rasters (None where the reference fails), each polygon's own seconds
+    (measured while all threads run), and the wall time."""
+    from oracle import oracle as O
+    O.lib()
+    order = sorted(range(len(rings)), key=lambda j: -len(rings[j]))
+    res, secs = [None] * len(rings), [0.0] * len(rings)
+
+    def one(j):
+        t = time.perf_counter()
+        try:
+            r = O.Raster(rings[j], vpr)
+        except RuntimeError:
+            r = None
+        return j, r, time.perf_counter() - t
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        for j, r, s in ex.map(one, order):
+            res[j], secs[j] = r, s
+    return res, secs, time.perf_counter() - t0
+
+
+def timed_queries(rs: dict, rt: dict, keys: list, threads: int) -> tuple[np.ndarray, np.ndarray, float]:
+    """Oracle intersect of (source key, target key) pairs over prebuilt rasters
+    on `threads` threads (dynamic chunks of 8 pairs): results (2 where a
+    raster is None), reference-order segment tests per pair, wall time."""
+    from oracle import oracle as O
+    n = len(keys)
+    res = np.zeros(n, np.uint8)
+    tests = np.zeros(n, np.uint64)
+    chunks = [(a, min(a + 8, n)) for a in range(0, n, 8)]
+
+    def run(ab):
+        for k in range(*ab):
+            a, b = rs[keys[k][0]], rt[keys[k][1]]
+            if a is None or b is None:
+                res[k] = 2
+                continue
+            v, c = O.intersect(a, b, counters=True)
+            res[k], tests[k] = int(v), c.segment_tests
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(run, chunks))
+    return res, tests, time.perf_counter() - t0
+
+
+class CpuRunner:
+    """Prepares the query sample's rasters once (untimed), then times steps of
+    the CPU path: a raster phase on a fresh systematic polygon sample and the
+    query phase on the prepared pairs."""
+
+    def __init__(self, job: Job, strips: list, args, threads: int, min_pairs: int, heavy=None):
+        self.args, self.threads = args, threads
+        self.cs = CpuSample(job, strips, args.seed)
+        self.strips = strips
+        q = self.cs.query_sample(min_pairs)
+        extra = np.zeros((0, 2), np.int64)
+        if heavy is not None and heavy[1] is not None:
+            pos = [i for i, sd in enumerate(strips) if sd["strip"] == heavy[0]]
+            if pos:
+                extra = np.stack([np.full(len(heavy[1]), pos[0]), heavy[1]], 1).astype(np.int64)
+        self.q_uniform, self.q_heavy = q, extra
+        allq = np.concatenate([q, extra])
+        self.allq = allq
+        # distinct polygons of the sampled pairs
+        skeys = sorted({(int(i), 0, int(strips[i]["pairs"][p, 0])) for i, p in allq})
+        tkeys = sorted({(int(i), 1, int(strips[i]["pairs"][p, 1])) for i, p in allq})
+        t0 = time.perf_counter()
+        rings = self.cs.rings(skeys + tkeys)
+        ras, secs, wall = timed_rasters(rings, args.vpr, threads)
+        self.prep_s = time.perf_counter() - t0
+        self.rs = {k: ras[j] for j, k in enumerate(skeys)}
+        self.rt = {k: ras[len(skeys) + j] for j, k in enumerate(tkeys)}
+        self.keys = [((int(i), 0, int(strips[i]["pairs"][p, 0])), (int(i), 1, int(strips[i]["pairs"][p, 1])))
+                     for i, p in allq]
+        self.n_prep_polys = len(rings)
+        log(f"CPU sample: {len(q)} cluster-sampled pairs + {len(extra)} heavy pairs, {len(rings)} polygons "
+            f"rasterized in {self.prep_s:.1f} s on {threads} threads")
+
+    def step(self, raster_polys: int, step_seed: int, query: bool = True) -> dict:
+        cs = self.cs
+        out = {}
+        if raster_polys > 0:
+            ent, k = cs.raster_sample(raster_polys, step_seed)
+            rings = cs.rings([tuple(e[:3]) for e in ent])
+            _, secs, wall = timed_rasters(rings, self.args.vpr, self.threads)
+            # the job's raster phase: the sample's per-polygon seconds scaled by
+            # k, spread evenly over the threads (132k+ polygons per strip keep
+            # every thread busy); per-polygon seconds were measured with all
+            # threads running, so shared-resource contention is included
+            out["raster_s"] = k * sum(secs) / self.threads
+            out["raster_sample"] = {"polygons": len(ent), "k": k, "vertices": int(ent[:, 3].sum()),
+                                    "cpu_s": sum(secs), "wall_s": wall}
+        if query:
+            nq = len(self.q_uniform)
+            res, tests, wall = timed_queries(self.rs, self.rt, self.keys[:nq], self.threads)
+            out["query_s"] = wall * cs.n_pairs / max(nq, 1)
+            out["query_sample"] = {"pairs": nq, "wall_s": wall}
+            out["res"], out["tests"] = res, tests
+        return out
+
+
+def cpu_baseline(job: Job, strips: list, args, threads: int, gpu_out: dict, heavy=None) -> dict:
+    """All-core CPU oracle over bounded samples of the rank's strips, and the
+    full-scale parity check of the GPU's results on the query sample plus
+    the heavy stratum."""
+    run = CpuRunner(job, strips, args, threads, args.parity_pairs, heavy)
+    st = run.step(args.raster_sample, args.seed + 500)
+    # parity: the uniform sample's results come from the timed step; the heavy
+    # stratum is queried here
+    nq = len(run.q_uniform)
+    hres, htests, _ = timed_queries(run.rs, run.rt, run.keys[nq:], threads) if len(run.q_heavy) else \
+        (np.zeros(0, np.uint8), np.zeros(0, np.uint64), 0.0)
+    exp = np.concatenate([st["res"], hres])
+    got = np.array([gpu_out[strips[i]["strip"]][p] for i, p in run.allq], np.uint8)
+    bad = int((got != exp).sum())
+    value = run.cs.n_pairs / (st["raster_s"] + st["query_s"])
+    ok = st["res"] != 2
+    tpp = float(st["tests"][ok].astype(np.float64).mean()) if ok.any() else None
+    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": (f"raster phase: {st['raster_sample']['polygons']} polygons (systematic sample by vertex "
+                       f"count of the {len(run.cs.poly)} polygon rasterizations of the timed strips), "
+                       f"{st['raster_sample']['cpu_s']:.1f} thread-seconds over {threads} threads, scaled x "
+                       f"{st['raster_sample']['k']:.0f}; query phase: {nq} pairs of uniformly drawn sources "
+                       f"(all their candidates), {st['query_sample']['wall_s']:.2f} s wall on {threads} threads, "
+                       f"scaled to the strips' {run.cs.n_pairs} pairs"),
+            "raster_s_per_job": st["raster_s"], "query_s_per_job": st["query_s"],
+            "pairs_in_job": run.cs.n_pairs,
+            "parity_sample_pairs": int(len(exp)), "parity_sample_mismatches": bad,
+            "parity_heavy_pairs": int(len(run.q_heavy)),
+            "parity_heavy_rule": "100 pairs drawn at random from the heaviest 1% of one strip's pairs by the "
+                                 "filter's refinement cost proxy",
+            "ref_tests_per_pair": tpp, "prep_s": run.prep_s}
 
 
 def run_reference(args) -> dict:
+    """The reference's CPU algorithm (the oracle port, all host cores) on the
+    same job: every step times a fresh raster-phase sample and the query
+    sample; value is the median over the timed steps."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return None
-    W = build_workload(args.seed, 0, args.strips, args.vpr)
+    from farm_gb300 import shard
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    job = Job(args.seed, args.strips)
+    mine = shard.strips_of_rank(0, 1, args.strips)
+    order_strips = [mine[i % len(mine)] for i in range(max(args.steps, 1))]
+    strips = [job.strip(b, rings=False) for b in sorted(set(order_strips))]
+    by_strip = {sd["strip"]: sd for sd in strips}
+    pairs_timed = sum(len(by_strip[b]["pairs"]) for b in order_strips)
     threads = os.cpu_count() or 1
-    vals = []
+    run = CpuRunner(job, strips, args, threads, args.parity_pairs)
+    for i in range(args.warmup):
+        run.step(0, args.seed + 600 + i)
+    vals, steps = [], []
     t0 = time.perf_counter()
-    for _ in range(args.warmup + args.steps):
-        vals.append(cpu_baseline(W, args, budget_s=args.ref_step_seconds, threads=threads))
+    for i in range(args.steps):
+        st = run.step(args.ref_raster_sample, args.seed + 700 + i)
+        vals.append(run.cs.n_pairs / (st["raster_s"] + st["query_s"]))
+        steps.append({k: v for k, v in st.items() if k not in ("res", "tests")})
+        log(f"reference step {i}: {vals[-1]:.1f} pairs/s (raster {st['raster_s']:.0f} s, query "
+            f"{st['query_s']:.0f} s per job)")
     wall = time.perf_counter() - t0
-    v = statistics.median([x["value"] for x in vals[args.warmup:]])
-    cb = dict(vals[-1])
-    cb["value"] = v
-    cb["kind"] = "port"
-    return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1000 / (args.warmup + args.steps),
+    v = statistics.median(vals)
+    last = steps[-1]
+    cb = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+          "sample": (f"per step: {last['raster_sample']['polygons']} polygons (systematic sample by vertex count, "
+                     f"x{last['raster_sample']['k']:.0f}) and {last['query_sample']['pairs']} cluster-sampled "
+                     f"pairs, on {threads} threads; median of {args.steps} steps"),
+          "raster_s_per_job": statistics.median(s["raster_s"] for s in steps),
+          "query_s_per_job": statistics.median(s["query_s"] for s in steps)}
+    return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1000 / max(args.steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic (seeded star polygons, configuration 2 generator)", "impl": "reference",
-            "config": {"workload": "intersect, configuration 2 (see ours); CPU oracle port of the reference, "
-                                   f"-v {args.vpr}", "vpr": args.vpr, "seed": args.seed},
+            "config": workload_config(job, args, order_strips, pairs_timed,
+                                      sum(by_strip[b]["vertices"] for b in order_strips)),
             "cpu_baseline": cb,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
@@ -689,12 +978,15 @@ def main():
     ap.add_argument("--vpr", type=int, default=64)
     ap.add_argument("--strips", type=int, default=10, help="strips the job is cut into (one per step)")
     ap.add_argument("--seed", type=int, default=2024)
-    ap.add_argument("--cpu-seconds", type=float, default=20.0)
-    ap.add_argument("--ref-step-seconds", type=float, default=20.0)
+    ap.add_argument("--parity-pairs", type=int, default=2000,
+                    help="pairs of the CPU query sample (cluster sample by source; also the parity sample)")
+    ap.add_argument("--raster-sample", type=int, default=600,
+                    help="polygons of the CPU raster-phase sample in the GPU arm's cpu_baseline")
+    ap.add_argument("--ref-raster-sample", type=int, default=150,
+                    help="polygons of the raster-phase sample per step of --impl reference")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--area-pairs", type=int, default=0,
-                    help="pairs of the configuration-4 area sample (0 = skip the area block; one pass over "
-                         "1,000 pairs takes ~13 s)")
+                    help="pairs of the configuration-4 area sample (0 = skip the area block)")
     ap.add_argument("--no-learned", dest="learned", action="store_false",
                     help="skip training and evaluating the learned scorer")
     ap.add_argument("--learned-pairs", type=int, default=2_000_000, help="training + held-out pairs")
