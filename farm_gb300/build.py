@@ -26,7 +26,21 @@ LIB = PKG / "lib"
 CSRC = PKG / "csrc"
 HOST = PKG / "host"
 ORACLE = ROOT / "oracle"
-REF_SRC = Path(os.environ.get("FARM_REF_SRC", "/root/reference/src"))
+
+
+def ref_src() -> Path | None:
+    """The reference's source tree: FARM_REF_SRC, else the default that the
+    recipe in oracle/ref/Makefile names. None when that tree is absent."""
+    env = os.environ.get("FARM_REF_SRC")
+    if env:
+        p = Path(env)
+    else:
+        r = subprocess.run(["make", "-s", "-C", str(ORACLE / "ref"), "print-ref"], stdout=subprocess.PIPE,
+                           stderr=subprocess.DEVNULL, text=True)
+        if r.returncode != 0 or not r.stdout.strip():
+            return None
+        p = Path(r.stdout.strip())
+    return p if (p / "geometry" / "Ideal.cpp").exists() else None
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread"]
@@ -73,9 +87,10 @@ def build_oracle() -> Path:
 
 def build_ref() -> Path | None:
     """Compile the reference's CPU code into oracle/_ref when its sources exist."""
-    if not (REF_SRC / "geometry" / "Ideal.cpp").exists():
+    src = ref_src()
+    if src is None:
         return None
-    _run(["make", "-s", "-C", str(ORACLE / "ref"), f"REF={REF_SRC}", f"-j{os.cpu_count() or 4}"])
+    _run(["make", "-s", "-C", str(ORACLE / "ref"), f"REF={src}", f"-j{os.cpu_count() or 4}"])
     return ORACLE / "_ref" / "ref_harness"
 
 

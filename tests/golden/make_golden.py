@@ -36,7 +36,7 @@ sys.path.insert(0, str(ROOT))
 from farm_gb300 import build  # noqa: E402
 from farm_gb300.polygons import StarParams, generate  # noqa: E402
 
-REF_SRC = build.REF_SRC
+REF_SRC = build.ref_src()
 
 # (name, params, seed, count, vpr, hierarchy)
 RASTER_CASES = [
@@ -73,7 +73,7 @@ def sha(p: Path) -> str:
 def main() -> None:
     harness = build.build_ref()
     if harness is None:
-        raise SystemExit(f"reference sources not found at {REF_SRC}")
+        raise SystemExit("reference sources not found (set FARM_REF_SRC to the reference's src/)")
     build.build_host()
     manifest = {"raster": [], "pairs": []}
     tmp = Path("/tmp/farm_golden")
