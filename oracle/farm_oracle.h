@@ -104,6 +104,9 @@ int fo_segment_contain(const fo_raster *r, const float *ring, float px, float py
  * each boundary inside the other, integrated with the shoelace formula about a
  * common local origin. Rings as stored (closing copy included), m vertices. */
 double fo_intersection_area(const float *a, uint32_t ma, const float *b, uint32_t mb);
+/* The same area by plain loops over every edge pair (the definition the
+ * indexed fo_intersection_area reproduces; for tests). */
+double fo_intersection_area_plain(const float *a, uint32_t ma, const float *b, uint32_t mb);
 
 /* Degree tables (util.h:68-96). */
 double fo_degree_per_km_longitude(double lat);

@@ -64,6 +64,8 @@ def lib() -> C.CDLL:
         L.fo_segment_contain.argtypes = [C.POINTER(FoRaster), fp, C.c_float, C.c_float]
         L.fo_intersection_area.argtypes = [fp, C.c_uint32, fp, C.c_uint32]
         L.fo_intersection_area.restype = C.c_double
+        L.fo_intersection_area_plain.argtypes = [fp, C.c_uint32, fp, C.c_uint32]
+        L.fo_intersection_area_plain.restype = C.c_double
         L.fo_degree_per_km_longitude.argtypes = [C.c_double]
         L.fo_degree_per_km_longitude.restype = C.c_double
         _lib = L
@@ -213,11 +215,14 @@ def within_heuristic(rs: Raster, rt: Raster, distance: float = 10.0, geography: 
     return bool(v)
 
 
-def intersection_area(a: np.ndarray, b: np.ndarray) -> float:
+def intersection_area(a: np.ndarray, b: np.ndarray, plain: bool = False) -> float:
+    """FP64 area of ring a intersected with ring b (plain: the definition by
+    loops over every edge pair, for checking the indexed version)."""
     fp = C.POINTER(C.c_float)
     a = np.ascontiguousarray(a, dtype=np.float32)
     b = np.ascontiguousarray(b, dtype=np.float32)
-    return lib().fo_intersection_area(a.ctypes.data_as(fp), len(a), b.ctypes.data_as(fp), len(b))
+    f = lib().fo_intersection_area_plain if plain else lib().fo_intersection_area
+    return f(a.ctypes.data_as(fp), len(a), b.ctypes.data_as(fp), len(b))
 
 
 def read_ref_rasters(path: str) -> list[dict]:

@@ -130,3 +130,22 @@ def test_oracle_area_matches_exact_rational(host_built, seed, n_hi, count):
         assert abs(O.intersection_area(b, a) - got) <= 1e-12 * max(got, 1e-300)
         nonzero += want > 0
     assert nonzero >= count // 2
+
+
+def test_indexed_area_oracle_equals_its_plain_definition(host_built):
+    """The area oracle finds crossing edges and inside tests through spatial
+    indexes; the loops over every edge pair that define it give the same
+    double, bit for bit, on star polygons of mixed sizes and shapes."""
+    from farm_gb300 import polygons as P
+    rng = np.random.default_rng(17)
+    for k in range(24):
+        na, nb = int(rng.integers(4, 2500)), int(rng.integers(4, 2500))
+        ra, rb = float(rng.uniform(0.2, 2.0)), float(rng.uniform(0.2, 2.0))
+        pa = P.StarParams(dom_lo=5.0, dom_hi=5.0 + 1e-9, r_lo=ra, r_hi=ra, n_lo=na, n_hi=na,
+                          sigma=float(rng.uniform(0.05, 0.7)))
+        pb = P.StarParams(dom_lo=5.0 + float(rng.uniform(-1, 1)), dom_hi=6.0, r_lo=rb, r_hi=rb, n_lo=nb, n_hi=nb,
+                          sigma=float(rng.uniform(0.05, 0.7)))
+        A = P.generate(pa, 100 + k, 1).ring(0)
+        B = P.generate(pb, 200 + k, 1).ring(0)
+        fast, plain = O.intersection_area(A, B), O.intersection_area(A, B, plain=True)
+        assert fast == plain, (k, fast, plain)
