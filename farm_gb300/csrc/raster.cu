@@ -331,11 +331,41 @@ __device__ inline int d2i_cert(const cval &q) {
     return (int)fi + (d1 < 1e-8f ? 1 : 0);
 }
 
+// The walk's decisions by the reference's FP64 expressions, for the
+// undecided cases only (out of line, so that their divisions are never
+// evaluated ahead of the test that selects them).
+__device__ __noinline__ int cell_fp64(float v, double start, double step) {
+    return double_to_int(((double)v - start) / step);
+}
+__device__ __noinline__ int xstep_fp64(int xl, double start_x, double step_x, double start_y, double step_y, double a,
+                                       double b, int *cur_y) {
+    const double xval = (double)xl * step_x + start_x;
+    const double yval = xval * a + b;
+    const double q = (yval - start_y) / step_y;
+    *cur_y = (int)q;
+    return fabs(q - round(q)) < 1e-9 ? 1 : 0;
+}
+__device__ __noinline__ int ystep_fp64(int yl, double start_x, double step_x, double start_y, double step_y, double a,
+                                       double b) {
+    const double yval = (double)yl * step_y + start_y;
+    const double xval = (yval - b) / a;
+    return (int)((xval - start_x) / step_x);
+}
+// the h-node abscissa the fill pass emits (Ideal.cpp:476)
+__device__ __noinline__ double hnode_fp64(int yl, double start_y, double step_y, double a, double b) {
+    return ((double)yl * step_y + start_y - b) / a;
+}
+// the line of the reference (Ideal.cpp:371-372)
+__device__ __noinline__ void line_ab_fp64(float x1, float y1, float x2, float y2, double *a, double *b) {
+    *a = ((double)y1 - (double)y2) / ((double)x1 - (double)x2);
+    *b = ((double)x1 * (double)y2 - (double)x2 * (double)y1) / ((double)x1 - (double)x2);
+}
+
 // double_to_int((v - start) / step) for a vertex coordinate v
 __device__ inline int cell_of(float v, const dflt &s, const dflt &is, double start, double step) {
     const cval q = cv_mul(cv_add(cv_f(v), cv_neg(cv_d(s))), cv_d(is));
     const int r = d2i_cert(q);
-    return r >= 0 ? r : double_to_int(((double)v - start) / step);
+    return r >= 0 ? r : cell_fp64(v, start, step);
 }
 
 template <typename Sink>
@@ -407,8 +437,7 @@ __device__ void walk_edge(const PolyHdr &h, const WalkF &g, float2 A, float2 B, 
     bool have_ab = false;
     auto need_ab = [&]() {
         if (!have_ab) {
-            a = ((double)y1 - (double)y2) / ((double)x1 - (double)x2);
-            b = ((double)x1 * (double)y2 - (double)x2 * (double)y1) / ((double)x1 - (double)x2);
+            line_ab_fp64(x1, y1, x2, y2, &a, &b);
             have_ab = true;
         }
     };
@@ -441,11 +470,7 @@ __device__ void walk_edge(const PolyHdr &h, const WalkF &g, float2 A, float2 B, 
             }
             if (corner < 0) {  // undecided: the reference's FP64 expression
                 need_ab();
-                const double xval = (double)xl * step_x + start_x;
-                const double yval = xval * a + b;
-                const double q = (yval - start_y) / step_y;
-                corner = fabs(q - round(q)) < 1e-9 ? 1 : 0;
-                cur_y = (int)q;
+                corner = xstep_fp64(xl, start_x, step_x, start_y, step_y, a, b, &cur_y);
             }
             if (corner) {
                 // Ideal.cpp:396-422: through a grid corner
@@ -512,16 +537,18 @@ __device__ void walk_edge(const PolyHdr &h, const WalkF &g, float2 A, float2 B, 
                 }
             }
             double xval = 0.0;
-            if (!ok || Sink::kValues) {
+            if (!ok) {
                 need_ab();
-                const double yval = (double)yl * step_y + start_y;
-                xval = (yval - b) / a;
-                if (!ok) cur_x = (int)((xval - start_x) / step_x);
+                cur_x = ystep_fp64(yl, start_x, step_x, start_y, step_y, a, b);
             }
             if (cur_x > xmax) cur_x = xmax;
             if (cur_x < xmin) cur_x = xmin;
             if (cur_x == x) {
                 passed = true;
+                if (Sink::kValues) {
+                    need_ab();
+                    xval = hnode_fp64(yl, start_y, step_y, a, b);
+                }
                 if (cur_starty < cur_endy) {
                     s.hnode(y + 1, xval);
                     s.cross(x, y, x, y + 1);
@@ -719,6 +746,19 @@ __device__ inline int clip_x_points(float2 A, float2 B, const LineF &X0, const L
     return n;
 }
 
+// The reference's FP64 expressions, evaluated only where the certified
+// double-float value is undecided. Kept out of line: inlined, the compiler
+// may evaluate them ahead of the test that selects them, which would issue
+// their FP64 divisions for every point.
+__device__ __noinline__ float clip_ord_fp64(float2 A, float2 B, double X) {
+    const double sl = ((double)B.y - A.y) / (double)(B.x - A.x);
+    return (float)(sl * (X - B.x) + B.y);
+}
+__device__ __noinline__ float clip_absc_fp64(float2 A, float2 B, double Y) {
+    const double sl = ((double)B.y - A.y) / (double)(B.x - A.x);
+    return (float)(((Y - B.y) / sl) + B.x);
+}
+
 // The edge's ordinate at column line X (Ideal.cpp:575-600): the reference
 // computes slope = ((double)B.y - A.y) / (double)(B.x - A.x) (the x difference
 // taken in float) and ord = slope * (X - B.x) + B.y in FP64, then stores it as
@@ -742,11 +782,7 @@ struct ClipXEdge {
             slope_err = __fadd_rn(slope_err, __fmul_rn(kU2 * 0.125f, fabsf(slope.hi)));
         }
     }
-    __device__ float ord_exact(double X) const {
-        if (vert) return ymin;
-        const double sl = ((double)B.y - A.y) / (double)(B.x - A.x);
-        return (float)(sl * (X - B.x) + B.y);
-    }
+    __device__ float ord_exact(double X) const { return vert ? ymin : clip_ord_fp64(A, B, X); }
     __device__ float ordf(double X, const LineF &L, bool cert) const {
         if (vert) return ymin;
         if (cert) {
@@ -816,10 +852,7 @@ struct ClipYEdge {
         }
     }
     __device__ bool general() const { return !vert && !horiz; }
-    __device__ float absc_exact(double Y) const {
-        const double sl = ((double)B.y - A.y) / (double)(B.x - A.x);
-        return (float)(((Y - B.y) / sl) + B.x);
-    }
+    __device__ float absc_exact(double Y) const { return clip_absc_fp64(A, B, Y); }
     __device__ float abscf(double Y, const LineF &L, bool cert) const {
         if (cert) {
             float et = __fmul_rn(kU2, fabsf(L.rn));  // the line's own split
@@ -1540,7 +1573,7 @@ __global__ void k_clipy(const PolyHdr *__restrict__ hdr, Chunk ch, const uint32_
                         const uint64_t *__restrict__ cpstart, const float2 *__restrict__ cpoly,
                         const uint32_t *__restrict__ cpcol, const uint32_t *__restrict__ colpoly, uint64_t ncp,
                         const double *__restrict__ rowy, const LineF *__restrict__ rowf, int cert,
-                        uint32_t *__restrict__ cnt, const uint64_t *__restrict__ scan, uint64_t *__restrict__ okey,
+                        uint32_t *__restrict__ cnt, const uint64_t *__restrict__ scan, uint32_t *__restrict__ okey,
                         float2 *__restrict__ opt) {
     for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < ncp; t += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t j = perm[t];
@@ -1548,7 +1581,6 @@ __global__ void k_clipy(const PolyHdr *__restrict__ hdr, Chunk ch, const uint32_
         uint32_t total = 0;
         if (j + 1 < cpstart[c + 1]) {
             const PolyHdr &h = hdr[colpoly[c]];
-            int x = (int)(c + ch.col0 - h.col);
             float2 A = cpoly[j], B = cpoly[j + 1];
             const float mny = A.y < B.y ? A.y : B.y, mxy = A.y < B.y ? B.y : A.y;
             const float mg = fmargin_f(mny, mxy);
@@ -1581,9 +1613,8 @@ __global__ void k_clipy(const PolyHdr *__restrict__ hdr, Chunk ch, const uint32_
                 }
                 int k = clip_y_points(A, B, L0, L1, pi, pi1, par, okey ? buf : nullptr);
                 if (okey && k) {
-                    uint64_t cell = (h.pix - ch.pix0) + (uint64_t)r * h.dimx + x;
-                    for (int q = 0; q < k; q++) {
-                        okey[at] = cell;
+                    for (int q = 0; q < k; q++) {  // the row within the column; the column is the edge's
+                        okey[at] = (uint32_t)r;
                         opt[at] = buf[q];
                         at++;
                     }
@@ -1619,18 +1650,81 @@ __device__ __forceinline__ double exact_fmul(float a, float b) {
     return __longlong_as_double((long long)(sign | (ex << 52) | frac));
 }
 
-// Cell-area schedule: pixels in order of their clip-point counts, heaviest
-// first (8-bit key, finer below 64 points), so that the lanes of a warp sum
-// runs of similar length. The order only schedules the sums.
-__global__ void k_cell_cost(const uint64_t *__restrict__ cellstart, uint64_t npix, uint8_t *__restrict__ key,
-                            uint32_t *__restrict__ idx) {
-    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < npix;
-         g += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t n = cellstart[g + 1] - cellstart[g];
-        const uint64_t k = n < 64 ? n : 64 + (n - 64) / 16;
-        key[g] = (uint8_t)(255 - (k < 255 ? k : 255));
-        idx[g] = (uint32_t)g;
+// The cell clip's points grouped by cell. k_clipy writes each column's
+// points contiguously, edge after edge of the column polygon, each tagged
+// with its row; a cell's points are the column's points of its row, in that
+// order. One warp per column buckets them stably by row, 32 points at a time
+// (lanes with equal rows found by __match_any_sync, ranked by lane): a count
+// pass, a scan over the column's rows, a scatter pass. This replaces a
+// global radix sort of every point by cell: two reads and one write of the
+// points instead of three sorting passes over 16-byte keys and values.
+// Afterwards cnt[g] holds the end of cell g's points within its column (its
+// start is the end of the cell above), and ckey[g] the cell's cost key for
+// the area schedule (cells of empty columns keep their preset key).
+__global__ void k_cell_bucket(const PolyHdr *__restrict__ hdr, Chunk ch, const uint64_t *__restrict__ cpstart,
+                              const uint64_t *__restrict__ yscan, const uint32_t *__restrict__ colpoly, uint64_t ncol,
+                              const uint32_t *__restrict__ rowkey, const uint64_t *__restrict__ pin,
+                              uint64_t *__restrict__ pout, uint32_t *__restrict__ cnt, uint8_t *__restrict__ ckey) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < ncol; c += nw) {
+        const uint64_t j0 = cpstart[c], j1 = cpstart[c + 1];
+        if (j0 == j1) continue;
+        const PolyHdr &h = hdr[colpoly[c]];
+        const uint64_t ib = yscan[j0], ie = yscan[j1];
+        const uint64_t dimx = (uint64_t)h.dimx;
+        const int nrows = h.nrows;
+        const uint64_t cell0 = (h.pix - ch.pix0) + (c + ch.col0 - h.col);  // the column's cell in row 0
+        uint32_t *C = cnt + cell0;
+        for (uint64_t base = ib; base < ie; base += 32) {  // points per row
+            const uint64_t i = base + lane;
+            const bool v = i < ie;
+            const unsigned act = __ballot_sync(full, v);
+            if (v) {
+                const uint32_t r = rowkey[i];
+                const unsigned grp = __match_any_sync(act, r);
+                if (lane == __ffs(grp) - 1) C[r * dimx] += (uint32_t)__popc(grp);
+            }
+            __syncwarp();
+        }
+        uint32_t run = 0;
+        for (int r0 = 0; r0 < nrows; r0 += 32) {  // rows -> starts, and the cells' cost keys
+            const int r = r0 + lane;
+            const uint32_t v = r < nrows ? C[(uint64_t)r * dimx] : 0u;
+            uint32_t inc = v;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t t = __shfl_up_sync(full, inc, o);
+                if (lane >= o) inc += t;
+            }
+            if (r < nrows) {
+                C[(uint64_t)r * dimx] = run + inc - v;
+                const uint32_t k = v < 64u ? v : 64u + (v - 64u) / 16u;
+                ckey[cell0 + (uint64_t)r * dimx] = (uint8_t)(255u - (k < 255u ? k : 255u));
+            }
+            run += __shfl_sync(full, inc, 31);
+        }
+        __syncwarp();
+        for (uint64_t base = ib; base < ie; base += 32) {  // stable scatter
+            const uint64_t i = base + lane;
+            const bool v = i < ie;
+            const unsigned act = __ballot_sync(full, v);
+            if (v) {
+                const uint32_t r = rowkey[i];
+                const unsigned grp = __match_any_sync(act, r);
+                const uint32_t at = C[r * dimx] + (uint32_t)__popc(grp & ((1u << lane) - 1u));
+                pout[ib + at] = pin[i];
+                __syncwarp(act);  // every lane has read its row's start
+                if (lane == __ffs(grp) - 1) C[r * dimx] += (uint32_t)__popc(grp);
+            }
+            __syncwarp();
+        }
     }
+}
+
+__global__ void k_iota_u32(uint32_t *__restrict__ a, uint64_t n) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
+        a[k] = (uint32_t)k;
 }
 
 // Per pixel: cell area (geometry_computation.h:275-297 over the cell's clip,
@@ -1639,9 +1733,10 @@ __global__ void k_cell_cost(const uint64_t *__restrict__ cellstart, uint64_t npi
 // products come from exact_fmul, so the FP64 pipe only takes the difference and
 // the running sum, in the reference's order.
 __global__ void k_cells(PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ pixbase, Chunk ch,
-                        const uint32_t *__restrict__ order, const uint64_t *__restrict__ cellstart,
-                        const float2 *__restrict__ cpt, const uint64_t *__restrict__ cpstart,
-                        uint8_t *__restrict__ status, double *__restrict__ areas, int cc) {
+                        const uint32_t *__restrict__ order, const uint32_t *__restrict__ cellend,
+                        const uint64_t *__restrict__ yscan, const float2 *__restrict__ cpt,
+                        const uint64_t *__restrict__ cpstart, uint8_t *__restrict__ status,
+                        double *__restrict__ areas, int cc) {
     for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < ch.npix;
          t += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t g = order ? order[t] : t;
@@ -1653,7 +1748,8 @@ __global__ void k_cells(PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ 
         if (x >= h.ncols || y >= h.nrows) continue;
         uint64_t cidx = h.col - ch.col0 + (uint64_t)x;
         if (cpstart[cidx + 1] == cpstart[cidx]) continue;  // empty column: not visited
-        uint64_t b = cellstart[g], e = cellstart[g + 1];
+        const uint64_t colbase = yscan[cpstart[cidx]];  // the column's points (k_cell_bucket)
+        const uint64_t b = colbase + (y ? cellend[g - (uint64_t)h.dimx] : 0u), e = colbase + cellend[g];
         uint64_t n = e - b;
         bool close = n > 0 && pt_ne(cpt[b], cpt[e - 1]);
         uint64_t m = n + (close ? 1 : 0);
@@ -2000,7 +2096,7 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
             L++;
             unsigned long long hbig = 0;
             FARM_TRY(d2h(s, &hbig, nbig, 8));
-            if (hbig) {
+            if (hbig) {  // lines beyond the shared-memory sort: the library's segmented sort
                 FARM_TRY(cub_call(s, [&](void *t, size_t &b) {
                     return cub::DeviceSegmentedSort::SortKeys(t, b, unsorted, nodes_out, (int64_t)nn, (int64_t)hbig,
                                                               big_b, big_e, st);
@@ -2188,34 +2284,42 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     FARM_TRY(s->s[S_VVAL].ensure(8 * nY + 16));
     FARM_TRY(s->s[S_HKEY].ensure(8 * nY + 16));
     FARM_TRY(s->s[S_HVAL].ensure(8 * nY + 16));
-    uint64_t *ykb = s->s[S_VKEY].as<uint64_t>(), *yks = s->s[S_HKEY].as<uint64_t>();
+    uint32_t *ykb = s->s[S_VKEY].as<uint32_t>();
     float2 *ypb = s->s[S_VVAL].as<float2>(), *yps = s->s[S_HVAL].as<float2>();
+    // per cell: the end of its points within its column, and its cost key
+    // (the cell order's buffers are free again after the cell-clip order)
+    FARM_TRY(s->s[S_TMP_A].ensure(4 * (ch.npix + 1) + 16));
+    uint32_t *cellend = s->s[S_TMP_A].as<uint32_t>();
+    FARM_CUDA(cudaMemsetAsync(cellend, 0, 4 * (ch.npix + 1), st));
     if (nY) {
         R.timer.time(T_CLIPY, st, [&] { k_clipy<<<gb(nCP), 256, 0, st>>>(R.hdr, ch, yperm, cpstart, cpoly, cpcol, colpoly, nCP, R.rowy, R.rowf,
                                          R.cert, nullptr, yscan, ykb, ypb); });
         L++;
-        FARM_TRY(sort_pairs(s, ykb, yks, reinterpret_cast<uint64_t *>(ypb), reinterpret_cast<uint64_t *>(yps), nY,
-                            key_bits(ch.npix)));
     }
-    // cell starts (the points are sorted by cell)
-    FARM_TRY(s->s[S_TMP_A].ensure(8 * (ch.npix + 1) + 16));
-    uint64_t *cellstart = s->s[S_TMP_A].as<uint64_t>();
-    k_seg_starts<<<gb(nY + 1), 256, 0, st>>>(yks, nY, ch.npix, cellstart);
-    L++;
-    // cells heaviest first (the clip-point sort's buffers are free again)
+    // (yperm lives in S_PERM: the emit pass above is done with it before these
+    // buffers are regrown or rewritten, stream-ordered)
+    FARM_TRY(s->s[S_PERM_K].ensure(2 * ch.npix + 16));
+    FARM_TRY(s->s[S_PERM].ensure(8 * ch.npix + 16));
+    uint8_t *ckey = s->s[S_PERM_K].as<uint8_t>(), *ckey_s = ckey + ch.npix;
+    uint32_t *cidx = s->s[S_PERM].as<uint32_t>(), *cidx_s = cidx + ch.npix;
+    FARM_CUDA(cudaMemsetAsync(ckey, 0xFF, ch.npix, st));
+    if (nY) {
+        unsigned cb = (unsigned)std::min<uint64_t>((ncol + 7) / 8, 64ull * sm_count());
+        k_cell_bucket<<<cb ? cb : 1, 256, 0, st>>>(R.hdr, ch, cpstart, yscan, colpoly, ncol, ykb,
+                                                  reinterpret_cast<const uint64_t *>(ypb),
+                                                  reinterpret_cast<uint64_t *>(yps), cellend, ckey);
+        L++;
+    }
+    // cells heaviest first
     uint32_t *corder = nullptr;
     if (ch.npix) {
-        FARM_TRY(s->s[S_PERM_K].ensure(2 * ch.npix + 16));
-        FARM_TRY(s->s[S_PERM].ensure(8 * ch.npix + 16));
-        uint8_t *key = s->s[S_PERM_K].as<uint8_t>(), *key_s = key + ch.npix;
-        uint32_t *idx = s->s[S_PERM].as<uint32_t>(), *idx_s = idx + ch.npix;
-        k_cell_cost<<<gb(ch.npix), 256, 0, st>>>(cellstart, ch.npix, key, idx);
+        k_iota_u32<<<gb(ch.npix), 256, 0, st>>>(cidx, ch.npix);
         L++;
-        FARM_TRY(sort_pairs(s, key, key_s, idx, idx_s, ch.npix, 8));
-        corder = idx_s;
+        FARM_TRY(sort_pairs(s, ckey, ckey_s, cidx, cidx_s, ch.npix, 8));
+        corder = cidx_s;
     }
-    R.timer.time(T_CELLS, st, [&] { k_cells<<<gb(ch.npix), 256, 0, st>>>(R.hdr, pixbase, ch, corder, cellstart, yps, cpstart,
-                                         s->d_status.as<uint8_t>(), s->d_areas.as<double>(), R.cc); });
+    R.timer.time(T_CELLS, st, [&] { k_cells<<<gb(ch.npix), 256, 0, st>>>(R.hdr, pixbase, ch, corder, cellend, yscan, yps,
+                                         cpstart, s->d_status.as<uint8_t>(), s->d_areas.as<double>(), R.cc); });
     L++;
 
     // ---- hierarchy
