@@ -86,4 +86,5 @@ def declare(lib):
     lib.farm_store_launches.restype = C.c_uint64
     lib.farm_store_device_bytes.argtypes = [vp, u64p]
     lib.farm_probe_issue_rates.argtypes = [f64p, f64p]
+    lib.farm_mbr_join_gpu.argtypes = [vp, C.c_double, C.c_int, C.c_int, vp, C.c_uint64, C.c_int, u64p]
 

@@ -115,6 +115,30 @@ class Store:
         check_gpu(rc)
         return 0
 
+    def mbr_join(self, expand: float = 0.0, geography: bool = False, self_join: bool = False, device=None,
+                 cap: int = 0):
+        """Candidate pairs of the loaded sides computed on the GPU (uint32
+        [k, 2], ascending (source, target)): a CUDA tensor when `device` is
+        given, else numpy. `cap` bounds the pairs (0: counted first)."""
+        lib = self._lib
+        n = C.c_uint64(0)
+        if cap <= 0:
+            rc = lib.farm_mbr_join_gpu(self._h, float(expand), int(geography), int(self_join), None, 0, MEM_HOST,
+                                       C.byref(n))
+            if rc not in (0, -4):
+                check_gpu(rc)
+            cap = int(n.value)
+        if device is not None:
+            import torch
+            out = torch.empty((max(cap, 1), 2), dtype=torch.int32, device=device)
+            check_gpu(lib.farm_mbr_join_gpu(self._h, float(expand), int(geography), int(self_join),
+                                             C.c_void_p(out.data_ptr()), cap, MEM_DEVICE, C.byref(n)))
+            return out[:n.value]
+        out = np.zeros((max(cap, 1), 2), dtype=np.uint32)
+        check_gpu(lib.farm_mbr_join_gpu(self._h, float(expand), int(geography), int(self_join),
+                                         C.c_void_p(out.ctypes.data), cap, MEM_HOST, C.byref(n)))
+        return out[:n.value]
+
     def intersect(self, pairs, mode: int = MODE_EXACT, out=None):
         """Per-pair 0/1 results (same memory kind as ``pairs``) and the found count."""
         n = pairs.shape[0]

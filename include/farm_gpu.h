@@ -70,8 +70,8 @@ typedef struct farm_stats {
     uint64_t pairs;          /* pairs decided */
     uint64_t found;          /* pairs whose result is true */
     uint64_t in_hits;        /* decided by an IN pixel overlap (intersect) */
-    uint64_t border_pairs;   /* BORDER x BORDER pixel pairs examined */
-    uint64_t segment_tests;  /* segment-pair (or point-segment) evaluations */
+    uint64_t border_pairs;   /* BORDER x BORDER pixel pairs examined (area: crossings counted) */
+    uint64_t segment_tests;  /* segment-pair (or point-segment) evaluations (area: FP64 crossing tests) */
     uint64_t fp64_rechecks;  /* within: edge-sequence pairs re-evaluated in FP64 after the FP32 pass;
                                 learned intersect: pairs refined exactly */
     double ms_total;         /* device time of the call (CUDA events) */
@@ -100,6 +100,19 @@ int farm_store_load(farm_store *s, int side, uint64_t n, const uint64_t *off, co
 /* Rasterize every loaded polygon (reference: preprocessing.cpp:4-29,
  * Ideal.cpp:920-955). Must precede the queries. */
 int farm_rasterize(farm_store *s, const farm_raster_opts *o);
+
+/* Candidate pairs on the GPU, from the loaded rings (no rasterization
+ * needed): every (source, target) whose closed MBRs overlap, the target's box
+ * widened by `expand` (the within distance; in degrees by the reference's
+ * longitude table when geography is set, Box.cpp:200-214), in ascending
+ * (source, target) order: the set and order farm_mbr_join (farm_host.h)
+ * returns, i.e. what the reference's R-tree search per target yields
+ * (RTree.h:581-600, intersect_cpu.cpp:18-36). target_is_source: a self-join
+ * of side 0 without (i, i). pairs: room for cap pairs (2 x uint32 each) in
+ * memory `mem`; *n gets the count, and FARM_EOVERFLOW is returned (pairs
+ * untouched) when it exceeds cap. */
+int farm_mbr_join_gpu(farm_store *s, double expand, int geography, int target_is_source, uint32_t *pairs,
+                      uint64_t cap, int mem, uint64_t *n);
 
 /* Decide Ideal::intersect(source[p.s], target[p.t]) for n pairs. pairs: 2n
  * uint32 (s, t). out: n bytes, may be NULL: 0 / 1, or 2 when either polygon
