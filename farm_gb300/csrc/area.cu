@@ -65,6 +65,8 @@ struct AreaArgs {
     const uint32_t *ep_pix;      // pixels listing each edge (edge -> pixel CSR)
     unsigned long long *next;
     unsigned long long *overflow;  // [0] unused, [1] items beyond cap_items
+    unsigned long long *work;      // [0] FP64 crossing tests, [1] crossings counted
+    long wide_window;              // windows above this many pixels: searched by the whole warp
 };
 
 __device__ __forceinline__ double cross2(double ax, double ay, double bx, double by) { return ax * by - ay * bx; }
@@ -202,6 +204,38 @@ __device__ void for_candidate_edges(const StoreView &sv, const PolyHdr &O, const
     }
 }
 
+// The same enumeration with the warp sharing one segment: every lane walks
+// the window in the same order (so each holds the same row cache), and the
+// candidate listings of each row — all sequences of all its pixels, in
+// order — are dealt to the lanes round robin; f runs for the lane's share.
+// A long edge across a dense polygon meets thousands of candidates, which a
+// single lane would otherwise test one after another.
+template <typename F>
+__device__ void for_candidate_edges_warp(const StoreView &sv, const PolyHdr &O, const SegWin &w, int cc,
+                                         RowCache &rc, int lane, F f) {
+    const uint8_t *st = sv.status + O.st;
+    const uint32_t *off = sv.offset + O.off;
+    const uint2 *seq = sv.seq + O.seq;
+    for (int y = w.sy; y <= w.ey; y++) {
+        int xa, xb;
+        const bool ok = row_cols(O, w, y, xa, xb);
+        rc.r[y & (kRowCache - 1)] = ok ? make_int2(xa, xb) : make_int2(1, 0);
+        if (!ok) continue;
+        uint32_t base = 0;  // listings of the row before the current sequence
+        for (int x = xa; x <= xb; x++) {
+            const uint32_t pid = (uint32_t)(y * O.dimx + x);
+            if (show_status(st[pid], cc) != 1) continue;
+            for (uint32_t q = off[pid]; q < off[pid + 1]; q++) {
+                const uint2 sq = seq[q];
+                // this lane's listings k of the sequence: (base + k) % 32 == lane
+                uint32_t k = (uint32_t)((lane - (int)(base & 31u) + 32) & 31);
+                for (; k < sq.y; k += 32) f(pid, xa, q, sq.x + k);
+                base += sq.y;
+            }
+        }
+    }
+}
+
 // Whether the listing of edge f met in pixel pid (sequence q, its row's first
 // column xa) is the first listing of f that for_candidate_edges meets: no
 // BORDER pixel of the window with a smaller id (an earlier row, or the same
@@ -288,9 +322,23 @@ __device__ __forceinline__ bool crossing(double px, double py, double dx, double
     return t >= 0 && t < 1 && u >= 0 && u < 1;
 }
 
+// An edge whose candidate window holds more pixels than this is searched by
+// the whole warp (for_candidate_edges_warp) instead of its own lane
+// (FARM_AREA_WIDE_WINDOW overrides it).
+constexpr long kWideWindow = 48;
+
+static long wide_window() {
+    const char *v = getenv("FARM_AREA_WIDE_WINDOW");
+    if (!v || !*v) return kWideWindow;
+    const long x = strtol(v, nullptr, 10);
+    return x > 0 ? x : kWideWindow;
+}
+
+
 __global__ void __launch_bounds__(256) k_area(const StoreView sv, AreaArgs a) {
     const int lane = threadIdx.x & 31;
     const int cc = sv.category_count;
+    unsigned long long my_tests = 0, my_cross = 0;
     for (;;) {
         const uint64_t n = *a.n;
         const uint64_t nitems = a.item_start[n];
@@ -334,14 +382,19 @@ __global__ void __launch_bounds__(256) k_area(const StoreView sv, AreaArgs a) {
             double px = 0, py = 0, dx = 0, dy = 0;
             double sum_t = 0;  // leaving t minus entering t
             int nc = 0;
+            float2 P = make_float2(0.f, 0.f), Q = P;
+            bool wide = false;
             if (valid) {
-                float2 P = mr[e], Q = mr[e + 1];
+                P = mr[e];
+                Q = mr[e + 1];
                 px = (double)P.x - ox;
                 py = (double)P.y - oy;
                 dx = (double)Q.x - P.x;
                 dy = (double)Q.y - P.y;
                 SegWin w;
-                if ((dx != 0 || dy != 0) && seg_window(O, P.x, P.y, Q.x, Q.y, w)) {
+                const bool has_w = (dx != 0 || dy != 0) && seg_window(O, P.x, P.y, Q.x, Q.y, w);
+                wide = has_w && (long)(w.ex - w.sx + 1) * (long)(w.ey - w.sy + 1) > a.wide_window;
+                if (has_w && !wide) {
                     // an edge of O may be listed by several pixels: count it
                     // at its first listing only (tested before the FP64
                     // crossing, which then runs once per edge pair)
@@ -349,12 +402,44 @@ __global__ void __launch_bounds__(256) k_area(const StoreView sv, AreaArgs a) {
                     for_candidate_edges(sv, O, w, cc, rc, [&](uint32_t pid, int xa, uint32_t q, uint32_t f) {
                         double t, den;
                         if (apart32(P, Q, orr[f], orr[f + 1]) ||
-                            !first_listing(sv, O, w, cc, rc, a.ep_off, a.ep_pix, pid, xa, q, f) ||
-                            !crossing(px, py, dx, dy, orr, f, ox, oy, t, den))
+                            !first_listing(sv, O, w, cc, rc, a.ep_off, a.ep_pix, pid, xa, q, f))
                             return;
+                        my_tests++;
+                        if (!crossing(px, py, dx, dy, orr, f, ox, oy, t, den)) return;
                         nc++;
                         sum_t += (osign * den > 0) ? t : -t;
                     });
+                }
+            }
+            // edges with wide windows: the whole warp takes one at a time
+            for (unsigned wm = __ballot_sync(0xffffffffu, wide); wm; wm &= wm - 1) {
+                const int src = __ffs(wm) - 1;
+                const float2 Pw = make_float2(__shfl_sync(0xffffffffu, P.x, src), __shfl_sync(0xffffffffu, P.y, src));
+                const float2 Qw = make_float2(__shfl_sync(0xffffffffu, Q.x, src), __shfl_sync(0xffffffffu, Q.y, src));
+                const double pxw = (double)Pw.x - ox, pyw = (double)Pw.y - oy;
+                const double dxw = (double)Qw.x - Pw.x, dyw = (double)Qw.y - Pw.y;
+                SegWin ww;
+                seg_window(O, Pw.x, Pw.y, Qw.x, Qw.y, ww);  // the owner's window, recomputed identically
+                RowCache rc;
+                double st_l = 0;
+                int nc_l = 0;
+                for_candidate_edges_warp(sv, O, ww, cc, rc, lane, [&](uint32_t pid, int xa, uint32_t q, uint32_t f) {
+                    double t, den;
+                    if (apart32(Pw, Qw, orr[f], orr[f + 1]) ||
+                        !first_listing(sv, O, ww, cc, rc, a.ep_off, a.ep_pix, pid, xa, q, f))
+                        return;
+                    my_tests++;
+                    if (!crossing(pxw, pyw, dxw, dyw, orr, f, ox, oy, t, den)) return;
+                    nc_l++;
+                    st_l += (osign * den > 0) ? t : -t;
+                });
+                for (int o = 16; o; o >>= 1) {
+                    st_l += __shfl_xor_sync(0xffffffffu, st_l, o);
+                    nc_l += __shfl_xor_sync(0xffffffffu, nc_l, o);
+                }
+                if (lane == src) {
+                    sum_t = st_l;
+                    nc = nc_l;
                 }
             }
             // parity of crossings of earlier edges of the chunk
@@ -365,10 +450,13 @@ __global__ void __launch_bounds__(256) k_area(const StoreView sv, AreaArgs a) {
                 acc += cross2(px, py, dx, dy) * len;
             }
             state ^= (__popc(odd) & 1);
+            if (valid) my_cross += (unsigned long long)nc;
         }
         for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (lane == 0) a.partial[it] = 0.5 * sign * acc;
     }
+    if (my_tests) atomicAdd(&a.work[0], my_tests);
+    if (my_cross) atomicAdd(&a.work[1], my_cross);
 }
 
 // orientation sign of every polygon (shoelace about its first vertex)
@@ -563,7 +651,7 @@ static int area_items(farm_store *s, const AreaBufs &b, cudaStream_t st) {
 }
 
 static int area_compute(farm_store *s, const AreaBufs &b, cudaStream_t st) {
-    FARM_CUDA(cudaMemsetAsync(b.ctr, 0, 24, st));
+    FARM_CUDA(cudaMemsetAsync(b.ctr, 0, 40, st));
     AreaArgs aa{b.pairs,
                 b.n,
                 s->n_side[0],
@@ -575,7 +663,9 @@ static int area_compute(farm_store *s, const AreaBufs &b, cudaStream_t st) {
                 s->s[Q_AREA_EPOFF].as<uint64_t>(),
                 s->s[Q_AREA_EPPIX].as<uint32_t>(),
                 b.ctr,
-                b.ctr + 1};
+                b.ctr + 1,
+                b.ctr + 3,
+                wide_window()};
     k_area<<<sm_count() * 8, 256, 0, st>>>(s->view(), aa);
     FARM_CUDA(cudaGetLastError());
     unsigned blocks = (unsigned)((b.cap_pairs + 255) / 256);
@@ -645,11 +735,15 @@ int intersection_area(farm_store *s, const uint32_t *pairs, uint64_t n, int mem,
     FARM_TRY(area_compute(s, b, stream));
     FARM_CUDA(cudaEventRecord(s->ev[7], stream));
     if (mem == FARM_MEM_HOST && out && n) FARM_CUDA(cudaMemcpyAsync(out, dout, 8 * n, cudaMemcpyDeviceToHost, stream));
+    unsigned long long work[2] = {0, 0};
+    FARM_CUDA(cudaMemcpyAsync(work, ctr + 3, 16, cudaMemcpyDeviceToHost, stream));
     FARM_CUDA(cudaStreamSynchronize(stream));
     s->launches += 4;
     if (st) {
         memset(st, 0, sizeof *st);
         st->pairs = n;
+        st->segment_tests = work[0];
+        st->border_pairs = work[1];
         float ms = 0;
         cudaEventElapsedTime(&ms, s->ev[6], s->ev[7]);
         st->ms_total = ms;
@@ -790,8 +884,8 @@ extern "C" int farm_area_plan_run(farm_area_plan *p, const uint32_t *pairs, uint
     FARM_CUDA(cudaEventRecord(s->ev[6], st));
     FARM_CUDA(cudaGraphLaunch(p->exec, st));
     FARM_CUDA(cudaEventRecord(s->ev[7], st));
-    unsigned long long flags[3] = {0, 0, 0};
-    FARM_CUDA(cudaMemcpyAsync(flags, p->ctr.p, 24, cudaMemcpyDeviceToHost, st));
+    unsigned long long flags[5] = {0, 0, 0, 0, 0};  // next, -, overflow, crossing tests, crossings
+    FARM_CUDA(cudaMemcpyAsync(flags, p->ctr.p, 40, cudaMemcpyDeviceToHost, st));
     if (n) FARM_CUDA(cudaMemcpyAsync(out, p->out.p, 8 * n, k_out, st));
     FARM_CUDA(cudaStreamSynchronize(st));
     s->launches += 3;
@@ -808,6 +902,8 @@ extern "C" int farm_area_plan_run(farm_area_plan *p, const uint32_t *pairs, uint
         st_out->ms_total = ms;
         st_out->ms_stage[2] = ms;
         st_out->kernel_launches = 1;  // one graph launch
+        st_out->segment_tests = flags[3];
+        st_out->border_pairs = flags[4];
     }
     return FARM_OK;
 }
