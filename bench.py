@@ -559,8 +559,10 @@ def run_ours(args) -> dict:
     # bytes go back to pinned host memory
     cap = max(sd["xy_bytes"] for sd in strips) // 4
     hbuf = [torch.empty(cap, dtype=torch.float32).pin_memory() for _ in range(2)]
-    hout = torch.empty(max(len(sd["pairs"]) for sd in strips), dtype=torch.uint8).pin_memory()
-    hpairs = {sd["strip"]: torch.from_numpy(sd["pairs"].view(np.int32)).pin_memory() for sd in strips}
+    nmax = max(len(sd["pairs"]) for sd in strips)
+    hout = torch.empty(nmax, dtype=torch.uint8).pin_memory()
+    hpairs_out = torch.empty((nmax, 2), dtype=torch.int32).pin_memory()
+    d_e2e_out = torch.empty(nmax, dtype=torch.uint8, device=dev)
     side = torch.cuda.Stream(dev)
 
     def refill(buf, sd):
@@ -573,16 +575,26 @@ def run_ours(args) -> dict:
         return ev
 
     def step_e2e(sd, buf):
+        # rings in from pinned host memory, candidates by the GPU MBR join,
+        # rasterize, filter + refine, and the pairs with their results out
         ns, nt = sd["d_sx"].numel(), sd["d_tx"].numel()
         store.load(0, sd["so"], buf[:ns].numpy().reshape(-1, 2))
         store.load(1, sd["to"], buf[ns:ns + nt].numpy().reshape(-1, 2))
+        dp = store.mbr_join(device=dev, cap=nmax)
         store.rasterize(vpr=args.vpr, category_count=16, strict=False)
-        n = len(sd["pairs"])
-        _, found = store.intersect(hpairs[sd["strip"]].numpy().view(np.uint32).reshape(-1, 2), out=hout[:n].numpy())
-        return found
+        n = dp.shape[0]
+        _, found = store.intersect(dp, out=d_e2e_out[:n])
+        hout[:n].copy_(d_e2e_out[:n], non_blocking=True)
+        hpairs_out[:n].copy_(dp, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        return found, n
 
     refill(hbuf[0], order[0]).synchronize()
-    step_e2e(order[0], hbuf[0])  # warm-up of the host path
+    _, n0 = step_e2e(order[0], hbuf[0])  # warm-up of the host path
+    # the GPU join's candidates are the host join's, in its order
+    if n0 != len(order[0]["pairs"]) or not np.array_equal(hpairs_out[:n0].numpy().view(np.uint32),
+                                                          order[0]["pairs"]):
+        raise SystemExit("the GPU MBR join differs from the host join")
     refill(hbuf[0], order[0]).synchronize()
     torch.cuda.synchronize()
     if world > 1:
@@ -603,9 +615,9 @@ def run_ours(args) -> dict:
     t_dev, t_e2e, total_pairs = shard.reduce_job(t_dev, t_e2e, pairs_timed, device=dev)
     value = total_pairs / t_dev
     e2e_value = total_pairs / t_e2e
-    h2d = int(sum(sd["xy_bytes"] + 8 * (len(sd["so"]) + len(sd["to"])) + sd["pairs"].nbytes for sd in order)
+    h2d = int(sum(sd["xy_bytes"] + 8 * (len(sd["so"]) + len(sd["to"])) for sd in order)
               / len(order))
-    d2h = int(sum(len(sd["pairs"]) for sd in order) / len(order))
+    d2h = int(sum(9 * len(sd["pairs"]) for sd in order) / len(order))
     del hbuf
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -615,8 +627,10 @@ def run_ours(args) -> dict:
                                   sum(sd["vertices"] for sd in order)),
         "found_in_timed_steps": int(sum(sd.get("found", 0) for sd in order)),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "note": "rings + pairs H2D from pinned host memory and result bytes D2H, every step; the next "
-                        "step's pinned rings are refilled from HBM during the step (inside the timed region)"},
+                "note": "per step: rings H2D from pinned host memory, the candidate pairs by the GPU MBR join (the "
+                        "host join's set and order, checked once), rasterization, filter + refine, and the pairs "
+                        "with their result bytes D2H; the next step's pinned rings are refilled from HBM during "
+                        "the step (inside the timed region)"},
         "gpu_launches": int(launches),
         "clocks": clk,
         "stage_ms": {"load": stage["load_ms"] / args.steps, "raster": stage["raster_ms"] / args.steps,
@@ -653,6 +667,8 @@ def run_ours(args) -> dict:
     store.close()
     del strips
     torch.cuda.empty_cache()
+    if rank == 0 and args.within_strips > 0:
+        result["within"] = within_eval(args)
     if rank == 0 and args.area_pairs > 0:
         result["area"] = area_eval(args)
     if world > 1:
@@ -720,6 +736,137 @@ def area_eval(args) -> dict:
             "nonzero_areas": int((out > 0).sum()), "rasterize_s": ras_s}
 
 
+# ------------------------------------------------- within (config 3) ----
+# Configuration 3: 200,000 star polygons in a 5,000 km square, mean radius
+# log-uniform 0.05..50 km, vertex count log-uniform 32..20,000, within 10 km,
+# planar (no degree scaling), self-join, the reference's default -v 10 and
+# the hierarchy within needs. Coordinates are in kilometres: in metres (up to
+# 5e6) the reference's Box, which starts from low = 1e5 and high = -1e5
+# (Box.h:6-12), would clamp every MBR to begin at 1e5, so the join would pair
+# almost everything; kilometres keep the geometry and stay inside that range.
+W_N, W_SIDE, W_DIST = 200_000, 5000.0, 10.0
+
+
+def within_eval(args) -> dict:
+    """Within-distance pairs/sec on one strip of configuration 3: the sources
+    centred in strip b of args.within_strips, every polygon that can lie
+    within the distance of them, and the self-join candidates (MBRs widened
+    by the distance, each source against every other polygon). One pass is
+    one farm_within_mode call on device pairs, timed with CUDA events (median
+    of three after a warm-up); a CPU oracle sample checks the results and
+    gives the CPU rate on all host cores."""
+    import torch
+    from farm_gb300 import polygons as P
+    from farm_gb300 import shard
+    from farm_gb300.engine import Store
+
+    t0 = time.time()
+    prm = P.StarParams(dom_lo=0.0, dom_hi=W_SIDE, r_lo=0.05, r_hi=50.0, n_lo=32, n_hi=20_000, sigma=0.3)
+    seed = args.seed + 300
+    cen = P.centres(prm, seed, W_N)
+    ext = shard.target_extents(cen, P.radii(prm, seed, W_N))
+    nb = args.within_strips
+    b = nb // 2
+    s_idx = shard.strip_sources(cen, b, nb, W_SIDE)
+    S = P.generate_indices(prm, seed, s_idx)
+    ms = S.mbrs()
+    lo, hi = ms[:, 0].min() - W_DIST, ms[:, 2].max() + W_DIST
+    u_idx = np.nonzero((ext[:, 1] >= lo) & (ext[:, 0] <= hi))[0].astype(np.uint64)
+    U = P.generate_indices(prm, seed, u_idx)
+    mu = U.mbrs()
+    src_pos = np.searchsorted(u_idx, s_idx)
+    loc = P.mbr_join(mu[src_pos], mu, expand=W_DIST, geography=False)
+    keep = src_pos[loc[:, 0]] != loc[:, 1]  # no polygon with itself
+    pairs = np.ascontiguousarray(np.stack([src_pos[loc[keep, 0]], loc[keep, 1]], 1).astype(np.uint32))
+    dev = torch.device("cuda", torch.cuda.current_device())
+    st = Store()
+    st.load(0, U.off, U.xy)
+    st.rasterize(vpr=10, hierarchy=True, strict=False)
+    ras_ms = st.raster_totals()["ms_total"]
+    dp = torch.from_numpy(pairs.view(np.int32)).to(dev).view(len(pairs), 2)
+    out = torch.empty(len(pairs), dtype=torch.uint8, device=dev)
+    st.within(dp, distance=W_DIST, geography=False, self_join=True, out=out)  # warm-up
+    ms, stats = [], {}
+    for _ in range(3):
+        torch.cuda.synchronize()
+        st.event_record(4)
+        st.within(dp, distance=W_DIST, geography=False, self_join=True, out=out)
+        st.event_record(5)
+        ms.append(st.event_elapsed(4, 5))
+        stats = dict(st.last_stats)
+    med = float(np.median(ms))
+    gpu = out.cpu().numpy()
+    st.close()
+    log(f"within: strip {b}/{nb} of configuration 3: {len(s_idx)} sources, {len(u_idx)} polygons, {len(pairs)} "
+        f"pairs, {med:.1f} ms per pass, {int((gpu == 1).sum())} within, {time.time() - t0:.1f} s wall")
+    res = {"metric": "within-distance pairs/sec, configuration 3 strip", "value": len(pairs) / (med * 1e-3),
+           "unit": "pairs/s", "ms_per_pass": med, "passes": 3, "warmup_passes": 1, "dtype": "f32+f64",
+           "rasterize_ms": ras_ms,
+           "config": {"workload": f"configuration 3 in km: {W_N} star polygons in a {W_SIDE:g} km square, radius "
+                                  "0.05..50 km, nv log-uniform 32..20,000, within 10 km, planar, self-join, -v 10 "
+                                  f"with the hierarchy; strip {b} of {nb} by source centre", "sources": int(len(s_idx)),
+                      "polygons_loaded": int(len(u_idx)), "pairs": int(len(pairs)),
+                      "vertices_loaded": int(U.total), "seed": seed},
+           "found": int((gpu == 1).sum()), "sequence_pairs": stats.get("sequence_pairs"),
+           "fp64_rechecks": stats.get("fp64_rechecks"),
+           "fp64_recheck_frac": (stats.get("fp64_rechecks", 0) / stats["sequence_pairs"])
+           if stats.get("sequence_pairs") else None}
+    if not args.no_cpu_baseline:
+        res["cpu_baseline"] = within_cpu(U, pairs, gpu, args)
+    return res
+
+
+def within_cpu(U, pairs, gpu: np.ndarray, args) -> dict:
+    """The CPU oracle's within on all host cores over a cluster sample of the
+    strip's pairs (all pairs of uniformly drawn sources), its rasterization
+    phase from a systematic sample of the loaded polygons by size; also the
+    parity check of the GPU's results on the sample."""
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(args.seed + 301)
+    srcs = rng.permutation(np.unique(pairs[:, 0]))
+    sel, got = [], 0
+    for s_ in srcs:
+        lo_, hi_ = np.searchsorted(pairs[:, 0], s_, "left"), np.searchsorted(pairs[:, 0], s_, "right")
+        sel.append(np.arange(lo_, hi_))
+        got += hi_ - lo_
+        if got >= args.within_parity_pairs:
+            break
+    sel = np.concatenate(sel)
+    polys = np.unique(pairs[sel].ravel())
+    rings = [U.ring(int(k)) for k in polys]
+    ras, _, prep_wall = timed_rasters(rings, 10, threads, hierarchy=True)
+    R = {int(k): r for k, r in zip(polys, ras)}
+    res = np.zeros(len(sel), np.uint8)
+    chunks = [(a, min(a + 8, len(sel))) for a in range(0, len(sel), 8)]
+
+    def run(ab):
+        for k in range(*ab):
+            s_, t_ = (int(v) for v in pairs[sel[k]])
+            a, b_ = R[s_], R[t_]
+            res[k] = 2 if a is None or b_ is None else int(O.within(a, b_, distance=W_DIST, geography=False))
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(run, chunks))
+    q_wall = time.perf_counter() - t0
+    # raster phase of the strip: systematic sample of the loaded polygons by size
+    nv = np.diff(U.off.astype(np.int64))
+    order = np.argsort(nv, kind="stable")
+    k = max(len(order) // 300, 1)
+    samp = order[int(rng.integers(k))::k]
+    _, secs, _ = timed_rasters([U.ring(int(j)) for j in samp], 10, threads, hierarchy=True)
+    raster_s = k * sum(secs) / threads
+    query_s = q_wall * len(pairs) / len(sel)
+    bad = int((gpu[sel] != res).sum())
+    return {"value": len(pairs) / (raster_s + query_s), "unit": "pairs/s", "cores": threads, "kind": "port",
+            "sample": f"query: {len(sel)} pairs of uniformly drawn sources (all their candidates), {q_wall:.2f} s "
+                      f"wall on {threads} threads, scaled to the strip's {len(pairs)} pairs; raster: {len(samp)} "
+                      f"polygons (systematic by size) x{k}",
+            "raster_s": raster_s, "query_s": query_s, "parity_sample_pairs": int(len(sel)),
+            "parity_sample_mismatches": bad, "prep_s": prep_wall}
+
+
 # ------------------------------------------------------- CPU baseline ----
 # The CPU side runs the oracle (a C port of the reference's algorithm) on
 # threads: ctypes releases the GIL, so T threads use T cores at once.
@@ -785,7 +932,7 @@ class CpuSample:
         return out
 
 
-def timed_rasters(rings: list, vpr: int, threads: int) -> tuple[list, list, float]:
+def timed_rasters(rings: list, vpr: int, threads: int, hierarchy: bool = False) -> tuple[list, list, float]:
     """Oracle rasters of the rings on `threads` threads, largest first: the
     rasters (None where the reference fails), each polygon's own seconds
     (measured while all threads run), and the wall time."""
@@ -797,7 +944,7 @@ def timed_rasters(rings: list, vpr: int, threads: int) -> tuple[list, list, floa
     def one(j):
         t = time.perf_counter()
         try:
-            r = O.Raster(rings[j], vpr)
+            r = O.Raster(rings[j], vpr, hierarchy)
         except RuntimeError:
             r = None
         return j, r, time.perf_counter() - t
@@ -987,6 +1134,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--area-pairs", type=int, default=0,
                     help="pairs of the configuration-4 area sample (0 = skip the area block)")
+    ap.add_argument("--within-strips", type=int, default=40,
+                    help="configuration 3 is cut into this many strips and the middle one is timed (0 = skip)")
+    ap.add_argument("--within-parity-pairs", type=int, default=1000)
     ap.add_argument("--no-learned", dest="learned", action="store_false",
                     help="skip training and evaluating the learned scorer")
     ap.add_argument("--learned-pairs", type=int, default=2_000_000, help="training + held-out pairs")
