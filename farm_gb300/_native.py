@@ -49,6 +49,8 @@ def host() -> C.CDLL:
         lib.farm_gen_fill_idx.argtypes = [C.POINTER(GenParams), C.c_uint64, u64p, C.c_uint64, u64p, f32p, C.c_int]
         lib.farm_dt_write.argtypes = [C.c_char_p, C.c_uint64, u64p, f32p]
         lib.farm_dt_read.argtypes = [C.c_char_p, u64p, u64p, u64p, f32p]
+        lib.farm_wkt_read.argtypes = [C.c_char_p, u64p, u64p, u64p, f32p]
+        lib.farm_wkt_to_dt.argtypes = [C.c_char_p, C.c_char_p, u64p]
         lib.farm_mbr.argtypes = [C.c_uint64, u64p, f32p, f64p, C.c_int]
         lib.farm_mbr_join.argtypes = [C.c_uint64, f64p, C.c_uint64, f64p, C.c_double, C.c_int, C.c_int, u64p, u32p,
                                       C.c_int]

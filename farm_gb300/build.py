@@ -143,6 +143,22 @@ def build_query_exe() -> Path:
     return out
 
 
+def build_tools_exe() -> Path:
+    """dump_polygons and generate_polygons: one host-only binary, two names."""
+    out = LIB / "farm_tools"
+    src = HOST / "tools_main.cpp"
+    deps = [src, ROOT / "include" / "farm_host.h", LIB / "libfarm_host.so"]
+    if not _newer(out, deps):
+        _run(["g++", *HOST_FLAGS, "-o", str(out), str(src), f"-L{LIB}", "-lfarm_host", f"-Wl,-rpath,$ORIGIN",
+              "-I", str(ROOT / "include")])
+    for name in ("dump_polygons", "generate_polygons"):
+        link = LIB / name
+        if link.is_symlink() or link.exists():
+            link.unlink()
+        link.symlink_to(out.name)
+    return out
+
+
 def build_all(with_ref: bool = True) -> None:
     with cf.ThreadPoolExecutor(max_workers=3) as ex:
         futs = [ex.submit(build_host), ex.submit(build_oracle), ex.submit(build_cuda)]
@@ -151,6 +167,7 @@ def build_all(with_ref: bool = True) -> None:
         for f in futs:
             f.result()
     build_query_exe()
+    build_tools_exe()
 
 
 if __name__ == "__main__":

@@ -492,3 +492,194 @@ int farm_mbr_join(uint64_t ns, const double *ms, uint64_t nt, const double *mt, 
 }
 
 }  // extern "C"
+
+// ---- WKT polygons (the reference's dump_polygons tool) ----------------------
+//
+// Each line of the input is one WKT geometry, parsed by the reference's rules
+// (storage.cpp:8-94 load_polygon_wkt, :683-715 read_polygon;
+// MyPolygon.cpp:227-262 read_vertices; util.h:108-152 read_double,
+// skip_space), which fix what the tool accepts:
+//  * parsing starts at the line's first '(' (so "POLYGON" or any other prefix
+//    is ignored, and a MULTIPOLYGON yields the boundary of its first polygon);
+//  * a ring's vertex count is one more than the commas between its '(' and the
+//    first ')' after it; each coordinate is the next run of the characters
+//    [-.0-9e] (so "1e+05" reads as the two numbers 1 and 05), converted by
+//    atof and stored as float32;
+//  * rings keep their order: VertexSequence::area() is an absolute value, so
+//    clockwise() is never true; the boundary is never reversed and a hole is
+//    reversed twice;
+//  * holes are parsed (their syntax is checked) but dropped: read_polygon
+//    appends them to the copy that get_holes() returns (MyPolygon.h:132);
+//  * an empty line is skipped. Where the reference asserts (a missing
+//    parenthesis) or reads past the line (no '(' at all, or too few numbers),
+//    this parser reports FARM_EFORMAT with the line number instead.
+namespace {
+
+struct WktPolygon {
+    std::vector<float> boundary;            // interleaved x, y as the WKT lists them
+    std::vector<std::vector<float>> holes;  // the same per hole
+};
+
+struct WktCursor {
+    const std::string &s;
+    size_t o;
+    bool at(char c) const { return o < s.size() && s[o] == c; }
+    void skip_space() {
+        while (o < s.size() && (s[o] == ' ' || s[o] == '\t' || s[o] == '\n')) o++;
+    }
+    static bool number_char(char c) { return c == '-' || c == '.' || (c >= '0' && c <= '9') || c == 'e'; }
+    bool number(double &v) {
+        while (o < s.size() && !number_char(s[o])) o++;
+        if (o >= s.size()) return false;
+        char tmp[100];
+        int k = 0;
+        while (o < s.size() && number_char(s[o])) {
+            if (k == 99) return false;  // the reference's token buffer holds 99 characters
+            tmp[k++] = s[o++];
+        }
+        tmp[k] = 0;
+        v = atof(tmp);
+        return true;
+    }
+    bool ring(std::vector<float> &out) {
+        skip_space();
+        if (!at('(')) return false;
+        o++;
+        size_t close = s.find(')', o);
+        if (close == std::string::npos) return false;
+        uint64_t nv = 1;
+        for (size_t k = o + 1; k < close; k++) nv += s[k] == ',';
+        out.resize(2 * nv);
+        for (uint64_t i = 0; i < 2 * nv; i++) {
+            double v;
+            if (!number(v)) return false;
+            out[i] = (float)v;
+        }
+        skip_space();
+        if (!at(')')) return false;
+        o++;
+        return true;
+    }
+};
+
+// 0: polygon parsed; 1: empty line (skipped); -1: malformed
+int wkt_parse(const std::string &line, WktPolygon &p) {
+    if (line.empty()) return 1;
+    size_t first = line.find('(');
+    if (first == std::string::npos) return -1;
+    WktCursor c{line, first};
+    c.skip_space();
+    if (!c.at('(')) return -1;
+    c.o++;
+    p.boundary.clear();
+    p.holes.clear();
+    if (!c.ring(p.boundary)) return -1;
+    c.skip_space();
+    while (c.at(',')) {
+        c.o++;
+        p.holes.emplace_back();
+        if (!c.ring(p.holes.back())) return -1;
+        c.skip_space();
+    }
+    if (!c.at(')')) return -1;
+    return 0;
+}
+
+int wkt_load(const char *path, std::vector<WktPolygon> &polys) {
+    FILE *f = fopen(path, "rb");
+    if (!f) return fail(FARM_EIO, std::string("cannot open ") + path);
+    std::string line;
+    uint64_t lineno = 0;
+    int ch;
+    bool more = true;
+    while (more) {
+        line.clear();
+        while ((ch = fgetc(f)) != EOF && ch != '\n') line.push_back((char)ch);
+        more = ch != EOF;
+        if (!more && line.empty()) break;
+        lineno++;
+        WktPolygon p;
+        int r = wkt_parse(line, p);
+        if (r < 0) {
+            fclose(f);
+            return fail(FARM_EFORMAT, std::string(path) + ":" + std::to_string(lineno) + ": malformed WKT polygon");
+        }
+        if (r == 0) polys.push_back(std::move(p));
+    }
+    fclose(f);
+    return FARM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int farm_wkt_read(const char *path, uint64_t *n_out, uint64_t *total_out, uint64_t *off, float *xy) {
+    if (!path || !n_out || !total_out) return fail(FARM_EINVAL, "null argument");
+    std::vector<WktPolygon> polys;
+    int rc = wkt_load(path, polys);
+    if (rc) return rc;
+    uint64_t total = 0;
+    for (auto &p : polys) total += p.boundary.size() / 2;
+    *n_out = polys.size();
+    *total_out = total;
+    if (!off || !xy) return FARM_OK;
+    off[0] = 0;
+    uint64_t at = 0;
+    for (size_t k = 0; k < polys.size(); k++) {
+        memcpy(xy + 2 * at, polys[k].boundary.data(), polys[k].boundary.size() * sizeof(float));
+        at += polys[k].boundary.size() / 2;
+        off[k + 1] = at;
+    }
+    return FARM_OK;
+}
+
+int farm_wkt_to_dt(const char *wkt_path, const char *dt_path, uint64_t *n_out) {
+    if (!wkt_path || !dt_path) return fail(FARM_EINVAL, "null argument");
+    std::vector<WktPolygon> polys;
+    int rc = wkt_load(wkt_path, polys);
+    if (rc) return rc;
+    // dump_polygons_to_file (storage.cpp:158-193) with MyPolygon::encode / get_meta
+    // (MyPolygon.cpp:728-745). read_polygon adds each hole through get_holes(),
+    // which returns the hole list by value (MyPolygon.h:132), so the holes are
+    // parsed but never reach the polygon: every record has no holes, and the
+    // meta's vertex count is the boundary's as parsed.
+    FILE *f = fopen(dt_path, "wb");
+    if (!f) return fail(FARM_EIO, std::string("cannot open ") + dt_path);
+    struct Meta {
+        uint32_t size, nv;
+        uint64_t offset;
+        double mbr[4];
+    };
+    static_assert(sizeof(Meta) == 48, "PolygonMeta layout");
+    std::vector<Meta> meta(polys.size());
+    uint64_t cur = 0;
+    bool ok = true;
+    for (size_t k = 0; k < polys.size() && ok; k++) {
+        const WktPolygon &p = polys[k];
+        uint64_t holes = 0, m = p.boundary.size() / 2;
+        uint64_t size = 16 + 8 * m;
+        if (size > 0xFFFFFFFFull) {
+            fclose(f);
+            return fail(FARM_EOVERFLOW, "polygon " + std::to_string(k) + " exceeds the 32-bit record size");
+        }
+        ok &= fwrite(&holes, 8, 1, f) == 1;
+        ok &= fwrite(&m, 8, 1, f) == 1;
+        ok &= fwrite(p.boundary.data(), 8, m, f) == m;
+        Meta &mt = meta[k];
+        mt.size = (uint32_t)size;
+        mt.nv = (uint32_t)m;
+        mt.offset = cur;
+        ring_mbr(p.boundary.data(), m, mt.mbr);
+        cur += size;
+    }
+    uint64_t n = polys.size();
+    if (ok && n) ok &= fwrite(meta.data(), sizeof(Meta), n, f) == n;
+    ok &= fwrite(&n, 8, 1, f) == 1;
+    ok &= fclose(f) == 0;
+    if (!ok) return fail(FARM_EIO, std::string("write failed: ") + dt_path);
+    if (n_out) *n_out = n;
+    return FARM_OK;
+}
+
+}  // extern "C"

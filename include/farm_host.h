@@ -83,6 +83,23 @@ int farm_dt_write(const char *path, uint64_t n, const uint64_t *off, const float
  * count, then with buffers of that size. */
 int farm_dt_read(const char *path, uint64_t *n_out, uint64_t *total_out, uint64_t *off, float *xy);
 
+/* WKT polygons, one per line, parsed by the rules of the reference's
+ * load_polygon_wkt / read_polygon (storage.cpp:8-94, :683-715;
+ * MyPolygon.cpp:227-262): parsing starts at the line's first '(', a ring has
+ * one vertex more than the commas before its first ')', coordinates are runs
+ * of [-.0-9e] read by atof and stored as float32, rings keep their order, a
+ * MULTIPOLYGON yields its first polygon and empty lines are skipped. A line
+ * the reference would assert on or read past gives FARM_EFORMAT.
+ *
+ * farm_wkt_read returns the boundaries as rings, in the two-call protocol of
+ * farm_dt_read. */
+int farm_wkt_read(const char *path, uint64_t *n_out, uint64_t *total_out, uint64_t *off, float *xy);
+/* WKT file to .dt file, byte for byte what the reference's dump_polygons
+ * tool writes (dump_polygons.cpp:4-15, storage.cpp:158-193): records without
+ * holes (the reference's parser appends holes to a copy, MyPolygon.h:132),
+ * each meta's vertex count the boundary's as parsed. n_out may be NULL. */
+int farm_wkt_to_dt(const char *wkt_path, const char *dt_path, uint64_t *n_out);
+
 /* Minimum bounding rectangles of the rings, as the reference computes them:
  * min/max of the float32 vertices in FP64, widened by the float32 constant 1e-9
  * (vertex_sequence.cpp:152-168). mbr is 4 doubles per polygon (lowx lowy highx highy). */

@@ -11,12 +11,17 @@ files, and records what the reference computes for them:
 * ``<case>.pairs.bin.gz`` — every MBR-candidate pair with the reference's
   decision, from ``ref_harness intersect|within``;
 * ``degree_table.json`` — the reference's longitude degree table (util.h:73) as
-  a SHA-256 of its printed values, which the regenerated table must match.
+  a SHA-256 of its printed values, which the regenerated table must match;
+* ``wkt_cases.wkt`` / ``wkt_cases.dt`` — WKT lines covering the parser's rules
+  (prefixes, holes, MULTIPOLYGON, spacing, exponents, many digits, an empty
+  line, a large ring) and the .dt the reference's ``dump_polygons`` tool
+  writes for them.
 
 The .dt inputs are committed next to the outputs, so the tests never need the
 reference or the generator's libm to reproduce them. Usage:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py        # everything
+    python tests/golden/make_golden.py wkt    # the WKT fixture only
 """
 from __future__ import annotations
 
@@ -70,6 +75,47 @@ def sha(p: Path) -> str:
     return hashlib.sha256(p.read_bytes()).hexdigest()
 
 
+def wkt_lines() -> list[str]:
+    """WKT text for the dump_polygons fixture: one case per line."""
+    import numpy as np
+    rng = np.random.default_rng(9)
+    lines = [
+        "POLYGON((0 0, 4 0, 4 3, 0 3, 0 0))",
+        "POLYGON ((10 10, 20 10, 20 20, 10 20, 10 10), (12 12, 12 14, 14 14, 14 12, 12 12))",
+        "SRID=4326;POLYGON((-5.5 -5.5,-1.25 -5.5,-1.25 -1.125,-5.5 -1.125,-5.5 -5.5),"
+        "(-5 -5,-5 -4,-4 -4,-4 -5,-5 -5), (-3 -3, -3 -2.5, -2.5 -2.5, -3 -3))",
+        "MULTIPOLYGON(((30 30, 31 30, 31 31, 30 30)), ((40 40, 42 40, 42 42, 40 40)))",
+        "POLYGON(( 1.5e-3 2.25e1 ,\t3.000000000000001 22.5 , 3 25.75 , 1.5e-3 2.25e1 ))",
+        "",
+        "POLYGON((0.1 0.2, 0.30000000000000004 0.2, 0.30000000000000004 0.7, 0.1 0.7, 0.1 0.2))",
+        "polygon((-179.999999 -89.5, 179.999999 -89.5, 179.999999 89.5, -179.999999 89.5, -179.999999 -89.5))",
+    ]
+    # a large ring: a star of 3,000 vertices written with 17 significant digits
+    n = 3000
+    ang = np.sort(rng.uniform(0, 2 * np.pi, n))
+    rad = 5.0 * np.exp(rng.normal(0, 0.2, n))
+    pts = [(50 + r * np.cos(a), 60 + r * np.sin(a)) for a, r in zip(ang, rad)]
+    pts.append(pts[0])
+    lines.append("POLYGON((" + ", ".join(f"{x:.17g} {y:.17g}" for x, y in pts) + "))")
+    return lines
+
+
+def make_wkt() -> None:
+    exe = REF_SRC and build.build_ref() and (ROOT / "oracle" / "_ref" / "dump_polygons")
+    if not exe or not exe.exists():
+        raise SystemExit("reference sources not found (set FARM_REF_SRC to the reference's src/)")
+    wkt = HERE / "wkt_cases.wkt"
+    wkt.write_text("\n".join(wkt_lines()) + "\n")
+    subprocess.run([str(exe), str(wkt), str(HERE / "wkt_cases.dt")], check=True, stdout=subprocess.DEVNULL,
+                   stderr=subprocess.DEVNULL)
+    mf = HERE / "manifest.json"
+    manifest = json.loads(mf.read_text()) if mf.exists() else {}
+    manifest["wkt"] = {"wkt": wkt.name, "dt": "wkt_cases.dt", "lines": len(wkt_lines()),
+                       "dt_sha256": sha(HERE / "wkt_cases.dt")}
+    mf.write_text(json.dumps(manifest, indent=1))
+    print("wrote the WKT fixture")
+
+
 def main() -> None:
     harness = build.build_ref()
     if harness is None:
@@ -113,7 +159,11 @@ def main() -> None:
         ",".join(vals).encode()).hexdigest()}
     (HERE / "manifest.json").write_text(json.dumps(manifest, indent=1))
     print("wrote", len(RASTER_CASES), "raster and", len(PAIR_CASES), "pair fixtures")
+    make_wkt()
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["wkt"]:
+        make_wkt()
+    else:
+        main()
