@@ -52,6 +52,8 @@ def declare(lib):
                                     C.POINTER(Stats)]
     lib.farm_within_mode.argtypes = [vp, vp, C.c_uint64, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, vp, u64p,
                                      C.POINTER(Stats)]
+    lib.farm_contain.argtypes = [vp, vp, C.c_uint64, C.c_int, vp, u64p, C.POINTER(Stats)]
+    lib.farm_contain_points.argtypes = [vp, C.c_int, vp, C.c_uint64, vp, C.c_uint64, C.c_int, vp, u64p]
     if hasattr(lib, "farm_intersection_area"):
         lib.farm_intersection_area.argtypes = [vp, vp, C.c_uint64, C.c_int, vp, C.POINTER(Stats)]
     lib.farm_raster_fetch.argtypes = [vp, C.c_int, C.c_uint64, C.POINTER(RasterView), u8p, u32p, u32p, u32p, f64p,

@@ -187,6 +187,10 @@ namespace farm {
 // its target index below the target count (the source count when self).
 // Device pairs are checked by a kernel (one synchronisation).
 int check_pairs(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, bool self, const char *who);
+// The same with explicit bounds: first index below n_first, second below
+// n_second; the names label the two counts in the message.
+int check_pair_limits(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, uint64_t n_first,
+                      uint64_t n_second, const char *who, const char *first_name, const char *second_name);
 }  // namespace farm
 
 // The store object behind the C ABI.
@@ -233,6 +237,7 @@ struct farm_store {
     farm::DevBuf cub_tmp;
     farm::DevBuf d_pairs, d_out, d_counters;
     farm::DevBuf d_check;  // pair-index validation counter
+    farm::DevBuf d_points; // staged query points (farm_contain_points)
     cudaEvent_t ev[8] = {};
     uint64_t launches = 0;  // engine kernels launched through this store
     void *mlp = nullptr;    // learned scorer state (mlp.cu)

@@ -1,0 +1,201 @@
+// Segment predicates and the warp-cooperative pixel-pair refinement shared
+// by the intersect and contain queries.
+//
+//   segment_intersect (geometry_computation.h:215-221) with Point::cross
+//   (Point.h:93-97) in FP32 without fused multiply-add, inter1
+//   (geometry_computation.h:195-212), retrieve_pixels (MyRaster.cpp:332-346)
+//   and segment_intersect_batch over two pixels' edge sequences
+//   (geometry_computation.h:224-237).
+#pragma once
+
+#include "common.cuh"
+
+namespace farm {
+
+// Point.h:93-97: (a - o) x (b - o) in float, no fused multiply-add
+__device__ __forceinline__ float cross3(float2 o, float2 a, float2 b) {
+    float ax = __fsub_rn(a.x, o.x), ay = __fsub_rn(a.y, o.y);
+    float bx = __fsub_rn(b.x, o.x), by = __fsub_rn(b.y, o.y);
+    return __fsub_rn(__fmul_rn(ax, by), __fmul_rn(ay, bx));
+}
+
+__device__ __forceinline__ int sgnf(float x) { return x >= 0 ? (x != 0 ? 1 : 0) : -1; }
+
+__device__ __forceinline__ bool inter1(double a, double b, double c, double d) {
+    double t;
+    if (a > b) { t = a; a = b; b = t; }
+    if (c > d) { t = c; c = d; d = t; }
+    return fmax(a, c) <= fmin(b, d);
+}
+
+// geometry_computation.h:215-221
+__device__ __forceinline__ bool seg_intersect(float2 a, float2 b, float2 c, float2 d) {
+    if (cross3(c, a, d) == 0.0f && cross3(c, b, d) == 0.0f)
+        return inter1(a.x, b.x, c.x, d.x) && inter1(a.y, b.y, c.y, d.y);
+    return sgnf(cross3(a, b, c)) != sgnf(cross3(a, b, d)) && sgnf(cross3(c, d, a)) != sgnf(cross3(c, d, b));
+}
+
+struct Window {
+    int sx, ex, sy, ey;
+};
+
+// MyRaster.cpp:332-346
+__device__ __forceinline__ Window retrieve(const double *mbr, double stx, double sty, int dimx, int dimy,
+                                           double b0, double b1, double b2, double b3) {
+    Window w;
+    w.sx = offset_x(mbr, stx, dimx, b0 + 1e-6);
+    w.sy = offset_y(mbr, sty, dimy, b1 + 1e-6);
+    w.ex = offset_x(mbr, stx, dimx, b2 - 1e-6);
+    w.ey = offset_y(mbr, sty, dimy, b3 - 1e-6);
+    return w;
+}
+
+__device__ __forceinline__ int sgn_code(float v) { return (v > 0.f) - (v < 0.f); }
+
+// (b - o) x (p - o) with e = b - o precomputed: the same roundings as cross3(o, b, p)
+__device__ __forceinline__ float cross_e(float2 o, float ex, float ey, float2 p) {
+    return __fsub_rn(__fmul_rn(ex, __fsub_rn(p.y, o.y)), __fmul_rn(ey, __fsub_rn(p.x, o.x)));
+}
+
+__device__ __forceinline__ bool inter1f(float a, float b, float c, float d) {
+    return fmaxf(fminf(a, b), fminf(c, d)) <= fminf(fmaxf(a, b), fmaxf(c, d));
+}
+
+// exclusive warp scan of cnt; total of all lanes in `total`
+__device__ __forceinline__ uint32_t warp_excl_scan(uint32_t cnt, int lane, uint32_t &total) {
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    total = __shfl_sync(0xffffffffu, incl, 31);
+    return incl - cnt;
+}
+
+// the last lane whose exclusive prefix is <= item (the lane that owns item)
+__device__ __forceinline__ int warp_owner(uint32_t excl, uint32_t item) {
+    int owner = 0;
+#pragma unroll
+    for (int b = 16; b; b >>= 1) {
+        int cand = owner + b;
+        uint32_t ex = __shfl_sync(0xffffffffu, excl, cand);
+        if (ex <= item) owner = cand;
+    }
+    return owner;
+}
+
+// Refine one BORDER x BORDER pixel pair: true iff some segment of the source
+// pixel's edge sequences intersects some segment of the target pixel's
+// (segment_intersect_batch over every sequence pair, geometry_computation.h:
+// 215-237; the reference stops at the first hit, so the set of segment pairs
+// it tests differs only in where it stops, and the boolean is the same).
+//
+// Whole-warp tile: each lane holds one source segment (a, b) (sequences of the
+// pixel flattened by a warp scan), and the warp walks the target pixel's
+// vertices in order, 32 at a time staged in shared memory and read as
+// broadcasts. segment_intersect's four cross products are shared along the
+// walk without changing a single rounding:
+//   a.cross(b, c) = cross3(a, b, c) is computed once per target vertex c and
+//     reused for the two target segments that end at c;
+//   c.cross(a, d) = -(c.cross(d, a)) exactly (the two products are the same
+//     IEEE products and round-to-nearest is symmetric), so the collinear test
+//     c.cross(a,d) == 0 && c.cross(b,d) == 0 reads the sign codes of
+//     c.cross(d, a) and c.cross(d, b) that the general test needs anyway.
+// Collinear cases are rare; a target chunk that has one (in a valid lane) is
+// walked again with the interval test (inter1, geometry_computation.h:195-212).
+static __device__ bool refine_pixel_pair(const StoreView &sv, const PolyHdr &S, const PolyHdr &T, uint32_t pa,
+                                         uint32_t pb, float2 *tbuf, unsigned long long &tests) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t *so = sv.offset + S.off, *to = sv.offset + T.off;
+    const uint32_t a0 = so[pa], a1 = so[pa + 1], b0 = to[pb], b1 = to[pb + 1];
+    const uint2 *sseq = sv.seq + S.seq, *tseq = sv.seq + T.seq;
+    const float2 *sr = sv.ring + S.ring, *tr = sv.ring + T.ring;
+    for (uint32_t g = a0; g < a1; g += 32) {
+        const uint32_t k = g + lane;
+        const uint2 r = k < a1 ? sseq[k] : make_uint2(0u, 0u);
+        uint32_t total;
+        const uint32_t excl = warp_excl_scan(r.y, lane, total);  // r.y segments per sequence
+        for (uint32_t sb = 0; sb < total; sb += 32) {
+            const uint32_t f = sb + lane;
+            const bool valid = f < total;
+            const int owner = warp_owner(excl, f);
+            const uint32_t ostart = __shfl_sync(0xffffffffu, r.x, owner);
+            const uint32_t oex = __shfl_sync(0xffffffffu, excl, owner);
+            float2 a = make_float2(0.f, 0.f), b = a;
+            if (valid) {
+                a = sr[ostart + (f - oex)];
+                b = sr[ostart + (f - oex) + 1];
+            }
+            const float ex = __fsub_rn(b.x, a.x), ey = __fsub_rn(b.y, a.y);
+            bool hit = false;
+            int sxp = 0;  // sign of a.cross(b, previous target vertex)
+            float2 cp = make_float2(0.f, 0.f);
+            bool pseg = false;  // previous target vertex starts a segment
+            for (uint32_t tg = b0; tg < b1; tg += 32) {
+                const uint32_t kk = tg + lane;
+                const uint2 r2 = kk < b1 ? tseq[kk] : make_uint2(0u, 0u);
+                uint32_t total2;
+                const uint32_t excl2 = warp_excl_scan(kk < b1 ? r2.y + 1 : 0u, lane, total2);  // vertices
+                for (uint32_t tb = 0; tb < total2; tb += 32) {
+                    const uint32_t f2 = tb + lane;
+                    const bool v2 = f2 < total2;
+                    const int o2 = warp_owner(excl2, f2);
+                    const uint32_t o_start = __shfl_sync(0xffffffffu, r2.x, o2);
+                    const uint32_t o_ex = __shfl_sync(0xffffffffu, excl2, o2);
+                    const uint32_t o_len = __shfl_sync(0xffffffffu, r2.y, o2);
+                    const uint32_t off = f2 - o_ex;
+                    float2 c = make_float2(0.f, 0.f);
+                    if (v2) c = tr[o_start + off];
+                    const unsigned segmask = __ballot_sync(0xffffffffu, v2 && off < o_len);
+                    __syncwarp();
+                    tbuf[lane] = c;
+                    __syncwarp();
+                    const int m = (int)min(32u, total2 - tb);
+                    const float2 cp0 = cp;
+                    const bool pseg0 = pseg;
+                    bool coll = false;
+                    uint32_t nseg = 0;
+#pragma unroll 4
+                    for (int j = 0; j < m; j++) {
+                        const float2 cc = tbuf[j];
+                        const int sxn = sgn_code(cross_e(a, ex, ey, cc));
+                        if (pseg) {  // target segment cp -> cc
+                            const float dx = __fsub_rn(cc.x, cp.x), dy = __fsub_rn(cc.y, cp.y);
+                            const int sya = sgn_code(cross_e(cp, dx, dy, a));
+                            const int syb = sgn_code(cross_e(cp, dx, dy, b));
+                            hit |= (sxp != sxn) & (sya != syb);
+                            coll |= (sya | syb) == 0;
+                            nseg++;
+                        }
+                        sxp = sxn;
+                        cp = cc;
+                        pseg = (segmask >> j) & 1u;
+                    }
+                    if (__any_sync(0xffffffffu, coll && valid)) {
+                        float2 cq = cp0;
+                        bool ps = pseg0;
+                        for (int j = 0; j < m; j++) {
+                            const float2 cc = tbuf[j];
+                            const int sxn = sgn_code(cross_e(a, ex, ey, cc));
+                            if (ps) {
+                                const float dx = __fsub_rn(cc.x, cq.x), dy = __fsub_rn(cc.y, cq.y);
+                                const int sya = sgn_code(cross_e(cq, dx, dy, a));
+                                const int syb = sgn_code(cross_e(cq, dx, dy, b));
+                                if ((sya | syb) == 0)
+                                    hit |= inter1f(a.x, b.x, cq.x, cc.x) && inter1f(a.y, b.y, cq.y, cc.y);
+                            }
+                            cq = cc;
+                            ps = (segmask >> j) & 1u;
+                        }
+                    }
+                    if (valid) tests += nseg;
+                    if (__any_sync(0xffffffffu, hit && valid)) return true;
+                }
+            }
+        }
+    }
+    return false;
+}
+
+}  // namespace farm

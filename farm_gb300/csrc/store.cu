@@ -80,13 +80,13 @@ __global__ void k_check_pairs(const uint32_t *__restrict__ pairs, uint64_t n, ui
     if (mine) atomicAdd(bad, mine);
 }
 
-int check_pairs(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, bool self, const char *who) {
+int check_pair_limits(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, uint64_t n_first,
+                      uint64_t n_second, const char *who, const char *first_name, const char *second_name) {
     if (!n) return FARM_OK;
-    const uint64_t n_src = s->n_side[0], n_tgt = self ? s->n_side[0] : s->n_side[1];
     uint64_t bad = 0, first = ~0ull;
     if (mem == FARM_MEM_HOST) {
         for (uint64_t k = 0; k < n; k++)
-            if (pairs[2 * k] >= n_src || pairs[2 * k + 1] >= n_tgt) {
+            if (pairs[2 * k] >= n_first || pairs[2 * k + 1] >= n_second) {
                 if (!bad) first = k;
                 bad++;
             }
@@ -96,7 +96,7 @@ int check_pairs(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, bool 
         FARM_CUDA(cudaMemsetAsync(d, 0, 8, s->stream));
         unsigned blocks = grid_for(n, 256);
         if (blocks > 8u * (unsigned)sm_count()) blocks = 8u * (unsigned)sm_count();
-        k_check_pairs<<<blocks, 256, 0, s->stream>>>(pairs, n, n_src, n_tgt, d);
+        k_check_pairs<<<blocks, 256, 0, s->stream>>>(pairs, n, n_first, n_second, d);
         FARM_CUDA(cudaGetLastError());
         unsigned long long h = 0;
         FARM_CUDA(cudaMemcpyAsync(&h, d, 8, cudaMemcpyDeviceToHost, s->stream));
@@ -105,12 +105,18 @@ int check_pairs(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, bool 
     }
     if (bad) {
         std::string m = std::string(who) + ": " + std::to_string(bad) + " pair index(es) out of range (" +
-                        std::to_string(n_src) + " sources, " + std::to_string(n_tgt) + " targets)";
+                        std::to_string(n_first) + " " + first_name + ", " + std::to_string(n_second) + " " +
+                        second_name + ")";
         if (first != ~0ull) m += ", first at pair " + std::to_string(first);
         set_error(m);
         return FARM_EINVAL;
     }
     return FARM_OK;
+}
+
+int check_pairs(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, bool self, const char *who) {
+    return check_pair_limits(s, pairs, n, mem, s->n_side[0], self ? s->n_side[0] : s->n_side[1], who, "sources",
+                             "targets");
 }
 
 // Copy stored rings into the padded layout: per polygon the stored vertices,
@@ -210,7 +216,7 @@ void farm_store_destroy(farm_store *s) {
     s->mlp = nullptr;
     DevBuf *bufs[] = {&s->d_xy_in, &s->d_off, &s->d_ring, &s->d_hdr, &s->d_status, &s->d_offset, &s->d_seq,
                       &s->d_hoff, &s->d_hnodes, &s->d_voff, &s->d_vnodes, &s->d_areas, &s->cub_tmp,
-                      &s->d_pairs, &s->d_out, &s->d_counters, &s->d_check};
+                      &s->d_pairs, &s->d_out, &s->d_counters, &s->d_check, &s->d_points};
     for (DevBuf *b : bufs) b->release();
     for (auto &b : s->s) b.release();
     for (auto &ev : s->ev)
@@ -226,7 +232,7 @@ int farm_store_device_bytes(farm_store *s, uint64_t *bytes) {
     }
     const DevBuf *bufs[] = {&s->d_xy_in, &s->d_off, &s->d_ring, &s->d_hdr, &s->d_status, &s->d_offset, &s->d_seq,
                             &s->d_hoff, &s->d_hnodes, &s->d_voff, &s->d_vnodes, &s->d_areas, &s->cub_tmp,
-                            &s->d_pairs, &s->d_out, &s->d_counters, &s->d_check};
+                            &s->d_pairs, &s->d_out, &s->d_counters, &s->d_check, &s->d_points};
     uint64_t t = 0;
     for (const DevBuf *b : bufs) t += b->cap;
     for (const auto &b : s->s) t += b.cap;

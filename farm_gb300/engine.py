@@ -169,6 +169,39 @@ class Store:
         self.last_stats = stats_dict(st)
         return out, found.value
 
+    def contain(self, pairs, out=None):
+        """Ideal::contain(Ideal *) per (source, target) pair: does the source hold the target."""
+        n = pairs.shape[0]
+        pp, mem = _addr(pairs)
+        if out is None:
+            out = np.zeros(n, dtype=np.uint8) if mem == MEM_HOST else _torch_empty_u8(n, pairs.device)
+        po, mo = _addr(out)
+        if mo != mem:
+            raise ValueError("pairs and out must live in the same memory")
+        found = C.c_uint64(0)
+        st = Stats()
+        check_gpu(self._lib.farm_contain(self._h, pp, n, mem, po, C.byref(found), C.byref(st)))
+        self.last_stats = stats_dict(st)
+        return out, found.value
+
+    def contain_points(self, points, pairs, side: int = 0, out=None):
+        """Ideal::contain(Point &) per (polygon, point) pair; points is an
+        [m, 2] float32 array in the same memory as pairs."""
+        if isinstance(points, np.ndarray) and points.dtype != np.float32:
+            raise TypeError("points must be float32")
+        n = pairs.shape[0]
+        pp, mem = _addr(pairs)
+        xp, mx = _addr(points)
+        if mx != mem:
+            raise ValueError("points and pairs must live in the same memory")
+        if out is None:
+            out = np.zeros(n, dtype=np.uint8) if mem == MEM_HOST else _torch_empty_u8(n, pairs.device)
+        po, _ = _addr(out)
+        found = C.c_uint64(0)
+        check_gpu(self._lib.farm_contain_points(self._h, int(side), xp, points.shape[0], pp, n, mem, po,
+                                                C.byref(found)))
+        return out, found.value
+
     def intersection_area(self, pairs, out=None):
         n = pairs.shape[0]
         pp, mem = _addr(pairs)

@@ -141,6 +141,22 @@ int farm_within(farm_store *s, const uint32_t *pairs, uint64_t n, double distanc
 int farm_within_mode(farm_store *s, const uint32_t *pairs, uint64_t n, double distance, int geography,
                      int target_is_source, int mode, int mem, uint8_t *out, uint64_t *found, farm_stats *st);
 
+/* Polygon containment, source[p.s] holds target[p.t], per candidate pair
+ * (Ideal::contain(Ideal *), Ideal.cpp:1159-1231; the reference's GPU form,
+ * query_contain.cu, is commented out, so no reference entry is replaced).
+ * out: one byte per pair, 1 / 0, or 2 where either polygon failed to
+ * rasterize. pairs and out live in memory `mem`. st may be NULL; border_pairs
+ * counts the pixel pairs whose edges were tested and segment_tests the
+ * segment pairs. */
+int farm_contain(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, uint8_t *out, uint64_t *found,
+                 farm_stats *st);
+/* Point containment, polygon p of `side` holds point q (Ideal::contain(Point &),
+ * Ideal.cpp:1101-1157), per (p, q) pair: xy holds npoints float32 (x, y)
+ * points; pairs are (polygon, point) indices; out as for farm_contain. xy,
+ * pairs and out live in memory `mem`. */
+int farm_contain_points(farm_store *s, int side, const float *xy, uint64_t npoints, const uint32_t *pairs,
+                        uint64_t n, int mem, uint8_t *out, uint64_t *found);
+
 /* FP64 area of source[p.s] ∩ target[p.t] for n pairs (out: n doubles). The
  * reference stops before computing it (Ideal.cpp:1683); this is the project's
  * boundary-integral formulation. */

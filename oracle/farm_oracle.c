@@ -1591,6 +1591,115 @@ int fo_segment_contain(const fo_raster *r, const float *ring, float px, float py
     return ret ? 2 : 0;
 }
 
+/* Ideal::contain(Point &) (Ideal.cpp:1101-1157): 1 when the polygon holds
+ * (px, py). The MBR test is box::contain(Point) (Box.cpp:65-70); a BORDER
+ * pixel flips the answer for each of its edges whose FP32 crossing abscissa
+ * lies in [px, the pixel's right border], then once more when an odd number
+ * of the right grid line's nodes lie below py (count_intersection_nodes,
+ * Ideal.cpp:988-1006). */
+int fo_contain_point(const fo_raster *r, const float *ring, float px, float py) {
+    const int cc = 16;
+    const pt *p = (const pt *)ring;
+    if (!(px >= r->mbr[0] && px <= r->mbr[2] && py >= r->mbr[1] && py <= r->mbr[3])) return 0;
+    int xo = off_x(r->mbr, r->step_x, r->dimx, px), yo = off_y(r->mbr, r->step_y, r->dimy, py);
+    int target = yo * r->dimx + xo;
+    double bx_high = r->mbr[0] + (xo + 1) * r->step_x;
+    int st = rs_show(r, (uint32_t)target, cc);
+    if (st == 2) return 1;
+    if (st == 0) return 0;
+    int ret = 0;
+    uint32_t ns = nseq(r, (uint32_t)target, cc);
+    for (uint32_t e = 0; e < ns; e++) {
+        const uint32_t *sq = r->seq + 2 * (r->offset[target] + e);
+        for (uint32_t k = 0; k < sq[1]; k++) {
+            pt a = p[sq[0] + k], b = p[sq[0] + k + 1];
+            if ((a.y >= py) != (b.y >= py)) {
+                /* every operand is a float: the reference evaluates this in FP32 */
+                float dx = b.x - a.x, dyp = py - a.y, dy = b.y - a.y;
+                float prod = dx * dyp;
+                float q = prod / dy;
+                float ix = q + a.x;
+                double int_x = ix;
+                if (px <= int_x && int_x <= bx_high) ret = !ret;
+            }
+        }
+    }
+    if (count_nodes(r, target, py) % 2 == 1) ret = !ret;
+    return ret;
+}
+
+/* Ideal::contain(Ideal *) (Ideal.cpp:1159-1231): 1 when polygon s holds
+ * polygon t. t's MBR must lie in s's (box::contain(box), Box.cpp:59-64); the
+ * s pixels in t's MBR window decide when all are OUT (0) or all IN (1);
+ * otherwise any OUT s pixel over an IN t pixel, any t edge of a BORDER t pixel
+ * crossing the border of an OUT s pixel over it, or any crossing edge pair of
+ * BORDER x BORDER pixels gives 0; failing all of those, t's first vertex
+ * decides. The reference returns at the first violation; every check only
+ * ever returns 0, so the order of the pixel pairs cannot change the answer. */
+int fo_contain(const fo_raster *s, const float *sring, const fo_raster *t, const float *tring, fo_counters *c) {
+    const int cc = 16;
+    fo_counters local = {0};
+    if (!c) c = &local;
+    memset(c, 0, sizeof *c);
+    const pt *sp = (const pt *)sring, *tp = (const pt *)tring;
+    if (!(t->mbr[0] >= s->mbr[0] && t->mbr[2] <= s->mbr[2] && t->mbr[1] >= s->mbr[1] && t->mbr[3] <= s->mbr[3]))
+        return 0;
+    window_t w = retrieve(s->mbr, s->step_x, s->step_y, s->dimx, s->dimy, t->mbr);
+    long nw = (w.ex >= w.sx && w.ey >= w.sy) ? (long)(w.ex - w.sx + 1) * (w.ey - w.sy + 1) : 0;
+    long etn = 0, itn = 0;
+    for (int i = w.sx; i <= w.ex; i++)
+        for (int j = w.sy; j <= w.ey; j++) {
+            int st = rs_show(s, (uint32_t)(j * s->dimx + i), cc);
+            etn += st == 0;
+            itn += st == 2;
+        }
+    c->window_pixels = (uint64_t)nw;
+    if (etn == nw) return 0;
+    if (itn == nw) return 1;
+    for (int i = w.sx; i <= w.ex; i++)
+        for (int j = w.sy; j <= w.ey; j++) {
+            uint32_t pa = (uint32_t)(j * s->dimx + i);
+            int sst = rs_show(s, pa, cc);
+            if (sst == 2) continue;
+            double bx[4] = {s->mbr[0] + i * s->step_x, s->mbr[1] + j * s->step_y, s->mbr[0] + (i + 1) * s->step_x,
+                            s->mbr[1] + (j + 1) * s->step_y};
+            window_t tw = retrieve(t->mbr, t->step_x, t->step_y, t->dimx, t->dimy, bx);
+            for (int u = tw.sx; u <= tw.ex; u++)
+                for (int v = tw.sy; v <= tw.ey; v++) {
+                    uint32_t pb = (uint32_t)(v * t->dimx + u);
+                    int tst = rs_show(t, pb, cc);
+                    if (sst == 0 && tst == 2) return 0;
+                    if (sst == 0 && tst == 1) {
+                        c->pixel_pairs++;
+                        /* the pixel's border as float points, low-low, low-high, high-high, high-low, low-low */
+                        pt border[5] = {{(float)bx[0], (float)bx[1]}, {(float)bx[0], (float)bx[3]},
+                                        {(float)bx[2], (float)bx[3]}, {(float)bx[2], (float)bx[1]},
+                                        {(float)bx[0], (float)bx[1]}};
+                        uint32_t nb = nseq(t, pb, cc);
+                        for (uint32_t e = 0; e < nb; e++) {
+                            const uint32_t *r2 = t->seq + 2 * (t->offset[pb] + e);
+                            c->seq_pairs++;
+                            if (batch_intersect(tp + r2[0], border, (int)r2[1], 4, &c->segment_tests)) return 0;
+                        }
+                    }
+                    if (sst == 1 && tst == 1) {
+                        c->pixel_pairs++;
+                        uint32_t na = nseq(s, pa, cc), nb = nseq(t, pb, cc);
+                        for (uint32_t a = 0; a < na; a++) {
+                            const uint32_t *r = s->seq + 2 * (s->offset[pa] + a);
+                            for (uint32_t b = 0; b < nb; b++) {
+                                const uint32_t *r2 = t->seq + 2 * (t->offset[pb] + b);
+                                c->seq_pairs++;
+                                if (batch_intersect(sp + r[0], tp + r2[0], (int)r[1], (int)r2[1], &c->segment_tests))
+                                    return 0;
+                            }
+                        }
+                    }
+                }
+        }
+    return fo_contain_point(s, sring, tp[0].x, tp[0].y);
+}
+
 /* --------------------------------------------------- area oracle -------- */
 
 /* Even-odd point in polygon, FP64 (points are float-exact in double). */

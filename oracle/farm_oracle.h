@@ -98,6 +98,10 @@ double fo_point_to_segment_distance(const float *p, const float *p1, const float
 
 /* Ideal::segment_contain (Ideal.cpp:1233-1327): 0 OUT, 1 BORDER, 2 IN. */
 int fo_segment_contain(const fo_raster *r, const float *ring, float px, float py);
+/* Ideal::contain(Point &) (Ideal.cpp:1101-1157): 1 when the polygon holds the point. */
+int fo_contain_point(const fo_raster *r, const float *ring, float px, float py);
+/* Ideal::contain(Ideal *) (Ideal.cpp:1159-1231): 1 when s holds t. */
+int fo_contain(const fo_raster *s, const float *sring, const fo_raster *t, const float *tring, fo_counters *c);
 
 /* FP64 area of the intersection of two simple polygons (the project's area
  * oracle: the reference never computes areas). Boundary integral: the parts of

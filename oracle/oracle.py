@@ -62,6 +62,8 @@ def lib() -> C.CDLL:
         L.fo_point_to_segment_distance.argtypes = [fp, fp, fp, C.c_int]
         L.fo_point_to_segment_distance.restype = C.c_double
         L.fo_segment_contain.argtypes = [C.POINTER(FoRaster), fp, C.c_float, C.c_float]
+        L.fo_contain_point.argtypes = [C.POINTER(FoRaster), fp, C.c_float, C.c_float]
+        L.fo_contain.argtypes = [C.POINTER(FoRaster), fp, C.POINTER(FoRaster), fp, C.POINTER(FoCounters)]
         L.fo_intersection_area.argtypes = [fp, C.c_uint32, fp, C.c_uint32]
         L.fo_intersection_area.restype = C.c_double
         L.fo_intersection_area_plain.argtypes = [fp, C.c_uint32, fp, C.c_uint32]
@@ -190,6 +192,60 @@ def intersect(rs: Raster, rt: Raster, counters: bool = False):
     if v < 0:
         raise RuntimeError(f"oracle intersect failed: {v}")
     return (bool(v), c) if counters else bool(v)
+
+
+def contain(rs: Raster, rt: Raster, counters: bool = False):
+    """Ideal::contain(Ideal *): does polygon rs hold polygon rt."""
+    c = FoCounters()
+    fp = C.POINTER(C.c_float)
+    v = lib().fo_contain(C.byref(rs.r), rs.ring.ctypes.data_as(fp), C.byref(rt.r), rt.ring.ctypes.data_as(fp),
+                         C.byref(c))
+    return (bool(v), c) if counters else bool(v)
+
+
+def contain_point(rs: Raster, x: float, y: float) -> bool:
+    """Ideal::contain(Point &): does polygon rs hold the float32 point (x, y)."""
+    fp = C.POINTER(C.c_float)
+    return bool(lib().fo_contain_point(C.byref(rs.r), rs.ring.ctypes.data_as(fp), float(np.float32(x)),
+                                       float(np.float32(y))))
+
+
+def contain_many(rs: list, rt: list, pairs, threads: int = 0) -> np.ndarray:
+    """Oracle polygon containment of (s, t) pairs on a thread pool: 0/1, 2 where
+    either raster is None."""
+    return _pairwise(lambda a, b: contain(a, b), rs, rt, pairs, threads)
+
+
+def contain_points_many(rs: list, pts, pairs, threads: int = 0) -> np.ndarray:
+    """Oracle point containment of (polygon, point) pairs: 0/1, 2 where the
+    polygon's raster is None."""
+    pts = np.asarray(pts, dtype=np.float32)
+    return _pairwise(lambda a, k: contain_point(a, pts[k, 0], pts[k, 1]), rs, range(len(pts)), pairs, threads)
+
+
+def _pairwise(fn, ra, rb, pairs, threads):
+    import concurrent.futures as cf
+    import os
+    pairs = np.asarray(pairs)
+    n = len(pairs)
+    res = np.zeros(n, np.uint8)
+    nt = threads or os.cpu_count() or 1
+    bounds = np.linspace(0, n, min(n, 4 * nt) + 1).astype(np.int64) if n else np.zeros(1, np.int64)
+
+    def run(lo_hi):
+        for k in range(*lo_hi):
+            a, b = ra[int(pairs[k, 0])], rb[int(pairs[k, 1])]
+            res[k] = 2 if a is None or b is None else int(fn(a, b))
+    with cf.ThreadPoolExecutor(max_workers=nt) as ex:
+        list(ex.map(run, zip(bounds[:-1], bounds[1:])))
+    return res
+
+
+def read_points(path: str) -> np.ndarray:
+    """A points file of the contain-point fixtures: uint64 n, then n float32 (x, y)."""
+    buf = open(path, "rb").read()
+    n = int(np.frombuffer(buf, dtype=np.uint64, count=1)[0])
+    return np.frombuffer(buf, dtype=np.float32, count=2 * n, offset=8).reshape(n, 2).copy()
 
 
 def intersect_heuristic(rs: Raster, rt: Raster) -> bool:

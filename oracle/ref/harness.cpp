@@ -6,6 +6,10 @@
 //   ref_harness raster    <in.dt> <vpr> <hier 0|1> <out.bin>
 //   ref_harness intersect <S.dt> <T.dt> <vpr> <out.bin>
 //   ref_harness within    <S.dt> <T.dt|-> <vpr> <out.bin>     (hierarchy on)
+//   ref_harness contain   <S.dt> <T.dt> <vpr> <out.bin>       (s contains t)
+//   ref_harness contain_point <S.dt> <points.bin> <vpr> <out.bin>
+//       points.bin: uint64 n, then n float32 (x, y); a pair is (polygon, point)
+//       for every polygon whose MBR the R-tree finds holding the point
 //
 // Two things are pinned so that the reference's output is deterministic:
 //  * every heap allocation is zero-filled (the reference leaves some arrays it
@@ -208,7 +212,47 @@ int main(int argc, char **argv) {
         for (Ideal *p : ps) dump_raster(w, p);
         return 0;
     }
-    if ((mode == "intersect" || mode == "within") && argc == 6) {
+    if (mode == "contain_point" && argc == 6) {
+        int saved = g_threads;
+        g_threads = 1;
+        vector<Ideal *> S = load(argv[2]);
+        g_threads = saved;
+        FILE *pf = fopen(argv[3], "rb");
+        if (!pf) { perror(argv[3]); return 2; }
+        uint64_t np = 0;
+        if (fread(&np, 8, 1, pf) != 1) { fprintf(stderr, "bad points file\n"); return 2; }
+        vector<Point> pts(np);
+        for (uint64_t k = 0; k < np; k++) {
+            float xy[2];
+            if (fread(xy, 4, 2, pf) != 2) { fprintf(stderr, "bad points file\n"); return 2; }
+            pts[k] = Point(xy[0], xy[1]);
+        }
+        fclose(pf);
+        int vpr = atoi(argv[4]);
+        for (Ideal *p : S) g_tree.Insert(p->getMBB()->low, p->getMBB()->high, p);
+        vector<pair<uint32_t, uint32_t>> pairs;
+        for (uint64_t k = 0; k < np; k++) {
+            double lo[2] = {pts[k].x, pts[k].y};
+            vector<uint32_t> hit;
+            g_tree.Search(lo, lo, [](Ideal *ideal, void *arg) {
+                ((vector<uint32_t> *)arg)->push_back((uint32_t)ideal->id);
+                return true;
+            }, &hit);
+            for (uint32_t h : hit) pairs.push_back(make_pair(h, (uint32_t)k));
+        }
+        rasterize_all(S, vpr, false);
+        vector<uint8_t> res(pairs.size(), 0);
+        parallel_for(pairs.size(), [&](size_t i) {
+            query_context ctx;
+            res[i] = (uint8_t)S[pairs[i].first]->contain(pts[pairs[i].second], &ctx, false);
+        });
+        write_pairs(argv[5], pairs, res);
+        size_t found = 0;
+        for (auto r : res) found += r;
+        printf("pairs %zu found %zu\n", pairs.size(), found);
+        return 0;
+    }
+    if ((mode == "intersect" || mode == "within" || mode == "contain") && argc == 6) {
         int saved = g_threads;
         g_threads = 1;
         vector<Ideal *> S = load(argv[2]);
@@ -238,7 +282,8 @@ int main(int argc, char **argv) {
             query_context ctx;
             Ideal *s = S[pairs[i].first];
             Ideal *t = T[pairs[i].second];
-            res[i] = within ? (uint8_t)s->within(t, &ctx) : (uint8_t)s->intersect(t, &ctx);
+            res[i] = within ? (uint8_t)s->within(t, &ctx)
+                            : mode == "contain" ? (uint8_t)s->contain(t, &ctx, false) : (uint8_t)s->intersect(t, &ctx);
         });
         write_pairs(argv[5], pairs, res);
         size_t found = 0;

@@ -35,6 +35,15 @@ def pair_case(case: dict):
     return S, T, ref
 
 
+def point_case(case: dict):
+    """A contain-point fixture: the polygons, the points and the reference's
+    (polygon, point, result) rows."""
+    S = read_dt(str(GOLDEN / f"{case['name']}_S.dt"))
+    pts = O.read_points(str(GOLDEN / f"{case['name']}_P.bin"))
+    ref = O.read_ref_pairs(_gunzip(f"{case['name']}.pairs.bin.gz"))
+    return S, pts, ref
+
+
 RASTER_FIELDS = ["mbr", "dimx", "dimy", "step", "status", "offset", "seq", "hoff", "hnodes", "voff", "vnodes", "areas",
                  "num_layers"]
 

@@ -12,6 +12,11 @@ files, and records what the reference computes for them:
   decision, from ``ref_harness intersect|within``;
 * ``degree_table.json`` — the reference's longitude degree table (util.h:73) as
   a SHA-256 of its printed values, which the regenerated table must match;
+* ``<case>.pairs.bin.gz`` under the manifest's ``contain`` and
+  ``contain_point`` keys — ``Ideal::contain`` of polygon pairs (large sources
+  holding small targets) and of (polygon, point) pairs, with the points (float32,
+  vertices and edge midpoints of the polygons among uniform ones) in
+  ``<case>_P.bin``;
 * ``wkt_cases.wkt`` / ``wkt_cases.dt`` — WKT lines covering the parser's rules
   (prefixes, holes, MULTIPOLYGON, spacing, exponents, many digits, an empty
   line, a large ring) and the .dt the reference's ``dump_polygons`` tool
@@ -22,6 +27,7 @@ reference or the generator's libm to reproduce them. Usage:
 
     python tests/golden/make_golden.py        # everything
     python tests/golden/make_golden.py wkt    # the WKT fixture only
+    python tests/golden/make_golden.py contain  # the contain fixtures only
 """
 from __future__ import annotations
 
@@ -62,6 +68,83 @@ PAIR_CASES = [
     ("p_intersect_v64_big", StarParams(dom_hi=12.0, n_lo=16, n_hi=20000), 205, 24, 90, 64, "intersect"),
     ("p_within_v64_big", StarParams(dom_hi=12.0, n_lo=16, n_hi=5000), 206, 100, 0, 64, "within"),
 ]
+
+# (name, source params, target params, seed, n_source, n_target, vpr): large
+# sources and small targets in one domain, so that containment occurs
+_BIG = dict(dom_hi=20.0, r_lo=1.0, r_hi=3.0)
+_SMALL = dict(dom_hi=20.0, r_lo=0.02, r_hi=0.6, n_lo=8)
+CONTAIN_CASES = [
+    ("k_contain_v10", StarParams(**_BIG, n_hi=2000), StarParams(**_SMALL, n_hi=400), 301, 40, 500, 10),
+    ("k_contain_v4", StarParams(**_BIG, n_hi=1000), StarParams(**_SMALL, n_hi=200), 302, 30, 400, 4),
+    ("k_contain_v64", StarParams(dom_hi=20.0, r_lo=2.0, r_hi=4.0, n_lo=2000, n_hi=20000),
+     StarParams(dom_hi=20.0, r_lo=0.02, r_hi=0.4, n_lo=8, n_hi=1500), 303, 12, 200, 64),
+]
+# (name, params, seed, n_polygons, n_uniform_points, vpr)
+CONTAIN_POINT_CASES = [
+    ("q_point_v10", StarParams(dom_hi=20.0, r_lo=0.5, r_hi=3.0, n_hi=2000), 311, 40, 6000, 10),
+    ("q_point_v64", StarParams(dom_hi=20.0, r_lo=0.5, r_hi=3.0, n_lo=2000, n_hi=20000), 312, 10, 6000, 64),
+]
+
+
+def contain_points(ps, seed: int, n_uniform: int, lo: float, hi: float):
+    """Query points: uniform ones, every 7th vertex of each polygon, and the
+    float32 midpoints of every 11th edge (points on or next to the boundary)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    pts = [rng.uniform(lo, hi, (n_uniform, 2)).astype(np.float32)]
+    for k in range(ps.n):
+        r = ps.ring(k).astype(np.float32)
+        pts.append(r[::7])
+        a, b = r[:-1:11].astype(np.float64), r[1::11].astype(np.float64)
+        m = len(b)
+        pts.append(((a[:m] + b) / 2).astype(np.float32))
+    return np.ascontiguousarray(np.concatenate(pts), dtype=np.float32)
+
+
+def write_points(path: Path, pts) -> None:
+    import numpy as np
+    with open(path, "wb") as f:
+        f.write(np.uint64(len(pts)).tobytes())
+        f.write(np.ascontiguousarray(pts, dtype=np.float32).tobytes())
+
+
+def make_contain() -> None:
+    harness = build.build_ref()
+    if harness is None:
+        raise SystemExit("reference sources not found (set FARM_REF_SRC to the reference's src/)")
+    build.build_host()
+    tmp = Path("/tmp/farm_golden")
+    tmp.mkdir(exist_ok=True)
+    mf = HERE / "manifest.json"
+    manifest = json.loads(mf.read_text()) if mf.exists() else {}
+    manifest["contain"], manifest["contain_point"] = [], []
+    for name, sp, tp, seed, ns, nt, vpr in CONTAIN_CASES:
+        S, T = generate(sp, seed, ns), generate(tp, seed + 5000, nt)
+        sdt, tdt = HERE / f"{name}_S.dt", HERE / f"{name}_T.dt"
+        S.write_dt(str(sdt))
+        T.write_dt(str(tdt))
+        out = tmp / f"{name}.pairs.bin"
+        subprocess.run([str(harness), "contain", str(sdt), str(tdt), str(vpr), str(out)], check=True,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL, env={"FARM_REF_THREADS": "4"})
+        gz(out, HERE / f"{name}.pairs.bin.gz")
+        manifest["contain"].append({"name": name, "mode": "contain", "vpr": vpr, "seed": seed, "n_source": ns,
+                                    "n_target": nt, "self_join": False, "params": sp.__dict__,
+                                    "target_params": tp.__dict__})
+    for name, prm, seed, n, npts, vpr in CONTAIN_POINT_CASES:
+        S = generate(prm, seed, n)
+        sdt = HERE / f"{name}_S.dt"
+        S.write_dt(str(sdt))
+        pts = contain_points(S, seed, npts, prm.dom_lo - 1.0, prm.dom_hi + 1.0)
+        pbin = HERE / f"{name}_P.bin"
+        write_points(pbin, pts)
+        out = tmp / f"{name}.pairs.bin"
+        subprocess.run([str(harness), "contain_point", str(sdt), str(pbin), str(vpr), str(out)], check=True,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL, env={"FARM_REF_THREADS": "4"})
+        gz(out, HERE / f"{name}.pairs.bin.gz")
+        manifest["contain_point"].append({"name": name, "vpr": vpr, "seed": seed, "n_source": n,
+                                          "n_points": int(len(pts)), "params": prm.__dict__})
+    mf.write_text(json.dumps(manifest, indent=1))
+    print("wrote", len(CONTAIN_CASES), "contain and", len(CONTAIN_POINT_CASES), "contain-point fixtures")
 
 
 def gz(src: Path, dst: Path) -> None:
@@ -160,10 +243,13 @@ def main() -> None:
     (HERE / "manifest.json").write_text(json.dumps(manifest, indent=1))
     print("wrote", len(RASTER_CASES), "raster and", len(PAIR_CASES), "pair fixtures")
     make_wkt()
+    make_contain()
 
 
 if __name__ == "__main__":
     if sys.argv[1:] == ["wkt"]:
         make_wkt()
+    elif sys.argv[1:] == ["contain"]:
+        make_contain()
     else:
         main()

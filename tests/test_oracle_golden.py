@@ -9,7 +9,7 @@ import hashlib
 import numpy as np
 import pytest
 
-from fixtures import manifest, pair_case, raster_case, raster_mismatches
+from fixtures import manifest, pair_case, point_case, raster_case, raster_mismatches
 from farm_gb300.polygons import degree_table, mbr_join
 from oracle import oracle as O
 
@@ -96,3 +96,27 @@ def test_oracle_within_heuristic_small_pixels(host_built):
     a, b = O.Raster(sq, 10, True), O.Raster(sq + np.float32(1.0), 10, True)
     assert not O.within_heuristic(a, b) and not O.within(a, b)
     assert O.within_heuristic(a, a) and O.within(a, a)
+
+
+@pytest.mark.parametrize("case", M.get("contain", []), ids=[c["name"] for c in M.get("contain", [])])
+def test_oracle_contain_matches_reference(host_built, case):
+    """Ideal::contain(Ideal *) of every MBR candidate pair (large sources, small
+    targets): the oracle against the reference's decisions."""
+    S, T, ref = pair_case(case)
+    pairs = mbr_join(S.mbrs(), T.mbrs())
+    assert np.array_equal(pairs.astype(np.int64), ref[:, :2])
+    RS, RT = O.rasterize_set(S, case["vpr"]), O.rasterize_set(T, case["vpr"])
+    got = O.contain_many(RS, RT, pairs)
+    assert np.array_equal(got.astype(np.int64), ref[:, 2]), f"{int((got != ref[:, 2]).sum())} mismatching pairs"
+    assert 0 < got.sum() < len(got)
+
+
+@pytest.mark.parametrize("case", M.get("contain_point", []), ids=[c["name"] for c in M.get("contain_point", [])])
+def test_oracle_contain_point_matches_reference(host_built, case):
+    """Ideal::contain(Point &) of every (polygon, point) pair whose MBR holds
+    the point, points on vertices and edge midpoints included."""
+    S, pts, ref = point_case(case)
+    RS = O.rasterize_set(S, case["vpr"])
+    got = O.contain_points_many(RS, pts, ref[:, :2])
+    assert np.array_equal(got.astype(np.int64), ref[:, 2]), f"{int((got != ref[:, 2]).sum())} mismatching pairs"
+    assert 0 < got.sum() < len(got)
