@@ -137,3 +137,42 @@ def test_gpu_area_autotune(gpu_lib):
     assert np.all(np.abs(tuned - base) <= 1e-9 * scale + 1e-12)
     sel = _checkable(S, T, pairs)
     check(S, T, pairs[sel], tuned[sel])
+
+
+def _star(nv, cx, cy, r, seed, sigma=0.3):
+    prm = P.StarParams(dom_lo=0.0, dom_hi=1e-9, r_lo=r, r_hi=r, n_lo=nv, n_hi=nv, sigma=sigma)
+    ring = P.generate(prm, seed, 1).ring(0).astype(np.float64)
+    ring[:, 0] += cx
+    ring[:, 1] += cy
+    return ring.astype(np.float32)
+
+
+_LARGE = {}
+
+
+@pytest.mark.parametrize("vpr", [10, 64])
+def test_gpu_area_large_polygons(gpu_lib, vpr):
+    """Configuration 4's heavy side: polygons of 50k-200k vertices against
+    sparser polygons whose long spiky edges cross them thousands of times
+    (the case the warp-shared window search exists for), against the FP64
+    oracle (a thread per pair) at 1e-9 relative. The radii keep consecutive
+    vertices a hundred float spacings apart or more, so that rounding the
+    coordinates to float32 leaves every ring simple (general position, which
+    the boundary integral assumes)."""
+    import concurrent.futures as cf
+    dense = [_star(200_000, 10.0, 10.0, 8.0, 1, sigma=0.15), _star(100_000, 10.5, 9.7, 5.0, 2, sigma=0.15),
+             _star(50_000, 9.5, 10.3, 4.0, 3, sigma=0.2)]
+    sparse = [_star(4_000, 10.2, 10.1, 9.0, 11, sigma=0.5), _star(9_000, 9.8, 10.2, 7.0, 12, sigma=0.5),
+              _star(1_500, 10.3, 9.9, 6.0, 13, sigma=0.6), _star(20_000, 10.0, 10.4, 8.0, 14, sigma=0.4)]
+    S, T = mkset(dense), mkset(sparse)
+    pairs = np.array([[0, 0], [0, 2], [1, 1], [1, 0], [2, 3], [2, 2]], np.uint32)
+    out = run_area(S, T, pairs, vpr)
+    if "exp" not in _LARGE:  # the oracle does not depend on -v: computed once
+        with cf.ThreadPoolExecutor(max_workers=len(pairs)) as ex:
+            _LARGE["exp"] = list(ex.map(lambda st: O.intersection_area(S.ring(int(st[0])), T.ring(int(st[1]))),
+                                        pairs))
+    exp = _LARGE["exp"]
+    for k, (s, t) in enumerate(pairs):
+        tol = RTOL * exp[k] + FLOOR * max(ring_area(S.ring(s)), ring_area(T.ring(t)))
+        assert abs(out[k] - exp[k]) <= tol, (k, s, t, out[k], exp[k])
+        assert exp[k] > 0
