@@ -46,6 +46,7 @@ def declare(lib):
     lib.farm_store_destroy.restype = None
     lib.farm_store_load.argtypes = [vp, C.c_int, C.c_uint64, vp, vp, C.c_int]
     lib.farm_rasterize.argtypes = [vp, C.POINTER(RasterOpts)]
+    lib.farm_store_load_dt.argtypes = [vp, C.c_int, C.c_char_p, C.c_int, u64p]
     lib.farm_intersect.argtypes = [vp, vp, C.c_uint64, C.c_int, C.c_int, vp, u64p, C.POINTER(Stats)]
     if hasattr(lib, "farm_within"):
         lib.farm_within.argtypes = [vp, vp, C.c_uint64, C.c_double, C.c_int, C.c_int, C.c_int, vp, u64p,

@@ -187,6 +187,9 @@ namespace farm {
 // its target index below the target count (the source count when self).
 // Device pairs are checked by a kernel (one synchronisation).
 int check_pairs(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, bool self, const char *who);
+// Book a loaded side's offsets (h from 0, n + 1 entries) and room for its
+// padded rings; *ring_first: the float2 index of the side's first ring.
+int stage_side(farm_store *s, int side, std::vector<uint64_t> h, uint64_t *ring_first);
 // The same with explicit bounds: first index below n_first, second below
 // n_second; the names label the two counts in the message.
 int check_pair_limits(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, uint64_t n_first,
@@ -220,6 +223,7 @@ struct farm_store {
     // input rings per side (host layout offsets on device, padded rings)
     uint64_t n_side[2] = {0, 0};
     std::vector<uint64_t> h_off[2];  // host copies of the offsets
+    std::vector<uint64_t> h_cat;     // both sides' offsets, concatenated (the source of d_off)
     farm::DevBuf d_xy_in;            // staging for host rings
     farm::DevBuf d_off;              // offsets of both sides, concatenated (n0+n1+1)
     farm::DevBuf d_ring;             // padded rings of both sides
@@ -238,6 +242,9 @@ struct farm_store {
     farm::DevBuf d_pairs, d_out, d_counters;
     farm::DevBuf d_check;  // pair-index validation counter
     farm::DevBuf d_points; // staged query points (farm_contain_points)
+    void *h_stage[2] = {nullptr, nullptr};  // pinned staging of the .dt loader (farm_store_load_dt)
+    size_t h_stage_cap = 0;
+    cudaEvent_t ev_stage[2] = {};
     cudaEvent_t ev[8] = {};
     uint64_t launches = 0;  // engine kernels launched through this store
     void *mlp = nullptr;    // learned scorer state (mlp.cu)

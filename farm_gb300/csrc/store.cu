@@ -221,6 +221,10 @@ void farm_store_destroy(farm_store *s) {
     for (auto &b : s->s) b.release();
     for (auto &ev : s->ev)
         if (ev) cudaEventDestroy(ev);
+    for (int i = 0; i < 2; i++) {
+        if (s->h_stage[i]) cudaFreeHost(s->h_stage[i]);
+        if (s->ev_stage[i]) cudaEventDestroy(s->ev_stage[i]);
+    }
     cudaStreamDestroy(s->stream);
     delete s;
 }
@@ -245,6 +249,56 @@ int farm_sync(farm_store *s) {
     FARM_CUDA(cudaStreamSynchronize(s->stream));
     return FARM_OK;
 }
+
+}  // extern "C"
+
+namespace farm {
+
+// Book a side's polygons in the store: per-side offsets (h, from 0), the
+// concatenated offsets of both sides on the device, and room in the padded
+// ring array, where polygon p's ring starts at cat[p] + 2p (the source side
+// first, so a target side appends in place when it fits). *ring_first gets
+// the float2 index of this side's first ring. The device offsets are copied
+// from s->h_cat, which stays valid until the next call.
+int stage_side(farm_store *s, int side, std::vector<uint64_t> h, uint64_t *ring_first) {
+    const uint64_t n = h.size() - 1;
+    s->rasterized = false;
+    if (side == 0) {  // a new source side drops any target side
+        s->n_side[1] = 0;
+        s->h_off[1].clear();
+    }
+    s->h_off[side] = std::move(h);
+    s->n_side[side] = n;
+    const uint64_t n0 = s->n_side[0], n1 = s->n_side[1];
+    const uint64_t t0 = s->h_off[0][n0], t1 = n1 ? s->h_off[1][n1] : 0;
+    std::vector<uint64_t> &cat = s->h_cat;
+    cat.assign(n0 + n1 + 1, 0);
+    for (uint64_t k = 0; k <= n0; k++) cat[k] = s->h_off[0][k];
+    for (uint64_t k = 1; k <= n1; k++) cat[n0 + k] = t0 + s->h_off[1][k];
+    const uint64_t total = t0 + t1;
+    const size_t need = (total + 2 * (n0 + n1)) * sizeof(float2) + 64;
+    if (need > s->d_ring.cap) {
+        DevBuf nr;
+        FARM_TRY(nr.ensure(need + need / 8));
+        if (side == 1 && s->d_ring.p)
+            FARM_CUDA(cudaMemcpyAsync(nr.p, s->d_ring.p, (t0 + 2 * n0) * sizeof(float2), cudaMemcpyDeviceToDevice,
+                                      s->stream));
+        FARM_CUDA(cudaStreamSynchronize(s->stream));
+        s->d_ring.release();
+        s->d_ring = nr;
+        nr.p = nullptr;
+    }
+    FARM_TRY(s->d_off.ensure((n0 + n1 + 1) * 8));
+    FARM_CUDA(cudaMemcpyAsync(s->d_off.p, cat.data(), (n0 + n1 + 1) * 8, cudaMemcpyHostToDevice, s->stream));
+    *ring_first = side == 0 ? 0 : t0 + 2 * n0;
+    s->n_poly = n0 + n1;
+    s->n_edges = total;
+    return FARM_OK;
+}
+
+}  // namespace farm
+
+extern "C" {
 
 int farm_store_load(farm_store *s, int side, uint64_t n, const uint64_t *off, const float *xy, int mem) {
     if (!s || side < 0 || side > 1 || !off || (n && !xy)) {
@@ -274,36 +328,11 @@ int farm_store_load(farm_store *s, int side, uint64_t n, const uint64_t *off, co
             return FARM_EOVERFLOW;
         }
     }
-    uint64_t o0 = h[0];
+    const uint64_t o0 = h[0];
     for (auto &v : h) v -= o0;
-    s->rasterized = false;
-    if (side == 0) {  // a new source side drops any target side
-        s->n_side[1] = 0;
-        s->h_off[1].clear();
-    }
-    s->h_off[side] = h;
-    s->n_side[side] = n;
-    uint64_t n0 = s->n_side[0], n1 = s->n_side[1];
-    uint64_t t0 = s->h_off[0][n0], t1 = n1 ? s->h_off[1][n1] : 0;
-    std::vector<uint64_t> cat(n0 + n1 + 1);
-    for (uint64_t k = 0; k <= n0; k++) cat[k] = s->h_off[0][k];
-    for (uint64_t k = 1; k <= n1; k++) cat[n0 + k] = t0 + s->h_off[1][k];
-    uint64_t total = t0 + t1;
-    // padded layout: polygon p's ring starts at cat[p] + 2p. The source side
-    // sits first, so loading the target side appends in place when it fits.
-    size_t need = (total + 2 * (n0 + n1)) * sizeof(float2) + 64;
-    if (need > s->d_ring.cap) {
-        DevBuf nr;
-        FARM_TRY(nr.ensure(need + need / 8));
-        if (side == 1 && s->d_ring.p)
-            FARM_CUDA(cudaMemcpyAsync(nr.p, s->d_ring.p, (t0 + 2 * n0) * sizeof(float2), cudaMemcpyDeviceToDevice,
-                                      s->stream));
-        FARM_CUDA(cudaStreamSynchronize(s->stream));
-        s->d_ring.release();
-        s->d_ring = nr;
-        nr.p = nullptr;
-    }
-    uint64_t side_total = side == 0 ? t0 : t1;
+    const uint64_t side_total = h[n];
+    uint64_t ring_first = 0;
+    FARM_TRY(stage_side(s, side, std::move(h), &ring_first));
     const float2 *src;
     if (mem == FARM_MEM_DEVICE) {
         src = reinterpret_cast<const float2 *>(xy) + o0;
@@ -313,9 +342,7 @@ int farm_store_load(farm_store *s, int side, uint64_t n, const uint64_t *off, co
                                   s->stream));
         src = s->d_xy_in.as<float2>();
     }
-    FARM_TRY(s->d_off.ensure((n0 + n1 + 1) * 8));
-    FARM_CUDA(cudaMemcpyAsync(s->d_off.p, cat.data(), (n0 + n1 + 1) * 8, cudaMemcpyHostToDevice, s->stream));
-    uint64_t first_poly = side == 0 ? 0 : n0;
+    const uint64_t first_poly = side == 0 ? 0 : s->n_side[0];
     if (n) {
         unsigned blocks = grid_for(side_total, 256);
         unsigned cap = 32u * (unsigned)sm_count();
@@ -325,9 +352,7 @@ int farm_store_load(farm_store *s, int side, uint64_t n, const uint64_t *off, co
         FARM_CUDA(cudaGetLastError());
         s->launches++;
     }
-    FARM_CUDA(cudaStreamSynchronize(s->stream));  // the host offset vector dies here
-    s->n_poly = n0 + n1;
-    s->n_edges = total;
+    FARM_CUDA(cudaStreamSynchronize(s->stream));
     return FARM_OK;
 }
 

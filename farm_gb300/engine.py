@@ -98,6 +98,12 @@ class Store:
         else:
             self.n_target = n
 
+    def load_dt(self, side: int, path: str, threads: int = 0) -> int:
+        """Stream a .dt file into one side (farm_store_load_dt); the polygons kept."""
+        n = C.c_uint64(0)
+        check_gpu(self._lib.farm_store_load_dt(self._h, int(side), str(path).encode(), int(threads), C.byref(n)))
+        return n.value
+
     def load_sets(self, source, target=None) -> None:
         self.load(0, source.off, source.xy)
         if target is not None:

@@ -97,6 +97,16 @@ void farm_store_destroy(farm_store *s);
  * For a self-join load side 0 only and pass target_is_source to the queries. */
 int farm_store_load(farm_store *s, int side, uint64_t n, const uint64_t *off, const float *xy, int mem);
 
+/* Load one side straight from a .dt file (storage.cpp format), replacing
+ * the reference's pthread loader (storage.cpp:320-449) and its per-polygon
+ * device copies: the file is mapped, all `threads` host threads (0 = every
+ * core) decode its records into two pinned staging buffers of 256 MiB in the
+ * store's ring layout, and each buffer is copied to HBM asynchronously while
+ * the threads fill the other. Holes are dropped and rings with fewer than 3
+ * in-memory vertices skipped, as the reference's loader does. *n_out (may be
+ * NULL) gets the polygons kept. The same side rules as farm_store_load. */
+int farm_store_load_dt(farm_store *s, int side, const char *path, int threads, uint64_t *n_out);
+
 /* Rasterize every loaded polygon (reference: preprocessing.cpp:4-29,
  * Ideal.cpp:920-955). Must precede the queries. */
 int farm_rasterize(farm_store *s, const farm_raster_opts *o);
