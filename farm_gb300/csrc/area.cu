@@ -67,6 +67,7 @@ struct AreaArgs {
     unsigned long long *overflow;  // [0] unused, [1] items beyond cap_items
     unsigned long long *work;      // [0] FP64 crossing tests, [1] crossings counted
     long wide_window;              // windows above this many pixels: searched by the whole warp
+    int spread;                    // take items in a spread order (see k_area)
 };
 
 __device__ __forceinline__ double cross2(double ax, double ay, double bx, double by) { return ax * by - ay * bx; }
@@ -334,6 +335,12 @@ static long wide_window() {
     return x > 0 ? x : kWideWindow;
 }
 
+// FARM_AREA_SPREAD=0 takes the items in pair order
+static int spread_items() {
+    const char *v = getenv("FARM_AREA_SPREAD");
+    return (v && *v == '0') ? 0 : 1;
+}
+
 
 __global__ void __launch_bounds__(256) k_area(const StoreView sv, AreaArgs a) {
     const int lane = threadIdx.x & 31;
@@ -350,6 +357,16 @@ __global__ void __launch_bounds__(256) k_area(const StoreView sv, AreaArgs a) {
         if (lane == 0) it = atomicAdd(a.next, 1ull);
         it = __shfl_sync(0xffffffffu, it, 0);
         if (it >= nitems) break;
+        // Items lie pair after pair, and the heavy pairs' items are each slow:
+        // taken in that order, a heavy pair near the end leaves a tail. The
+        // k-th item taken is item k * P mod nitems (P prime, coprime to
+        // nitems: a bijection), which spreads every pair's items over the
+        // pass. Each item writes its own partial, and the per-pair reduction
+        // runs in item order, so the results do not depend on this order.
+        if (a.spread) {
+            const uint64_t P = (nitems % 1000003ull) ? 1000003ull : 999983ull;
+            it = (unsigned long long)((it * P) % nitems);
+        }
         uint32_t p = find_segment(a.item_start, (uint32_t)n, it);
         uint64_t rel = it - a.item_start[p];
         const PolyHdr &S = sv.hdr[a.pairs[2 * p]];
@@ -665,7 +682,8 @@ static int area_compute(farm_store *s, const AreaBufs &b, cudaStream_t st) {
                 b.ctr,
                 b.ctr + 1,
                 b.ctr + 3,
-                wide_window()};
+                wide_window(),
+                spread_items()};
     k_area<<<sm_count() * 8, 256, 0, st>>>(s->view(), aa);
     FARM_CUDA(cudaGetLastError());
     unsigned blocks = (unsigned)((b.cap_pairs + 255) / 256);

@@ -198,8 +198,8 @@ int check_pair_limits(farm_store *s, const uint32_t *pairs, uint64_t n, int mem,
 
 // The store object behind the C ABI.
 namespace farm {
-// Scratch slots of farm_store::s. The rasterizer's pipeline uses slots 0-33
-// and 40-43 (raster.cu) only while farm_rasterize runs; the queries reuse Q_SCR0-5
+// Scratch slots of farm_store::s. The rasterizer's pipeline uses slots 0-34
+// and 40-47 (raster.cu) only while farm_rasterize runs; the queries reuse Q_SCR0-5
 // within one call; Q_WITHIN_SUF and Q_AREA_ORIENT are theirs alone (the
 // area orientations stay valid across calls and a captured area plan holds
 // their address).

@@ -44,6 +44,35 @@ __device__ __forceinline__ double apx_area(uint8_t f, double pa, int cc) {
     return ((1.0 * f - 1) / (cc - 2) * pa + (1.0 * f - 0) / (cc - 2) * pa) / 2;
 }
 
+// The warp's queue of BORDER x BORDER pixel pairs in descending fill
+// probability, the order the reference refines candidates in (Ideal.cpp:
+// 1393-1395): a bitonic network over the queue in shared memory, each lane
+// taking every 32nd element. The boolean does not depend on the order; the
+// order decides how soon an intersecting pair meets its first crossing.
+__device__ void sort_queue_desc(float *key, uint2 *val, int n, int lane) {
+    int N = 1;
+    while (N < n) N <<= 1;
+    for (int i = n + lane; i < N; i += 32) key[i] = -INFINITY;
+    __syncwarp();
+    for (int k = 2; k <= N; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = lane; i < N; i += 32) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const float a = key[i], b = key[ixj];
+                    if ((a < b) == ((i & k) == 0)) {
+                        key[i] = b;
+                        key[ixj] = a;
+                        const uint2 t = val[i];
+                        val[i] = val[ixj];
+                        val[ixj] = t;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+}
+
 // kMode: K_EXACT refines; K_APPROX is the reference's -a heuristic
 // (kernel_calculate_probability, query_intersect.cu:100-134) instead of
 // refinement — a BORDER x BORDER pixel pair decides "true" when
@@ -57,9 +86,11 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     k_intersect(const StoreView sv, PairView pv, unsigned long long *__restrict__ next, uint8_t *__restrict__ out,
                 IxCounters *__restrict__ ctr) {
     __shared__ uint2 queue[kWarpsPerBlock][kQueue];
+    __shared__ float qkeys[kWarpsPerBlock][kQueue];
     __shared__ float2 tbufs[kWarpsPerBlock][32];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     uint2 *q = queue[wib];
+    float *qk = qkeys[wib];
     float2 *tb = tbufs[wib];
     const int cc = sv.category_count;
     unsigned long long my_found = 0, my_in = 0, my_bb = 0, my_tests = 0, my_ws = 0, my_wt = 0;
@@ -83,8 +114,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         uint32_t pair_bb = 0;
         int qn = 0;  // warp-uniform queue fill
         auto flush = [&]() {
-            // the warp refines the queued pixel pairs one after another and
-            // stops at the first hit
+            // the warp refines the queued pixel pairs one after another, most
+            // probable first, and stops at the first hit
+            if (qn > 1) sort_queue_desc(qk, q, qn, lane);
             bool hit = false;
             for (int k = 0; k < qn && !hit; k++) {
                 const uint2 pp = q[k];
@@ -144,6 +176,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
                 uint32_t o_pa = __shfl_sync(0xffffffffu, pa, owner);
                 int o_st = __shfl_sync(0xffffffffu, pa_st, owner);
                 bool in_hit = false, bb = false;
+                float prob = 0.f;  // fill probability of a BORDER x BORDER pair (refinement order)
                 uint32_t pb = 0;
                 if (valid) {
                     uint32_t r = item - o_excl;
@@ -156,11 +189,14 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
                             in_hit = true;
                         } else if (kMode == K_APPROX) {
                             const double spa = S.step_x * S.step_y, tpa = T.step_x * T.step_y;
-                            const double prob = (apx_area(sst[o_pa], spa, cc) + apx_area(tst[pb], tpa, cc)) /
-                                                (spa > tpa ? spa : tpa);
-                            in_hit = prob > 1.0;
+                            const double pr = (apx_area(sst[o_pa], spa, cc) + apx_area(tst[pb], tpa, cc)) /
+                                              (spa > tpa ? spa : tpa);
+                            in_hit = pr > 1.0;
                             bb = true;
                         } else {
+                            const double spa = S.step_x * S.step_y, tpa = T.step_x * T.step_y;
+                            prob = (float)((apx_area(sst[o_pa], spa, cc) + apx_area(tst[pb], tpa, cc)) /
+                                           (spa > tpa ? spa : tpa));
                             bb = true;
                         }
                     }
@@ -186,7 +222,11 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
                             break;
                         }
                     }
-                    if (bb) q[qn + __popc(m & ((1u << lane) - 1))] = make_uint2(o_pa, pb);
+                    if (bb) {
+                        const int at = qn + __popc(m & ((1u << lane) - 1));
+                        q[at] = make_uint2(o_pa, pb);
+                        qk[at] = prob;
+                    }
                     qn += nb;
                     if (lane == 0) my_bb += nb;
                     __syncwarp();

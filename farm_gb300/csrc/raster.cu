@@ -72,6 +72,9 @@ enum Scratch {
     S_ROWYF = 41,
     S_WALKF = 42,  // per-polygon walk constants (WalkF)
     S_LINEBIG = 43, // grid lines too long for the shared-memory node sort
+    S_XTILE = 44,   // bucketing (k_bucket): per-polygon tile and counter offsets
+    S_XSLOT = 45,   // bucketing: (bucket, tile) counters and their scan
+    S_XSTART = 34,  // column clip: first point of each polygon
 };
 
 // ------------------------------------------------------------ headers ----
@@ -1203,6 +1206,62 @@ __device__ inline double dval(uint64_t k) {
     return __longlong_as_double((long long)b);
 }
 
+// Lines of at most 32 nodes, most of them: one warp per line, a bitonic
+// network across the lanes (shuffles, no block barrier).
+__global__ void k_line_sort_warp(const double *__restrict__ in, double *__restrict__ out,
+                                 const uint64_t *__restrict__ start, uint64_t nseg) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t l = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; l < nseg; l += nw) {
+        const uint64_t b = start[l], n = start[l + 1] - b;
+        if (n == 0 || n > 32) continue;
+        uint64_t k = (uint64_t)lane < n ? dkey(in[b + lane]) : ~0ull;
+        for (int size = 2; size <= 32; size <<= 1)
+            for (int j = size >> 1; j > 0; j >>= 1) {
+                const uint64_t o = __shfl_xor_sync(full, k, j);
+                const bool up = (lane & size) == 0, lower = (lane & j) == 0;
+                k = (lower == up) ? (k < o ? k : o) : (k < o ? o : k);
+            }
+        if ((uint64_t)lane < n) out[b + lane] = dval(k);
+    }
+}
+
+// Lines of 33 to 256 nodes: one warp per line, a bitonic network over the
+// line in the warp's slice of shared memory (warp barriers only).
+constexpr int kLineMid = 256;
+__global__ void __launch_bounds__(256) k_line_sort_mid(const double *__restrict__ in, double *__restrict__ out,
+                                                       const uint64_t *__restrict__ start, uint64_t nseg) {
+    __shared__ uint64_t sks[8][kLineMid];
+    const int lane = threadIdx.x & 31;
+    uint64_t *sk = sks[threadIdx.x >> 5];
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t l = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; l < nseg; l += nw) {
+        const uint64_t b = start[l], n = start[l + 1] - b;
+        if (n <= 32 || n > (uint64_t)kLineMid) continue;
+        uint32_t N = 64;
+        while (N < n) N <<= 1;
+        for (uint32_t i = lane; i < N; i += 32) sk[i] = i < n ? dkey(in[b + i]) : ~0ull;
+        __syncwarp();
+        for (uint32_t k = 2; k <= N; k <<= 1)
+            for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                for (uint32_t i = lane; i < N; i += 32) {
+                    const uint32_t ixj = i ^ j;
+                    if (ixj > i) {
+                        const uint64_t x = sk[i], y = sk[ixj];
+                        if ((x > y) == ((i & k) == 0)) {
+                            sk[i] = y;
+                            sk[ixj] = x;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        for (uint32_t i = lane; i < n; i += 32) out[b + i] = dval(sk[i]);
+        __syncwarp();
+    }
+}
+
 __global__ void __launch_bounds__(256) k_line_sort(const double *__restrict__ in, double *__restrict__ out,
                                                    const uint64_t *__restrict__ start, uint64_t nseg,
                                                    uint64_t *__restrict__ big_b, uint64_t *__restrict__ big_e,
@@ -1210,7 +1269,7 @@ __global__ void __launch_bounds__(256) k_line_sort(const double *__restrict__ in
     __shared__ uint64_t sk[kLineSortMax];
     for (uint64_t l = blockIdx.x; l < nseg; l += gridDim.x) {
         const uint64_t b = start[l], n = start[l + 1] - b;
-        if (n == 0) continue;
+        if (n <= (uint64_t)kLineMid) continue;  // k_line_sort_warp, k_line_sort_mid
         if (n > (uint64_t)kLineSortMax) {
             if (threadIdx.x == 0) {
                 const unsigned long long at = atomicAdd(nbig, 1ull);
@@ -1262,39 +1321,66 @@ __global__ void k_line_offsets(PolyHdr *__restrict__ hdr, Chunk ch, int vertical
     }
 }
 
-// Ideal.cpp:540-573, one thread per row.
+// Ideal.cpp:540-573: the scanline fill of the non-BORDER pixels.
 __global__ void k_scanline(const PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ rowbase, Chunk ch,
                            uint8_t *__restrict__ status, const uint32_t *__restrict__ hoff,
                            const double *__restrict__ hnodes, int cc) {
-    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ch.nrow;
-         g += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t p = ch.p0 + find_segment(rowbase + ch.p0, ch.np, g + ch.row0);
+    // One warp per row, 32 pixels at a time. The reference's sweep consumes,
+    // at each BORDER pixel x, the row's nodes up to its right border
+    // start_x + step_x * (x + 1), and sets every other pixel from the parity
+    // of the nodes consumed so far. The nodes are sorted, so the nodes
+    // consumed before pixel x are those <= the right border of the last
+    // BORDER pixel left of x: each pixel finds that pixel by a warp max-scan
+    // and counts the nodes by binary search.
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t g = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < ch.nrow; g += nw) {
+        const uint32_t p = ch.p0 + find_segment(rowbase + ch.p0, ch.np, g + ch.row0);
         const PolyHdr &h = hdr[p];
-        int y = (int)(g + ch.row0 - rowbase[p]);
+        const int y = (int)(g + ch.row0 - rowbase[p]);
         if (y < 1 || y >= h.dimy || h.err) continue;
         const double start_x = h.mbr[0];
-        bool isin = false;
-        uint32_t i = hoff[h.hline + y], j = hoff[h.hline + y + 1];
+        const uint32_t i0 = hoff[h.hline + y], j0 = hoff[h.hline + y + 1];
         const double *nodes = hnodes + h.hnode;
         uint8_t *st = status + h.st + (uint64_t)y * h.dimx;
-        for (int x = 0; x < h.dimx; x++) {
-            if (show_status(st[x], cc) != 1) {
+        int carry = -1;  // last BORDER pixel of the earlier batches
+        for (int x0 = 0; x0 < h.dimx; x0 += 32) {
+            const int x = x0 + lane;
+            const bool v = x < h.dimx;
+            const uint8_t sx = v ? st[x] : 0;
+            const bool border = v && show_status(sx, cc) == 1;
+            int last = border ? x : -1;  // inclusive max-scan of BORDER positions
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(full, last, o);
+                if (lane >= o && t > last) last = t;
+            }
+            int before = __shfl_up_sync(full, last, 1);  // last BORDER pixel strictly left of x
+            if (lane == 0) before = -1;
+            if (before < carry) before = carry;
+            if (v && !border) {
+                bool isin = false;
+                if (before >= 0) {
+                    const double rb = start_x + h.step_x * (before + 1);
+                    uint32_t lo = i0, hi = j0;  // first node > rb
+                    while (lo < hi) {
+                        const uint32_t mid = (lo + hi) >> 1;
+                        if (nodes[mid] <= rb) lo = mid + 1;
+                        else hi = mid;
+                    }
+                    isin = ((lo - i0) & 1u) != 0;
+                }
                 st[x] = isin ? 2 : 0;
-                continue;
             }
-            int pass = 0;
-            while (i < j && nodes[i] <= start_x + h.step_x * (x + 1)) {
-                pass++;
-                i++;
-            }
-            if (pass % 2 == 1) isin = !isin;
+            const int tail = __shfl_sync(full, last, 31);
+            if (tail > carry) carry = tail;
         }
     }
 }
 
 // Per edge: points contributed to every column (count pass or emit pass).
 // Both passes run the same arithmetic, so they agree point for point.
-__global__ void k_clipx(const StoreView sv, const PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off,
+__global__ void __launch_bounds__(256, 4) k_clipx(const StoreView sv, const PolyHdr *__restrict__ hdr, const uint64_t *__restrict__ off,
                         Chunk ch, const uint32_t *__restrict__ perm, const double *__restrict__ colx,
                         const LineF *__restrict__ colf, int cert, uint32_t *__restrict__ cnt,
                         const uint64_t *__restrict__ scan, uint64_t *__restrict__ okey, float2 *__restrict__ opt) {
@@ -1339,6 +1425,105 @@ __global__ void k_clipx(const StoreView sv, const PolyHdr *__restrict__ hdr, con
             pi = pi1;
         }
         if (cnt) cnt[k] = total;
+    }
+}
+
+// Stable per-polygon bucketing, in place of global radix sorts whose keys
+// are (polygon-local bucket + the polygon's base): the column clip's points
+// by column (B_COL), the walk's visits by pixel (B_PIX). Items of polygon q
+// of the chunk are [pstart[q], pstart[q + 1]), in the order the reference
+// adds them (clip order, crossing order), each tagged with its key; a
+// bucket's items must keep that order. The polygon's items are cut into
+// tiles of kTile items; one warp per tile counts its items per bucket (lanes
+// with equal buckets found by __match_any_sync), the counters laid out per
+// polygon as [bucket][tile] are scanned once, and the same warps scatter
+// their items to the scanned positions, ranked by lane within each 32-item
+// batch. Polygons are contiguous in the chunk and their buckets ascend with
+// the polygon, so the positions are the chunk's global sorted ones: the
+// result of a stable sort by key. A key outside its polygon's buckets (which
+// a correct walk never writes) is clamped there and the polygon is marked
+// FARM_EINTERNAL.
+constexpr uint32_t kTile = 4096;
+enum BucketKind { B_COL = 0, B_PIX = 1 };
+
+template <int kKind>
+__device__ __forceinline__ void bucket_geom(const PolyHdr &h, const Chunk &ch, uint64_t &base, uint64_t &nb) {
+    if (kKind == B_COL) {
+        base = h.col - ch.col0;
+        nb = h.ncols > 0 ? (uint64_t)h.ncols : 0;
+    } else {
+        base = h.pix - ch.pix0;
+        nb = h.P;
+    }
+}
+
+// per polygon of the chunk: the first item of its points (column clip)
+__global__ void k_xstarts(const uint64_t *__restrict__ off, Chunk ch, const uint64_t *__restrict__ xscan,
+                          uint64_t *__restrict__ pstart) {
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q <= ch.np; q += gridDim.x * blockDim.x)
+        pstart[q] = xscan[off[ch.p0 + q] - ch.e0];
+}
+
+template <int kKind>
+__global__ void k_btiles(const PolyHdr *__restrict__ hdr, Chunk ch, const uint64_t *__restrict__ pstart,
+                         uint64_t *__restrict__ ntile, uint64_t *__restrict__ nslot) {
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q <= ch.np; q += gridDim.x * blockDim.x) {
+        if (q == ch.np) {
+            ntile[q] = 0;
+            nslot[q] = 0;
+            continue;
+        }
+        const uint64_t n = pstart[q + 1] - pstart[q];
+        uint64_t base, nb;
+        bucket_geom<kKind>(hdr[ch.p0 + q], ch, base, nb);
+        if (n && nb == 0) nb = 1;  // clamped keys (k_bucket)
+        const uint64_t t = (n + kTile - 1) / kTile;
+        ntile[q] = t;
+        nslot[q] = t * nb;
+    }
+}
+
+template <int kKind, bool kScatter>
+__global__ void k_bucket(PolyHdr *__restrict__ hdr, Chunk ch, const uint64_t *__restrict__ pstart,
+                         const uint64_t *__restrict__ tileoff, uint64_t ntiles, const uint64_t *__restrict__ slotoff,
+                         uint64_t *__restrict__ slot, const uint64_t *__restrict__ key,
+                         const uint64_t *__restrict__ val, uint64_t *__restrict__ key_out,
+                         uint64_t *__restrict__ val_out) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t t = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntiles; t += nw) {
+        const uint32_t q = find_segment(tileoff, ch.np, t);
+        const uint64_t lt = t - tileoff[q], nt = tileoff[q + 1] - tileoff[q];
+        const uint64_t pb = pstart[q], pe = pstart[q + 1];
+        const uint64_t i0 = pb + lt * kTile, i1 = min(i0 + kTile, pe);
+        uint64_t base, nb;
+        bucket_geom<kKind>(hdr[ch.p0 + q], ch, base, nb);
+        if (nb == 0) nb = 1;
+        uint64_t *S = slot + slotoff[q] + lt;  // bucket b's counter: S[b * nt]
+        for (uint64_t ib = i0; ib < i1; ib += 32) {
+            const uint64_t i = ib + lane;
+            const bool v = i < i1;
+            const unsigned act = __ballot_sync(full, v);
+            if (v) {
+                const uint64_t k = key[i];
+                uint64_t b = k - base;
+                if (b >= nb) {  // never for a correct walk or clip
+                    b = nb - 1;
+                    if (kScatter) atomicMin(&hdr[ch.p0 + q].err, FARM_EINTERNAL);
+                }
+                const unsigned grp = __match_any_sync(act, (uint32_t)b);
+                const bool leader = lane == __ffs(grp) - 1;
+                if (kScatter) {
+                    const uint64_t at = S[b * nt] + (uint64_t)__popc(grp & ((1u << lane) - 1u));
+                    key_out[at] = k;
+                    val_out[at] = val[i];
+                    __syncwarp(act);  // every lane has read its bucket's position
+                }
+                if (leader) S[b * nt] += (uint64_t)__popc(grp);
+            }
+            __syncwarp();
+        }
     }
 }
 
@@ -1569,7 +1754,7 @@ __global__ void k_cp_cost(const PolyHdr *__restrict__ hdr, const uint64_t *__res
 
 // Per column-polygon edge: points contributed to each row (count or emit).
 // Both passes run the same arithmetic, so they agree point for point.
-__global__ void k_clipy(const PolyHdr *__restrict__ hdr, Chunk ch, const uint32_t *__restrict__ perm,
+__global__ void __launch_bounds__(256, 4) k_clipy(const PolyHdr *__restrict__ hdr, Chunk ch, const uint32_t *__restrict__ perm,
                         const uint64_t *__restrict__ cpstart, const float2 *__restrict__ cpoly,
                         const uint32_t *__restrict__ cpcol, const uint32_t *__restrict__ colpoly, uint64_t ncp,
                         const double *__restrict__ rowy, const LineF *__restrict__ rowf, int cert,
@@ -1897,6 +2082,14 @@ static unsigned gb(uint64_t n) {
     return (unsigned)(g ? g : 1);
 }
 
+// blocks for a warp-per-item grid-stride kernel of `warps` warps per block
+static unsigned warp_blocks(uint64_t items, int warps = 8) {
+    uint64_t g = (items + warps - 1) / warps;
+    uint64_t cap = (uint64_t)(256 / warps) * 8ull * sm_count();
+    if (g > cap) g = cap;
+    return (unsigned)(g ? g : 1);
+}
+
 // scratch budget per chunk (crossings and edges bound the sizes of every
 // intermediate array)
 // (FARM_CHUNK_EDGES / FARM_CHUNK_CROSS / FARM_CHUNK_PIX override them, e.g. to
@@ -1975,6 +2168,38 @@ static int edge_order(RasterCtx &R, uint32_t p0, uint32_t np, uint64_t e0, uint6
     return FARM_OK;
 }
 
+// Items [pstart[q], pstart[q + 1]) of each polygon q of the chunk, keyed by
+// key (its base + a bucket), into key_out / val_out stably by key (k_bucket).
+template <int kKind>
+static int bucket_sort(RasterCtx &R, const Chunk &ch, const uint64_t *pstart, const uint64_t *key,
+                       const uint64_t *val, uint64_t *key_out, uint64_t *val_out, uint64_t n) {
+    if (!n) return FARM_OK;
+    farm_store *s = R.s;
+    cudaStream_t st = s->stream;
+    const uint64_t np1 = (uint64_t)ch.np + 1;
+    FARM_TRY(s->s[S_XTILE].ensure(8 * 4 * np1 + 64));
+    uint64_t *ntile = s->s[S_XTILE].as<uint64_t>(), *nslot = ntile + np1, *tileoff = nslot + np1,
+             *slotoff = tileoff + np1;
+    k_btiles<kKind><<<gb(np1), 256, 0, st>>>(R.hdr, ch, pstart, ntile, nslot);
+    FARM_TRY(excl_scan(s, ntile, tileoff, np1));
+    FARM_TRY(excl_scan(s, nslot, slotoff, np1));
+    uint64_t ntiles = 0, nslots = 0;
+    FARM_TRY(d2h(s, &ntiles, tileoff + ch.np, 8));
+    FARM_TRY(d2h(s, &nslots, slotoff + ch.np, 8));
+    FARM_TRY(s->s[S_XSLOT].ensure(16 * (nslots + 1) + 64));
+    uint64_t *cnt = s->s[S_XSLOT].as<uint64_t>(), *pos = cnt + (nslots + 1);
+    FARM_CUDA(cudaMemsetAsync(cnt, 0, 8 * (nslots + 1), st));
+    const unsigned tb = warp_blocks(ntiles);
+    k_bucket<kKind, false><<<tb, 256, 0, st>>>(R.hdr, ch, pstart, tileoff, ntiles, slotoff, cnt, key, val, nullptr,
+                                               nullptr);
+    FARM_TRY(excl_scan(s, cnt, pos, nslots + 1));
+    k_bucket<kKind, true><<<tb, 256, 0, st>>>(R.hdr, ch, pstart, tileoff, ntiles, slotoff, pos, key, val, key_out,
+                                              val_out);
+    R.launches += 3;
+    FARM_CUDA(cudaGetLastError());
+    return FARM_OK;
+}
+
 static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     farm_store *s = R.s;
     cudaStream_t st = s->stream;
@@ -2036,7 +2261,7 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     if (nC) {
         k_visits<<<gb(nC), 256, 0, st>>>(R.hdr, ch, cbase, nC, cfrom, cto, cedge, vkey, vval);
         L++;
-        FARM_TRY(sort_pairs(s, vkey, vkey2, vval, vval2, nC, key_bits(ch.npix)));
+        FARM_TRY(bucket_sort<B_PIX>(R, ch, cbase, vkey, vval, vkey2, vval2, nC));
     }
     FARM_TRY(s->s[S_PIXCNT].ensure(4 * (ch.npix + 1) + 16));
     uint32_t *pixcnt = s->s[S_PIXCNT].as<uint32_t>();
@@ -2092,8 +2317,10 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
             unsigned long long *nbig = reinterpret_cast<unsigned long long *>(big_e + (nl + 1));
             FARM_CUDA(cudaMemsetAsync(nbig, 0, 8, st));
             unsigned lb = (unsigned)std::min<uint64_t>(nl, 8ull * sm_count());
+            k_line_sort_warp<<<warp_blocks(nl), 256, 0, st>>>(unsorted, nodes_out, lstart, nl);
+            k_line_sort_mid<<<warp_blocks(nl), 256, 0, st>>>(unsorted, nodes_out, lstart, nl);
             k_line_sort<<<lb ? lb : 1, 256, 0, st>>>(unsorted, nodes_out, lstart, nl, big_b, big_e, nbig);
-            L++;
+            L += 3;
             unsigned long long hbig = 0;
             FARM_TRY(d2h(s, &hbig, nbig, 8));
             if (hbig) {  // lines beyond the shared-memory sort: the library's segmented sort
@@ -2109,8 +2336,8 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     }
 
     // ---- scanline
-    k_scanline<<<gb(ch.nrow), 256, 0, st>>>(R.hdr, rowbase, ch, s->d_status.as<uint8_t>(), s->d_hoff.as<uint32_t>(),
-                                            s->d_hnodes.as<double>(), R.cc);
+    k_scanline<<<warp_blocks(ch.nrow), 256, 0, st>>>(R.hdr, rowbase, ch, s->d_status.as<uint8_t>(),
+                                                     s->d_hoff.as<uint32_t>(), s->d_hnodes.as<double>(), R.cc);
     L++;
 
     // ---- fill: strip clip per column
@@ -2136,13 +2363,23 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     FARM_TRY(s->s[S_VVAL2].ensure(8 * nX + 16));
     uint64_t *xkey = s->s[S_VKEY].as<uint64_t>(), *xkey_s = s->s[S_VKEY2].as<uint64_t>();
     float2 *xpt = s->s[S_VVAL].as<float2>(), *xpt_s = s->s[S_VVAL2].as<float2>();
-    const int colbits = key_bits(ch.ncol);
     if (nX) {
         R.timer.time(T_CLIPX, st, [&] { k_clipx<<<gb(ne), 256, 0, st>>>(sv, R.hdr, R.doff, ch, xperm, R.colx, R.colf, R.cert, nullptr, xscan, xkey, xpt); });
         L++;
-        FARM_TRY(sort_pairs(s, xkey, xkey_s, reinterpret_cast<uint64_t *>(xpt), reinterpret_cast<uint64_t *>(xpt_s),
-                            nX, colbits));
+        // group the points by column (k_bucket), in clip order within each
+        FARM_TRY(s->s[S_XSTART].ensure(8 * ((uint64_t)ch.np + 1) + 64));
+        uint64_t *pstart = s->s[S_XSTART].as<uint64_t>();
+        k_xstarts<<<gb((uint64_t)ch.np + 1), 256, 0, st>>>(R.doff, ch, xscan, pstart);
+        L++;
+        FARM_TRY(bucket_sort<B_COL>(R, ch, pstart, xkey, reinterpret_cast<const uint64_t *>(xpt), xkey_s,
+                                    reinterpret_cast<uint64_t *>(xpt_s), nX));
     }
+    // column starts (the points are grouped by column)
+    const uint64_t ncol = ch.ncol;
+    FARM_TRY(s->s[S_LINESCAN].ensure(8 * (ncol + 1) + 16));
+    uint64_t *colstart = s->s[S_LINESCAN].as<uint64_t>();
+    k_seg_starts<<<gb(nX + 1), 256, 0, st>>>(xkey_s, nX, ncol, colstart);
+    L++;
     // duplicates: one stable sort by (column, 16-bit hash of the bits), then
     // a backward scan of each run
     FARM_TRY(s->s[S_HKEY].ensure(8 * nX + 16));
@@ -2159,16 +2396,10 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
     if (nX) {
         k_ptbits<<<gb(nX), 256, 0, st>>>(xpt_s, xkey_s, nX, bits, pos);
         L++;
-        FARM_TRY(sort_pairs(s, bits, bits_s, pos, pos_s, nX, colbits + 16));
+        FARM_TRY(sort_pairs(s, bits, bits_s, pos, pos_s, nX, key_bits(ch.ncol) + 16));
         k_dup_hash<<<gb(nX), 256, 0, st>>>(bits_s, pos_s, xpt_s, nX, drop);
         L++;
     }
-    // column starts (the points are sorted by column)
-    const uint64_t ncol = ch.ncol;
-    FARM_TRY(s->s[S_LINESCAN].ensure(8 * (ncol + 1) + 16));
-    uint64_t *colstart = s->s[S_LINESCAN].as<uint64_t>();
-    k_seg_starts<<<gb(nX + 1), 256, 0, st>>>(xkey_s, nX, ncol, colstart);
-    L++;
     if (nX) {
         // small first copies: tolerance-equality dependencies, then the
         // sequential rule on them
