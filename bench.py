@@ -181,13 +181,15 @@ def filter_bytes(stats: dict, n_pairs: int, bits: int) -> float:
 FP64_NOMINAL = 2 * 152 * 2.07e9
 FP32_NOMINAL = 128 * 152 * 2.07e9
 
-# DRAM traffic per unit of the rasterizer's heavy kernels, from one ncu
-# capture each (dram__bytes_read.sum + dram__bytes_write.sum per launch, divided
-# by the units that launch processed); the capture command and the figures are
-# in profiles/k_walk_k_clip_small_strip.md. Per launch here = per unit x the
-# units of the measured launches.
+# DRAM traffic per unit of the kernels that can be the dominant one, from one
+# ncu capture on a small configuration-2 strip (dram__bytes_read.sum +
+# dram__bytes_write.sum summed over the launches, divided by the units they
+# processed); the capture command and the figures are in
+# profiles/dram_traffic_small_strip.md. A step's traffic is the per-unit
+# figure times the step's units.
 TRAFFIC_PER_UNIT = {
-    "edge_walk": None,   # bytes per edge (k_walk_tot + k_walk_fill)
+    "edge_walk": 523.1,   # bytes per edge (k_walk_tot + k_walk_fill): 112.0 GB / 2.14e8 edges
+    "refine": 6640.6,     # bytes per candidate pair (k_intersect): 174.8 MB / 26,320 pairs
 }
 
 
@@ -283,10 +285,11 @@ def rooflines(rt: dict, qs: dict, n_pairs: float, stage: dict, steps: int, peaks
     dom["kernel"] = {"edge_walk": "k_walk_tot + k_walk_fill", "cell_clip": "k_clipy (count + emit)",
                      "column_clip": "k_clipx (count + emit)", "cell_area": "k_cells",
                      "refine": "k_intersect (filter + refine)"}[name]
-    units = {"edge_walk": rt["vertices"] / steps}
+    units = {"edge_walk": rt["vertices"] / steps, "refine": n_pairs / steps}
     tpu = TRAFFIC_PER_UNIT.get(name)
     dom["traffic"] = tpu * units[name] if tpu and name in units else None
-    dom["traffic_note"] = ("ncu dram bytes per unit x units per step (profiles/)" if dom["traffic"] else
+    dom["traffic_note"] = ("ncu dram bytes per unit on a 400-strip case x units per step "
+                           "(profiles/dram_traffic_small_strip.md)" if dom["traffic"] else
                            "no ncu capture of this kernel's DRAM bytes")
     return {"dominant": dom, "stages": st}
 
@@ -1132,7 +1135,7 @@ def main():
     ap.add_argument("--ref-raster-sample", type=int, default=150,
                     help="polygons of the raster-phase sample per step of --impl reference")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--area-pairs", type=int, default=0,
+    ap.add_argument("--area-pairs", type=int, default=1000,
                     help="pairs of the configuration-4 area sample (0 = skip the area block)")
     ap.add_argument("--within-strips", type=int, default=40,
                     help="configuration 3 is cut into this many strips and the middle one is timed (0 = skip)")
