@@ -214,6 +214,7 @@ enum ScratchSlot : int {
     Q_AREA_ORIENT = 36,
     Q_AREA_EPOFF = 37,  // area: edge -> pixel index offsets (per ring position)
     Q_AREA_EPPIX = 38,  // area: edge -> pixel index entries
+    Q_PAIR_ORDER = 39,  // intersect: the longest-first pair order
 };
 }  // namespace farm
 

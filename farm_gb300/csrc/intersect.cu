@@ -13,6 +13,7 @@
 // at the first decisive hit.
 #include <cub/cub.cuh>
 
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -30,6 +31,7 @@ struct PairView {
     uint64_t n;
     uint64_t tgt_base;         // global index of target 0
     uint32_t *bb = nullptr;    // K_FILTER: per pair, refinement cost proxy (float bits)
+    const uint32_t *order = nullptr;  // pairs taken in this order (largest first), else in index order
 };
 
 struct IxCounters {
@@ -96,7 +98,10 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     unsigned long long my_found = 0, my_in = 0, my_bb = 0, my_tests = 0, my_ws = 0, my_wt = 0;
     for (;;) {
         unsigned long long pid = 0;
-        if (lane == 0) pid = atomicAdd(next, 1ull);
+        if (lane == 0) {
+            pid = atomicAdd(next, 1ull);
+            if (pv.order && pid < pv.n) pid = pv.order[pid];
+        }
         pid = __shfl_sync(0xffffffffu, pid, 0);
         if (pid >= pv.n) break;
         const uint32_t s = pv.pairs[2 * pid], t = pv.pairs[2 * pid + 1];
@@ -285,6 +290,45 @@ int intersect_filter(farm_store *s, const uint32_t *dpairs, uint64_t n, uint8_t 
     return FARM_OK;
 }
 
+// Work order for the exact query: pairs by descending product of their
+// polygons' vertex counts, so that the heaviest pairs start first and the
+// pass does not end on a long pair that started last (longest-first
+// scheduling). Results are written by pair index, so the order is invisible.
+__global__ void k_pair_cost(const StoreView sv, const uint32_t *__restrict__ pairs, uint64_t n, uint64_t tgt_base,
+                            uint32_t *__restrict__ key, uint32_t *__restrict__ idx) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        const float c = (float)sv.hdr[pairs[2 * k]].nv * (float)sv.hdr[tgt_base + pairs[2 * k + 1]].nv;
+        key[k] = ~__float_as_uint(c);  // positive floats order as their bits; ~ for descending
+        idx[k] = (uint32_t)k;
+    }
+}
+
+// FARM_PAIR_ORDER=0 takes the pairs in index order
+static bool pair_order_on() {
+    const char *v = getenv("FARM_PAIR_ORDER");
+    return !(v && *v == '0');
+}
+
+static int pair_order(farm_store *s, const uint32_t *dpairs, uint64_t n, const uint32_t **order) {
+    *order = nullptr;
+    if (n < 2 || n > 0xFFFFFFFFull) return FARM_OK;
+    cudaStream_t stream = s->stream;
+    FARM_TRY(s->s[Q_PAIR_ORDER].ensure(16 * n + 64));
+    uint32_t *key = s->s[Q_PAIR_ORDER].as<uint32_t>(), *key_s = key + n, *idx = key_s + n, *idx_s = idx + n;
+    unsigned blocks = grid_for(n, 256);
+    if (blocks > 16u * (unsigned)sm_count()) blocks = 16u * (unsigned)sm_count();
+    k_pair_cost<<<blocks, 256, 0, stream>>>(s->view(), dpairs, n, s->n_side[0], key, idx);
+    FARM_CUDA(cudaGetLastError());
+    s->launches++;
+    size_t bytes = 0;
+    FARM_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, bytes, key, key_s, idx, idx_s, (int64_t)n, 0, 32, stream));
+    FARM_TRY(s->cub_tmp.ensure(bytes + 64));
+    FARM_CUDA(cub::DeviceRadixSort::SortPairs(s->cub_tmp.p, bytes, key, key_s, idx, idx_s, (int64_t)n, 0, 32,
+                                              stream));
+    *order = idx_s;
+    return FARM_OK;
+}
+
 int intersect(farm_store *s, const uint32_t *pairs, uint64_t n, int mode, int mem, uint8_t *out, uint64_t *found,
               farm_stats *st) {
     if (!s->rasterized) {
@@ -315,6 +359,7 @@ int intersect(farm_store *s, const uint32_t *pairs, uint64_t n, int mode, int me
     PairView pv{dpairs, n, s->n_side[0]};
     StoreView sv = s->view();
     FARM_CUDA(cudaEventRecord(s->ev[6], stream));
+    if (mode == FARM_MODE_EXACT && pair_order_on()) FARM_TRY(pair_order(s, dpairs, n, &pv.order));
     int blocks = sm_count() * 8;
     if (mode == FARM_MODE_APPROX)
         k_intersect<K_APPROX><<<blocks, kWarpsPerBlock * 32, 0, stream>>>(sv, pv, next, dout, ctr);
