@@ -694,8 +694,9 @@ def area_eval(args) -> dict:
     Configuration 4 mixes tiny and huge polygons (vertex counts log-uniform
     8..200,000 on each side) in one launch. The sample draws two pools of
     polygons from the star generator and takes args.area_pairs of their
-    MBR-overlapping pairs at random, in one batch: one CUDA-graph launch of
-    the persistent work-stealing kernel per pass. value = pairs / device time
+    MBR-overlapping pairs at random, in one batch: the autotuner first picks
+    the per-bucket knobs on a subsample, then one CUDA-graph launch of the
+    persistent work-stealing kernel per pass. value = pairs / device time
     of one pass, timed with CUDA events (median of three passes after one
     warm-up pass)."""
     from farm_gb300 import polygons as P
@@ -714,8 +715,17 @@ def area_eval(args) -> dict:
     st.load_sets(S, T)
     st.rasterize(vpr=10, strict=False)
     ras_s = st.raster_totals()["ms_total"] / 1000.0
-    # items per pair at the smallest chunk the autotuner may pick (32 edges)
-    plan = st.area_plan(max_pairs=len(pairs), max_items=int(((es + 31) // 32 + (et + 31) // 32).sum()) + 64)
+    # the autotuner picks both knobs per size bucket on a 30% subsample of the
+    # batch (chunk: edges per work item; window: pixels above which an edge is
+    # searched by the whole warp); the plan below is captured with its tables
+    t_tune = time.time()
+    tune_sel = np.sort(rng.permutation(len(pairs))[:max(1, (3 * len(pairs)) // 10)])
+    chunk_tab, wide_tab = st.area_autotune(pairs[tune_sel], with_wide=True)
+    tune_s = time.time() - t_tune
+    tuned = {str(b): [int(chunk_tab[b]), int(wide_tab[b])] for b in range(32) if chunk_tab[b] > 0}
+    log(f"area autotune: {tune_s:.1f} s on {len(tune_sel)} pairs, bucket -> [chunk, window] {tuned}")
+    # items per pair at the smallest chunk the autotuner may pick (8 edges)
+    plan = st.area_plan(max_pairs=len(pairs), max_items=int(((es + 7) // 8 + (et + 7) // 8).sum()) + 64)
     plan.run(pairs)
     warm_ms = plan.last_stats["ms_total"]
     ms = []
@@ -736,7 +746,11 @@ def area_eval(args) -> dict:
                                    "graph launch per pass", "vpr": 10, "pairs": len(pairs),
                        "edges_in_pairs": int(es.sum() + et.sum()), "largest_pair_edges": int((es + et).max()),
                        "pool_vertices": int(S.total + T.total), "seed": args.seed + 400},
-            "nonzero_areas": int((out > 0).sum()), "rasterize_s": ras_s}
+            "nonzero_areas": int((out > 0).sum()), "rasterize_s": ras_s,
+            "autotune": {"sample_pairs": int(len(tune_sel)), "seconds": tune_s,
+                         "bucket_to_chunk_window": tuned,
+                         "note": "bucket = floor(log2(larger edge count)); chunk = edges per work item, "
+                                 "window = candidate-window pixels above which the whole warp shares an edge"}}
 
 
 # ------------------------------------------------- within (config 3) ----

@@ -76,7 +76,8 @@ def declare(lib):
     lib.farm_area_plan_destroy.argtypes = [vp]
     lib.farm_area_plan_destroy.restype = None
     lib.farm_area_set_chunks.argtypes = [vp, vp]
-    lib.farm_area_autotune.argtypes = [vp, vp, C.c_uint64, C.c_int, vp]
+    lib.farm_area_autotune.argtypes = [vp, vp, C.c_uint64, C.c_int, vp, vp]
+    lib.farm_area_set_wide.argtypes = [vp, vp]
     lib.farm_mlp_set_band_cost.argtypes = [vp, C.c_float]
     lib.farm_intersect_filter.argtypes = [vp, vp, C.c_uint64, vp, vp]
     lib.farm_mlp_features.argtypes = [vp, vp, C.c_uint64, vp, C.c_uint64]

@@ -34,15 +34,20 @@
 
 namespace farm {
 
-// Edges per work item by size bucket: bucket b holds pairs whose larger edge
-// count has floor(log2) == b. Chosen by farm_area_autotune (default 256).
+// The two tuning knobs of the area pass by size bucket (bucket b holds pairs
+// whose larger edge count has floor(log2) == b), chosen by farm_area_autotune:
+// c, the edges per work item (default 16), and w, the candidate-window size in
+// pixels above which an edge is searched by the whole warp instead of its own
+// lane (default 200).
 struct Chunks {
     uint16_t c[32];
-    __host__ __device__ uint32_t of(uint32_t es, uint32_t et) const {
+    uint16_t w[32];
+    __host__ __device__ static int bucket(uint32_t es, uint32_t et) {
         uint32_t m = es > et ? es : et;
-        int b = m ? 31 - clz32(m) : 0;
-        return c[b];
+        return m ? 31 - clz32(m) : 0;
     }
+    __host__ __device__ uint32_t of(uint32_t es, uint32_t et) const { return c[bucket(es, et)]; }
+    __host__ __device__ uint32_t wide_of(uint32_t es, uint32_t et) const { return w[bucket(es, et)]; }
     __host__ __device__ static int clz32(uint32_t x) {
 #ifdef __CUDA_ARCH__
         return __clz(x);
@@ -66,7 +71,6 @@ struct AreaArgs {
     unsigned long long *next;
     unsigned long long *overflow;  // [0] unused, [1] items beyond cap_items
     unsigned long long *work;      // [0] FP64 crossing tests, [1] crossings counted
-    long wide_window;              // windows above this many pixels: searched by the whole warp
     int spread;                    // take items in a spread order (see k_area)
 };
 
@@ -323,16 +327,18 @@ __device__ __forceinline__ bool crossing(double px, double py, double dx, double
     return t >= 0 && t < 1 && u >= 0 && u < 1;
 }
 
-// An edge whose candidate window holds more pixels than this is searched by
-// the whole warp (for_candidate_edges_warp) instead of its own lane
-// (FARM_AREA_WIDE_WINDOW overrides it).
-constexpr long kWideWindow = 48;
+// Default knobs: edges per item, and the window size (pixels) above which an
+// edge is searched by the whole warp (for_candidate_edges_warp) instead of
+// its own lane. FARM_AREA_WIDE_WINDOW overrides the window size of every
+// bucket.
+constexpr int kDefaultChunk = 16;
+constexpr int kDefaultWide = 200;
 
-static long wide_window() {
+static long wide_window_env() {
     const char *v = getenv("FARM_AREA_WIDE_WINDOW");
-    if (!v || !*v) return kWideWindow;
+    if (!v || !*v) return 0;
     const long x = strtol(v, nullptr, 10);
-    return x > 0 ? x : kWideWindow;
+    return x > 0 && x < 65536 ? x : 0;
 }
 
 // FARM_AREA_SPREAD=0 takes the items in pair order
@@ -373,6 +379,7 @@ __global__ void __launch_bounds__(256) k_area(const StoreView sv, AreaArgs a) {
         const PolyHdr &T = sv.hdr[a.tgt_base + a.pairs[2 * p + 1]];
         uint32_t es = S.nv - 1, et = T.nv - 1;  // edges (the ring's last edge is the zero-length closing one)
         const uint32_t chunk = a.chunks.of(es, et);
+        const long wide_window = (long)a.chunks.wide_of(es, et);
         uint64_t cs = (es + chunk - 1) / chunk;
         bool side_t = rel >= cs;
         const PolyHdr &M = side_t ? T : S;  // the boundary integrated
@@ -410,7 +417,7 @@ __global__ void __launch_bounds__(256) k_area(const StoreView sv, AreaArgs a) {
                 dy = (double)Q.y - P.y;
                 SegWin w;
                 const bool has_w = (dx != 0 || dy != 0) && seg_window(O, P.x, P.y, Q.x, Q.y, w);
-                wide = has_w && (long)(w.ex - w.sx + 1) * (long)(w.ey - w.sy + 1) > a.wide_window;
+                wide = has_w && (long)(w.ex - w.sx + 1) * (long)(w.ey - w.sy + 1) > wide_window;
                 if (has_w && !wide) {
                     // an edge of O may be listed by several pixels: count it
                     // at its first listing only (tested before the FP64
@@ -578,7 +585,11 @@ __global__ void k_area_reduce(const uint64_t *__restrict__ item_start, const uin
 
 static Chunks chunks_of(const farm_store *s) {
     Chunks c;
-    for (int b = 0; b < 32; b++) c.c[b] = (uint16_t)(s->area_chunk[b] > 0 ? s->area_chunk[b] : 256);
+    const long env_w = wide_window_env();
+    for (int b = 0; b < 32; b++) {
+        c.c[b] = (uint16_t)(s->area_chunk[b] > 0 ? s->area_chunk[b] : kDefaultChunk);
+        c.w[b] = (uint16_t)(env_w ? env_w : (s->area_wide[b] > 0 ? s->area_wide[b] : kDefaultWide));
+    }
     return c;
 }
 
@@ -682,7 +693,6 @@ static int area_compute(farm_store *s, const AreaBufs &b, cudaStream_t st) {
                 b.ctr,
                 b.ctr + 1,
                 b.ctr + 3,
-                wide_window(),
                 spread_items()};
     k_area<<<sm_count() * 8, 256, 0, st>>>(s->view(), aa);
     FARM_CUDA(cudaGetLastError());
@@ -943,11 +953,30 @@ extern "C" int farm_area_set_chunks(farm_store *s, const int32_t *chunk_by_bucke
     return FARM_OK;
 }
 
+extern "C" int farm_area_set_wide(farm_store *s, const int32_t *wide_by_bucket) {
+    using namespace farm;
+    if (!s || !wide_by_bucket) {
+        set_error("invalid arguments to farm_area_set_wide");
+        return FARM_EINVAL;
+    }
+    for (int b = 0; b < 32; b++)
+        if (wide_by_bucket[b] < 0 || wide_by_bucket[b] > 65535) {
+            set_error("farm_area_set_wide: window sizes must lie in 1..65535 (0 = default)");
+            return FARM_EINVAL;
+        }
+    for (int b = 0; b < 32; b++) s->area_wide[b] = wide_by_bucket[b];
+    return FARM_OK;
+}
+
 // Autotuner: for every size bucket present in the sample (floor(log2) of a
-// pair's larger edge count), time the area pass on up to 2048 of its pairs
-// with each candidate chunk size and keep the fastest. The store keeps the
-// table (farm_area_set_chunks); it is also returned.
-extern "C" int farm_area_autotune(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, int32_t *table_out) {
+// pair's larger edge count), time the area pass on up to 2048 of its pairs,
+// first over the candidate chunk sizes 8..256 (edges per work item), then, at the
+// best chunk, over the candidate window thresholds (pixels above which an
+// edge is searched by the whole warp), and keep the fastest of each. One
+// untimed pass per bucket warms up. The store keeps both tables
+// (farm_area_set_chunks, farm_area_set_wide); they are also returned.
+extern "C" int farm_area_autotune(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, int32_t *chunk_out,
+                                  int32_t *wide_out) {
     using namespace farm;
     if (!s || (n && !pairs)) {
         set_error("invalid arguments to farm_area_autotune");
@@ -974,43 +1003,65 @@ extern "C" int farm_area_autotune(farm_store *s, const uint32_t *pairs, uint64_t
             set_error("farm_area_autotune: pair index out of range");
             return FARM_EINVAL;
         }
-        uint32_t m = std::max(edges(0, hp[2 * i]), edges(1, hp[2 * i + 1]));
-        int b = m ? 31 - __builtin_clz(m) : 0;
+        const int b = Chunks::bucket(edges(0, hp[2 * i]), edges(1, hp[2 * i + 1]));
         if (byb[b].size() < 2 * 2048) {
             byb[b].push_back(hp[2 * i]);
             byb[b].push_back(hp[2 * i + 1]);
         }
     }
-    static const int32_t kCand[] = {32, 64, 128, 256, 512, 1024, 2048};
-    int32_t saved[32];
-    memcpy(saved, s->area_chunk, sizeof saved);
-    int32_t best_tab[32];
-    memcpy(best_tab, s->area_chunk, sizeof best_tab);
+    static const int32_t kChunkCand[] = {8, 16, 32, 64, 128, 256};
+    static const int32_t kWideCand[] = {24, 48, 200, 800};
+    int32_t saved_c[32], saved_w[32];
+    memcpy(saved_c, s->area_chunk, sizeof saved_c);
+    memcpy(saved_w, s->area_wide, sizeof saved_w);
+    int32_t best_c[32], best_w[32];
+    memcpy(best_c, s->area_chunk, sizeof best_c);
+    memcpy(best_w, s->area_wide, sizeof best_w);
+    auto restore = [&]() {
+        memcpy(s->area_chunk, saved_c, sizeof saved_c);
+        memcpy(s->area_wide, saved_w, sizeof saved_w);
+    };
+    // one pass of bucket b's pairs with chunk c and window w everywhere
+    auto timed = [&](int b, int32_t c, int32_t w, double *ms) -> int {
+        for (int q = 0; q < 32; q++) {
+            s->area_chunk[q] = c;
+            s->area_wide[q] = w;
+        }
+        farm_stats stt;
+        const int rc = intersection_area(s, byb[b].data(), byb[b].size() / 2, FARM_MEM_HOST, nullptr, &stt);
+        *ms = stt.ms_total;
+        return rc;
+    };
     for (int b = 0; b < 32; b++) {
         if (byb[b].empty()) continue;
-        const uint64_t nb = byb[b].size() / 2;
-        double best_ms = 1e300;
-        int32_t best = 256;
-        for (int32_t c : kCand) {
-            for (int q = 0; q < 32; q++) s->area_chunk[q] = c;
-            double ms = 1e300;
-            for (int rep = 0; rep < 2; rep++) {  // the first run warms up
-                farm_stats stt;
-                int rc = intersection_area(s, byb[b].data(), nb, FARM_MEM_HOST, nullptr, &stt);
-                if (rc != FARM_OK) {
-                    memcpy(s->area_chunk, saved, sizeof saved);
-                    return rc;
-                }
-                if (rep) ms = stt.ms_total;
-            }
-            if (ms < best_ms) {
+        double ms = 0, best_ms = 1e300;
+        int rc = timed(b, kDefaultChunk, kDefaultWide, &ms);  // warm-up
+        int32_t bc = kDefaultChunk, bw = kDefaultWide;
+        for (int32_t c : kChunkCand) {
+            if (rc == FARM_OK) rc = timed(b, c, kDefaultWide, &ms);
+            if (rc == FARM_OK && ms < best_ms) {
                 best_ms = ms;
-                best = c;
+                bc = c;
             }
         }
-        best_tab[b] = best;
+        for (int32_t w : kWideCand) {
+            if (w == kDefaultWide) continue;  // timed above at bc
+            if (rc == FARM_OK) rc = timed(b, bc, w, &ms);
+            if (rc == FARM_OK && ms < best_ms) {
+                best_ms = ms;
+                bw = w;
+            }
+        }
+        if (rc != FARM_OK) {
+            restore();
+            return rc;
+        }
+        best_c[b] = bc;
+        best_w[b] = bw;
     }
-    memcpy(s->area_chunk, best_tab, sizeof best_tab);
-    if (table_out) memcpy(table_out, best_tab, sizeof best_tab);
+    memcpy(s->area_chunk, best_c, sizeof best_c);
+    memcpy(s->area_wide, best_w, sizeof best_w);
+    if (chunk_out) memcpy(chunk_out, best_c, sizeof best_c);
+    if (wide_out) memcpy(wide_out, best_w, sizeof best_w);
     return FARM_OK;
 }

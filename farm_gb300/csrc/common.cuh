@@ -252,6 +252,7 @@ struct farm_store {
     uint64_t raster_epoch = 0;     // bumped by every rasterization (plans check it)
     uint64_t orient_epoch = ~0ull;  // raster_epoch the cached orientations belong to
     uint64_t edgepix_epoch = ~0ull; // raster_epoch the area's edge -> pixel index belongs to
-    int32_t area_chunk[32] = {};   // edges per area item by size bucket (0: the default 256)
+    int32_t area_chunk[32] = {};   // edges per area item by size bucket (0: the default 16)
+    int32_t area_wide[32] = {};    // area: warp-shared windows above this many pixels, by bucket (0: 200)
     farm::StoreView view() const;
 };

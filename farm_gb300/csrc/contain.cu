@@ -135,9 +135,9 @@ __device__ bool edges_cross_box(const StoreView &sv, const PolyHdr &T, uint32_t 
 __global__ void __launch_bounds__(kContainWarps * 32)
     k_contain(const StoreView sv, const uint32_t *__restrict__ pairs, uint64_t n, uint64_t tgt_base,
               unsigned long long *__restrict__ next, uint8_t *__restrict__ out, ContainCounters *__restrict__ ctr) {
-    __shared__ float2 tbufs[kContainWarps][32];
+    __shared__ float4 tbufs[kContainWarps][32];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    float2 *tb = tbufs[wib];
+    float4 *tb = tbufs[wib];
     const int cc = sv.category_count;
     unsigned long long my_found = 0, my_pp = 0, my_tests = 0;
     for (;;) {

@@ -89,11 +89,11 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
                 IxCounters *__restrict__ ctr) {
     __shared__ uint2 queue[kWarpsPerBlock][kQueue];
     __shared__ float qkeys[kWarpsPerBlock][kQueue];
-    __shared__ float2 tbufs[kWarpsPerBlock][32];
+    __shared__ float4 tbufs[kWarpsPerBlock][32];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     uint2 *q = queue[wib];
     float *qk = qkeys[wib];
-    float2 *tb = tbufs[wib];
+    float4 *tb = tbufs[wib];
     const int cc = sv.category_count;
     unsigned long long my_found = 0, my_in = 0, my_bb = 0, my_tests = 0, my_ws = 0, my_wt = 0;
     for (;;) {

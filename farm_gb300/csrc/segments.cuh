@@ -101,11 +101,19 @@ __device__ __forceinline__ int warp_owner(uint32_t excl, uint32_t item) {
 //   c.cross(a, d) = -(c.cross(d, a)) exactly (the two products are the same
 //     IEEE products and round-to-nearest is symmetric), so the collinear test
 //     c.cross(a,d) == 0 && c.cross(b,d) == 0 reads the sign codes of
-//     c.cross(d, a) and c.cross(d, b) that the general test needs anyway.
+//     c.cross(d, a) and c.cross(d, b) that the general test needs anyway;
+//   for the target segment c -> d, c.cross(d, a) = (d-c) x (a-c) takes the
+//     differences a - c, which are the exact negations of the differences
+//     c - a the lane formed one vertex earlier for a.cross(b, c); the lane
+//     keeps c - a and c - b and evaluates (d-c) x (c-a), the same products
+//     and difference negated, so its sign code is the reference's negated;
+//   the target segment's own d - c is formed once, by the lane that stages d.
 // Collinear cases are rare; a target chunk that has one (in a valid lane) is
 // walked again with the interval test (inter1, geometry_computation.h:195-212).
+// tbuf holds 32 float4 per warp: the vertex and its difference from the
+// vertex before it.
 static __device__ bool refine_pixel_pair(const StoreView &sv, const PolyHdr &S, const PolyHdr &T, uint32_t pa,
-                                         uint32_t pb, float2 *tbuf, unsigned long long &tests) {
+                                         uint32_t pb, float4 *tbuf, unsigned long long &tests) {
     const int lane = threadIdx.x & 31;
     const uint32_t *so = sv.offset + S.off, *to = sv.offset + T.off;
     const uint32_t a0 = so[pa], a1 = so[pa + 1], b0 = to[pb], b1 = to[pb + 1];
@@ -130,7 +138,8 @@ static __device__ bool refine_pixel_pair(const StoreView &sv, const PolyHdr &S, 
             const float ex = __fsub_rn(b.x, a.x), ey = __fsub_rn(b.y, a.y);
             bool hit = false;
             int sxp = 0;  // sign of a.cross(b, previous target vertex)
-            float2 cp = make_float2(0.f, 0.f);
+            float uxp = 0.f, uyp = 0.f, wxp = 0.f, wyp = 0.f;  // previous target vertex - a, - b
+            float2 cp = make_float2(0.f, 0.f);  // previous target vertex (warp-uniform)
             bool pseg = false;  // previous target vertex starts a segment
             for (uint32_t tg = b0; tg < b1; tg += 32) {
                 const uint32_t kk = tg + lane;
@@ -148,36 +157,44 @@ static __device__ bool refine_pixel_pair(const StoreView &sv, const PolyHdr &S, 
                     float2 c = make_float2(0.f, 0.f);
                     if (v2) c = tr[o_start + off];
                     const unsigned segmask = __ballot_sync(0xffffffffu, v2 && off < o_len);
+                    // the vertex before c in the walk: lane - 1's, or the last of the previous chunk
+                    float px = __shfl_up_sync(0xffffffffu, c.x, 1), py = __shfl_up_sync(0xffffffffu, c.y, 1);
+                    if (lane == 0) {
+                        px = cp.x;
+                        py = cp.y;
+                    }
                     __syncwarp();
-                    tbuf[lane] = c;
+                    tbuf[lane] = make_float4(c.x, c.y, __fsub_rn(c.x, px), __fsub_rn(c.y, py));
                     __syncwarp();
                     const int m = (int)min(32u, total2 - tb);
                     const float2 cp0 = cp;
                     const bool pseg0 = pseg;
                     bool coll = false;
-                    uint32_t nseg = 0;
 #pragma unroll 4
                     for (int j = 0; j < m; j++) {
-                        const float2 cc = tbuf[j];
-                        const int sxn = sgn_code(cross_e(a, ex, ey, cc));
-                        if (pseg) {  // target segment cp -> cc
-                            const float dx = __fsub_rn(cc.x, cp.x), dy = __fsub_rn(cc.y, cp.y);
-                            const int sya = sgn_code(cross_e(cp, dx, dy, a));
-                            const int syb = sgn_code(cross_e(cp, dx, dy, b));
+                        const float4 t = tbuf[j];
+                        const float ux = __fsub_rn(t.x, a.x), uy = __fsub_rn(t.y, a.y);
+                        const int sxn = sgn_code(__fsub_rn(__fmul_rn(ex, uy), __fmul_rn(ey, ux)));
+                        if (pseg) {  // target segment cp -> t: (t - cp) x (cp - a), (t - cp) x (cp - b)
+                            const float pa_ = __fsub_rn(__fmul_rn(t.z, uyp), __fmul_rn(t.w, uxp));
+                            const float pb_ = __fsub_rn(__fmul_rn(t.z, wyp), __fmul_rn(t.w, wxp));
+                            const int sya = sgn_code(pa_), syb = sgn_code(pb_);
                             hit |= (sxp != sxn) & (sya != syb);
                             coll |= (sya | syb) == 0;
-                            nseg++;
                         }
+                        uxp = ux;
+                        uyp = uy;
+                        wxp = __fsub_rn(t.x, b.x);
+                        wyp = __fsub_rn(t.y, b.y);
                         sxp = sxn;
-                        cp = cc;
                         pseg = (segmask >> j) & 1u;
                     }
+                    cp = make_float2(tbuf[m - 1].x, tbuf[m - 1].y);
                     if (__any_sync(0xffffffffu, coll && valid)) {
                         float2 cq = cp0;
                         bool ps = pseg0;
                         for (int j = 0; j < m; j++) {
-                            const float2 cc = tbuf[j];
-                            const int sxn = sgn_code(cross_e(a, ex, ey, cc));
+                            const float2 cc = make_float2(tbuf[j].x, tbuf[j].y);
                             if (ps) {
                                 const float dx = __fsub_rn(cc.x, cq.x), dy = __fsub_rn(cc.y, cq.y);
                                 const int sya = sgn_code(cross_e(cq, dx, dy, a));
@@ -189,7 +206,9 @@ static __device__ bool refine_pixel_pair(const StoreView &sv, const PolyHdr &S, 
                             ps = (segmask >> j) & 1u;
                         }
                     }
-                    if (valid) tests += nseg;
+                    // segment tests of this chunk: one per target vertex whose predecessor starts a segment
+                    const unsigned low = m > 1 ? (segmask & ((1u << (m - 1)) - 1u)) : 0u;
+                    if (valid) tests += (pseg0 ? 1u : 0u) + (unsigned)__popc(low);
                     if (__any_sync(0xffffffffu, hit && valid)) return true;
                 }
             }

@@ -480,6 +480,32 @@ __global__ void k_cand_bounds(const WCand *__restrict__ c, uint64_t n, uint64_t 
     }
 }
 
+// Work order of the refinement: the pairs with the most candidates first
+// (longest-first scheduling, so that the pass does not end on a long pair
+// that started last). key[p] = ~(candidates of p) at p's last candidate;
+// pairs without candidates keep the all-ones key and come last. Results are
+// written by pair index, so the order is invisible.
+__global__ void k_within_cost(const WCand *__restrict__ c, uint64_t n, const uint64_t *__restrict__ first,
+                              uint32_t *__restrict__ key) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        if (k + 1 == n || c[k + 1].pair != c[k].pair) {
+            const uint64_t cnt = k + 1 - first[c[k].pair];
+            key[c[k].pair] = ~(uint32_t)(cnt < 0xFFFFFFFEull ? cnt : 0xFFFFFFFEull);
+        }
+    }
+}
+
+__global__ void k_iota32(uint32_t *__restrict__ v, uint64_t n) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
+        v[k] = (uint32_t)k;
+}
+
+// FARM_PAIR_ORDER=0 takes the pairs in index order
+static bool within_order_on() {
+    const char *v = getenv("FARM_PAIR_ORDER");
+    return !(v && *v == '0');
+}
+
 // suf[k] = the smallest lo of the pair's candidates after k (100000 after the
 // last), the bound Ideal.cpp:2615-2621 recomputes for every candidate; one
 // warp per refined pair scans its candidates backwards 32 at a time.
@@ -527,6 +553,7 @@ struct RefineArgs {
     uint8_t *out;
     unsigned long long *next;
     unsigned long long *stats;  // seq pairs, point-segment tests
+    const uint32_t *order;      // pairs taken in this order (most candidates first), or index order
 };
 
 // Ideal.cpp:2612-2643 in the candidates' order.
@@ -537,7 +564,10 @@ __global__ void __launch_bounds__(256) k_within_refine(const StoreView sv, Refin
     unsigned long long my_seq = 0, my_tests = 0, my_rechk = 0;
     for (;;) {
         unsigned long long pid = 0;
-        if (lane == 0) pid = atomicAdd(a.next, 1ull);
+        if (lane == 0) {
+            pid = atomicAdd(a.next, 1ull);
+            if (a.order && pid < a.n) pid = a.order[pid];
+        }
         pid = __shfl_sync(0xffffffffu, pid, 0);
         if (pid >= a.n) break;
         if (a.out[pid] != W_REFINE) continue;
@@ -770,6 +800,21 @@ static int within_round(farm_store *s, const uint32_t *dpairs, uint64_t n, uint8
         ra.out = dout;
         ra.next = ctr + 4;
         ra.stats = ctr + 5;
+        ra.order = nullptr;
+        if (within_order_on() && n > 1 && n < 0xFFFFFFFFull) {
+            FARM_TRY(s->s[Q_PAIR_ORDER].ensure(16 * n + 64));
+            uint32_t *key = s->s[Q_PAIR_ORDER].as<uint32_t>(), *key_s = key + n, *idx = key_s + n, *idx_s = idx + n;
+            FARM_CUDA(cudaMemsetAsync(key, 0xFF, 4 * n, st));
+            k_within_cost<<<gbw(nc), 256, 0, st>>>(cand.as<WCand>(), nc, first.as<uint64_t>(), key);
+            k_iota32<<<gbw(n), 256, 0, st>>>(idx, n);
+            launches += 2;
+            size_t ob = 0;
+            FARM_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, ob, key, key_s, idx, idx_s, (int64_t)n, 0, 32, st));
+            FARM_TRY(s->cub_tmp.ensure(ob + 64));
+            FARM_CUDA(cub::DeviceRadixSort::SortPairs(s->cub_tmp.p, ob, key, key_s, idx, idx_s, (int64_t)n, 0, 32,
+                                                      st));
+            ra.order = idx_s;
+        }
         k_within_refine<<<sm_count() * 8, 256, 0, st>>>(sv, ra);
         launches += 2;
         unsigned long long hs[3];

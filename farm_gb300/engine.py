@@ -225,12 +225,20 @@ class Store:
         check_gpu(self._lib.farm_area_plan_create(self._h, max_pairs, max_items, C.byref(h)))
         return AreaPlan(self, h)
 
-    def area_autotune(self, pairs) -> np.ndarray:
+    def area_autotune(self, pairs, with_wide: bool = False):
+        """Tune the area knobs per size bucket on a sample of pairs; returns the
+        chunk table, or (chunk table, window table) with with_wide."""
         pairs = np.ascontiguousarray(pairs, dtype=np.uint32)
         tab = np.zeros(32, np.int32)
+        wide = np.zeros(32, np.int32)
         check_gpu(self._lib.farm_area_autotune(self._h, C.c_void_p(pairs.ctypes.data), pairs.shape[0], MEM_HOST,
-                                               C.c_void_p(tab.ctypes.data)))
-        return tab
+                                               C.c_void_p(tab.ctypes.data), C.c_void_p(wide.ctypes.data)))
+        return (tab, wide) if with_wide else tab
+
+    def area_set_wide(self, table) -> None:
+        tab = np.ascontiguousarray(table, dtype=np.int32)
+        assert tab.size == 32
+        check_gpu(self._lib.farm_area_set_wide(self._h, C.c_void_p(tab.ctypes.data)))
 
     def area_set_chunks(self, table) -> None:
         tab = np.ascontiguousarray(table, dtype=np.int32)

@@ -219,19 +219,25 @@ int farm_tc_gemm_test(const void *A, const void *B, float *C, int M, int N, int 
  * up to max_pairs pairs in and replays the graph (results as
  * farm_intersection_area). max_items bounds the batch's work items: each pair
  * has ceil(edges_s / chunk) + ceil(edges_t / chunk) of them (chunk per size
- * bucket, 256 by default); a batch needing more fails with FARM_EOVERFLOW.
+ * bucket, 16 by default); a batch needing more fails with FARM_EOVERFLOW.
  * A plan is tied to the store's current rasterization. */
 typedef struct farm_area_plan farm_area_plan;
 int farm_area_plan_create(farm_store *s, uint64_t max_pairs, uint64_t max_items, farm_area_plan **out);
 int farm_area_plan_run(farm_area_plan *p, const uint32_t *pairs, uint64_t n, int mem, double *out, farm_stats *st);
 void farm_area_plan_destroy(farm_area_plan *p);
 /* Edges per area work item by size bucket b = floor(log2(larger edge count of
- * the pair)), 32 entries (0 = default 256). */
+ * the pair)), 32 entries (0 = default 16). */
 int farm_area_set_chunks(farm_store *s, const int32_t *chunk_by_bucket);
-/* Time each candidate chunk size (32 ... 2048) on up to 2048 pairs of every
- * bucket present in the sample, keep the fastest per bucket in the store and
- * return the table (32 entries). */
-int farm_area_autotune(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, int32_t *table_out);
+/* Candidate-window size (pixels of the other polygon's raster) above which an
+ * edge is searched by the whole warp rather than its own lane, by size
+ * bucket, 32 entries (0 = default 200). */
+int farm_area_set_wide(farm_store *s, const int32_t *wide_by_bucket);
+/* Per size bucket present in the sample (up to 2048 pairs each): time the
+ * chunk sizes 8..256, then at the best chunk the window sizes 24..800, keep
+ * the fastest of each in the store and return both tables (32 entries each;
+ * either output may be NULL). */
+int farm_area_autotune(farm_store *s, const uint32_t *pairs, uint64_t n, int mem, int32_t *chunk_out,
+                       int32_t *wide_out);
 
 /* ---- learned scorer (FARM_MODE_LEARNED): 520 -> 256 -> 256 -> 1 MLP, GELU,
  * bf16 weights/activations on tcgen05 tensor cores, fp32 accumulate. It takes
@@ -292,6 +298,7 @@ uint64_t farm_store_launches(farm_store *s);
  * (multiplies or adds per second), the denominators of the FP64- and
  * FP32-bound rooflines. No counterpart in the reference. */
 int farm_probe_issue_rates(double *fp64_ops_per_s, double *fp32_ops_per_s);
+
 /* Device bytes the store currently holds in its own allocations (rings,
  * rasters, query scratch), the learned scorer's state excluded. No
  * counterpart in the reference. */

@@ -128,9 +128,10 @@ def test_gpu_area_autotune(gpu_lib):
     st.load_sets(S, T)
     st.rasterize(vpr=10)
     base = st.intersection_area(pairs)
-    tab = st.area_autotune(pairs)
+    tab, wide = st.area_autotune(pairs, with_wide=True)
     assert tab.shape == (32,) and (tab > 0).any()
-    assert set(np.unique(tab[tab > 0])) <= {32, 64, 128, 256, 512, 1024, 2048}
+    assert set(np.unique(tab[tab > 0])) <= {8, 16, 32, 64, 128, 256}
+    assert set(np.unique(wide[tab > 0])) <= {24, 48, 200, 800}
     tuned = st.intersection_area(pairs)
     st.close()
     scale = np.maximum(base, 1e-300)
