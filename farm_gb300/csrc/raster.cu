@@ -1907,6 +1907,65 @@ __global__ void k_cell_bucket(const PolyHdr *__restrict__ hdr, Chunk ch, const u
     }
 }
 
+// Work order by an 8-bit cost key, sorted within tiles of kOrderTile items
+// (a counting sort in shared memory per block): perm[t0 + j] lists the tile's
+// items by ascending key. The order only schedules the work (every output
+// position comes from a scan), and what it is for is that the 32 lanes of a
+// warp carry similar trip counts, which a sort within the tile gives as well
+// as a global one, in one read of the keys and one write of the permutation.
+constexpr uint32_t kOrderTile = 4096;
+__global__ void __launch_bounds__(256) k_local_order(const uint8_t *__restrict__ key, uint64_t n,
+                                                     uint32_t *__restrict__ perm) {
+    __shared__ uint32_t cnt[256];
+    const int tid = threadIdx.x, lane = tid & 31;
+    const uint64_t t0 = (uint64_t)blockIdx.x * kOrderTile;
+    if (t0 >= n) return;
+    const uint32_t m = (uint32_t)min((uint64_t)kOrderTile, n - t0);
+    cnt[tid] = 0;
+    __syncthreads();
+    uint32_t kk[kOrderTile / 256];
+#pragma unroll
+    for (int j = 0; j < (int)(kOrderTile / 256); j++) {
+        const uint32_t i = (uint32_t)j * 256u + (uint32_t)tid;
+        kk[j] = i < m ? key[t0 + i] : 256u;  // 256: no item
+        const unsigned peers = __match_any_sync(0xffffffffu, kk[j]);
+        if (kk[j] < 256u && lane == __ffs(peers) - 1) atomicAdd(&cnt[kk[j]], (uint32_t)__popc(peers));
+    }
+    __syncthreads();
+    // exclusive scan of the 256 counts by the first warp (8 per lane)
+    if (tid < 32) {
+        uint32_t v[8], sum = 0;
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            v[q] = cnt[tid * 8 + q];
+            sum += v[q];
+        }
+        uint32_t incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += u;
+        }
+        uint32_t run = incl - sum;
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            cnt[tid * 8 + q] = run;
+            run += v[q];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < (int)(kOrderTile / 256); j++) {
+        const uint32_t i = (uint32_t)j * 256u + (uint32_t)tid;
+        const unsigned peers = __match_any_sync(0xffffffffu, kk[j]);
+        const int leader = __ffs(peers) - 1;
+        uint32_t b = 0;
+        if (kk[j] < 256u && lane == leader) b = atomicAdd(&cnt[kk[j]], (uint32_t)__popc(peers));
+        b = __shfl_sync(0xffffffffu, b, leader);
+        if (kk[j] < 256u) perm[t0 + b + (uint32_t)__popc(peers & ((1u << lane) - 1u))] = (uint32_t)(t0 + i);
+    }
+}
+
 __global__ void k_iota_u32(uint32_t *__restrict__ a, uint64_t n) {
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
         a[k] = (uint32_t)k;
@@ -2152,6 +2211,16 @@ struct RasterCtx {
     bool counts_kept = false;    // phase 1's per-edge counts are valid for phase 2
 };
 
+// perm = items [0, n) ordered by key within tiles (k_local_order)
+static int local_order(RasterCtx &R, const uint8_t *key, uint64_t n, uint32_t *perm) {
+    if (!n) return FARM_OK;
+    const uint64_t tiles = (n + kOrderTile - 1) / kOrderTile;
+    k_local_order<<<(unsigned)tiles, 256, 0, R.s->stream>>>(key, n, perm);
+    R.launches++;
+    FARM_CUDA(cudaGetLastError());
+    return FARM_OK;
+}
+
 // Edges [e0, e0 + ne) of polygons [p0, p0 + np) in walk order (k_edge_cost).
 static int edge_order(RasterCtx &R, uint32_t p0, uint32_t np, uint64_t e0, uint64_t ne, const uint32_t **perm,
                       int x_only = 0) {
@@ -2163,7 +2232,8 @@ static int edge_order(RasterCtx &R, uint32_t p0, uint32_t np, uint64_t e0, uint6
     uint32_t *idx = s->s[S_PERM].as<uint32_t>(), *idx_s = idx + ne;
     k_edge_cost<<<gb(ne), 256, 0, st>>>(s->view(), R.hdr, R.doff, p0, np, e0, ne, x_only, key, idx);
     R.launches++;
-    FARM_TRY(sort_pairs(s, key, key_s, idx, idx_s, ne, 8));
+    (void)key_s;
+    FARM_TRY(local_order(R, key, ne, idx_s));
     *perm = idx_s;
     return FARM_OK;
 }
@@ -2488,7 +2558,8 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
         uint32_t *idx = s->s[S_PERM].as<uint32_t>(), *idx_s = idx + nCP;
         k_cp_cost<<<gb(nCP), 256, 0, st>>>(R.hdr, cpstart, cpoly, cpcol, colpoly, nCP, key, idx);
         L++;
-        FARM_TRY(sort_pairs(s, key, key_s, idx, idx_s, nCP, 8));
+        (void)key_s;
+        FARM_TRY(local_order(R, key, nCP, idx_s));
         yperm = idx_s;
     }
 

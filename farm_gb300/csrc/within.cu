@@ -557,11 +557,41 @@ struct RefineArgs {
 };
 
 // Ideal.cpp:2612-2643 in the candidates' order.
+// exclusive warp scan of v; the warp's total in `total`
+__device__ __forceinline__ uint32_t warp_scan_excl(uint32_t v, int lane, uint32_t &total) {
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    total = __shfl_sync(0xffffffffu, incl, 31);
+    return incl - v;
+}
+
+// float <-> int keys whose signed order is the floats' order (no NaNs)
+__device__ __forceinline__ int ord_key(float v) {
+    const int i = __float_as_int(v);
+    return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float ord_val(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
+
+// Sequence pairs of one candidate pixel pair refined together (see below)
+// when there are at most this many.
+constexpr uint32_t kFlatSP = 64;
+
 __global__ void __launch_bounds__(256) k_within_refine(const StoreView sv, RefineArgs a) {
     const int lane = threadIdx.x & 31;
     const bool geo = a.geo != 0;
     const int cc = sv.category_count;
     unsigned long long my_seq = 0, my_tests = 0, my_rechk = 0;
+    __shared__ uint2 s_seq[8][2 * kFlatSP];
+    __shared__ uint32_t s_off[8][kFlatSP + 1];
+    __shared__ int s_lb[8][kFlatSP];
+    const int wib = threadIdx.x >> 5;
+    uint2 *sa = s_seq[wib], *sb = s_seq[wib] + kFlatSP;
+    uint32_t *off = s_off[wib];
+    int *lbk = s_lb[wib];
     for (;;) {
         unsigned long long pid = 0;
         if (lane == 0) {
@@ -594,6 +624,106 @@ __global__ void __launch_bounds__(256) k_within_refine(const StoreView sv, Refin
             if (show_status(sv.status[T.st + id2], cc) == 1) {
                 b0 = to[id2];
                 b1 = to[id2 + 1];
+            }
+            const uint32_t na = a1 - a0, nb = b1 - b0;
+            if (na * nb <= kFlatSP) {
+                // All sequence pairs of the pixel pair at once: the FP32
+                // lower bounds of every (point, segment) test of every
+                // sequence pair are spread over the lanes, with a minimum per
+                // sequence pair; then the reference's sequential rule is
+                // replayed on them in its order (source sequence outer,
+                // target inner), with the FP64 minimum of a sequence pair
+                // computed where its bound may lower the running minimum.
+                // The bounds are those of the loop below, so the decisions
+                // are the same.
+                const uint32_t nsp = na * nb;
+                for (uint32_t i = lane; i < na; i += 32) sa[i] = sseq[a0 + i];
+                for (uint32_t j = lane; j < nb; j += 32) sb[j] = tseq[b0 + j];
+                __syncwarp();
+                // tests of sequence pairs lane and lane + 32
+                auto sp_tests = [&](uint32_t sp) -> uint32_t {
+                    if (sp >= nsp) return 0u;
+                    const uint2 e1 = sa[sp / nb], e2 = sb[sp % nb];
+                    return (e1.y >= 2 && e2.y >= 2) ? e2.y * (e1.y - 1) + e1.y * (e2.y - 1) : 0u;
+                };
+                const uint32_t sz0 = sp_tests((uint32_t)lane), sz1 = sp_tests((uint32_t)lane + 32u);
+                uint32_t tot0, tot1;
+                const uint32_t ex0 = warp_scan_excl(sz0, lane, tot0);
+                const uint32_t ex1 = warp_scan_excl(sz1, lane, tot1);
+                const uint32_t total = tot0 + tot1;
+                if ((uint32_t)lane < nsp) {
+                    off[lane] = ex0;
+                    lbk[lane] = ord_key(3.4e38f);
+                }
+                if ((uint32_t)lane + 32u < nsp) {
+                    off[lane + 32] = tot0 + ex1;
+                    lbk[lane + 32] = ord_key(3.4e38f);
+                }
+                if (lane == 0) off[nsp] = total;
+                __syncwarp();
+                for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+                    const uint32_t t = t0 + lane;
+                    if (t < total) {
+                        uint32_t lo = 0, hi = nsp;  // the last sp with off[sp] <= t
+                        while (hi - lo > 1) {
+                            const uint32_t mid = (lo + hi) >> 1;
+                            if (off[mid] <= t) lo = mid; else hi = mid;
+                        }
+                        const uint32_t sp = lo, k2 = t - off[sp];
+                        const uint2 e1 = sa[sp / nb], e2 = sb[sp % nb];
+                        const uint32_t n1 = e2.y * (e1.y - 1);
+                        float d, er;
+                        if (k2 < n1) {
+                            const uint32_t pi = k2 / (e1.y - 1), si = k2 % (e1.y - 1);
+                            d = pt_seg_dist32(tr[e2.x + pi], sr[e1.x + si], sr[e1.x + si + 1], geo, er);
+                        } else {
+                            const uint32_t r = k2 - n1;
+                            const uint32_t pi = r / (e2.y - 1), si = r % (e2.y - 1);
+                            d = pt_seg_dist32(sr[e1.x + pi], tr[e2.x + si], tr[e2.x + si + 1], geo, er);
+                        }
+                        atomicMin(&lbk[sp], ord_key(d - er));
+                    }
+                }
+                __syncwarp();
+                for (uint32_t sp = 0; sp < nsp && decided < 0; sp++) {
+                    const uint32_t nsz = off[sp + 1] - off[sp];
+                    if (nsz == 0) continue;  // a sequence of fewer than 2 points
+                    const uint2 e1 = sa[sp / nb], e2 = sb[sp % nb];
+                    const uint32_t n1 = e2.y * (e1.y - 1), n2 = e1.y * (e2.y - 1);
+                    const float lb = ord_val(lbk[sp]);
+                    if (lane == 0) {
+                        my_seq++;
+                        my_tests += nsz;
+                    }
+                    if ((double)lb < min_dist) {
+                        double m = 1.7976931348623157e308;
+                        for (uint32_t k2 = lane; k2 < n1 + n2; k2 += 32) {
+                            double dd;
+                            if (k2 < n1) {
+                                uint32_t pi = k2 / (e1.y - 1), si = k2 % (e1.y - 1);
+                                dd = pt_seg_dist(tr[e2.x + pi], sr[e1.x + si], sr[e1.x + si + 1], geo);
+                            } else {
+                                uint32_t r = k2 - n1;
+                                uint32_t pi = r / (e2.y - 1), si = r % (e2.y - 1);
+                                dd = pt_seg_dist(sr[e1.x + pi], tr[e2.x + si], tr[e2.x + si + 1], geo);
+                            }
+                            m = m < dd ? m : dd;
+                        }
+                        for (int o = 16; o; o >>= 1) {
+                            double v = __shfl_xor_sync(0xffffffffu, m, o);
+                            m = m < v ? m : v;
+                        }
+                        if (lane == 0) my_rechk++;
+                        min_dist = min_dist < m ? min_dist : m;
+                    }
+                    if (min_dist < a.thr) {
+                        decided = 1;
+                    } else if (min_dist < ref) {
+                        decided = 0;
+                    }
+                }
+                __syncwarp();
+                continue;
             }
             for (uint32_t ia = a0; ia < a1 && decided < 0; ia++) {
                 uint2 e1 = sseq[ia];
