@@ -720,10 +720,12 @@ def area_eval(args) -> dict:
     # searched by the whole warp); the plan below is captured with its tables
     t_tune = time.time()
     tune_sel = np.sort(rng.permutation(len(pairs))[:max(1, (3 * len(pairs)) // 10)])
-    chunk_tab, wide_tab = st.area_autotune(pairs[tune_sel], with_wide=True)
+    tuned = {}
+    if args.area_tune:
+        chunk_tab, wide_tab = st.area_autotune(pairs[tune_sel], with_wide=True)
+        tuned = {str(b): [int(chunk_tab[b]), int(wide_tab[b])] for b in range(32) if chunk_tab[b] > 0}
     tune_s = time.time() - t_tune
-    tuned = {str(b): [int(chunk_tab[b]), int(wide_tab[b])] for b in range(32) if chunk_tab[b] > 0}
-    log(f"area autotune: {tune_s:.1f} s on {len(tune_sel)} pairs, bucket -> [chunk, window] {tuned}")
+    log(f"area autotune: {tune_s:.1f} s on {len(tune_sel)} pairs, bucket -> [chunk, window] {tuned or 'defaults'}")
     # items per pair at the smallest chunk the autotuner may pick (8 edges)
     plan = st.area_plan(max_pairs=len(pairs), max_items=int(((es + 7) // 8 + (et + 7) // 8).sum()) + 64)
     plan.run(pairs)
@@ -747,7 +749,7 @@ def area_eval(args) -> dict:
                        "edges_in_pairs": int(es.sum() + et.sum()), "largest_pair_edges": int((es + et).max()),
                        "pool_vertices": int(S.total + T.total), "seed": args.seed + 400},
             "nonzero_areas": int((out > 0).sum()), "rasterize_s": ras_s,
-            "autotune": {"sample_pairs": int(len(tune_sel)), "seconds": tune_s,
+            "autotune": {"ran": bool(args.area_tune), "sample_pairs": int(len(tune_sel)), "seconds": tune_s,
                          "bucket_to_chunk_window": tuned,
                          "note": "bucket = floor(log2(larger edge count)); chunk = edges per work item, "
                                  "window = candidate-window pixels above which the whole warp shares an edge"}}
@@ -1151,6 +1153,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--area-pairs", type=int, default=1000,
                     help="pairs of the configuration-4 area sample (0 = skip the area block)")
+    ap.add_argument("--no-area-tune", dest="area_tune", action="store_false",
+                    help="time the area block with the default knobs (skip the autotuner)")
     ap.add_argument("--within-strips", type=int, default=40,
                     help="configuration 3 is cut into this many strips and the middle one is timed (0 = skip)")
     ap.add_argument("--within-parity-pairs", type=int, default=1000)
