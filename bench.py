@@ -577,27 +577,47 @@ def run_ours(args) -> dict:
         ev.record(side)
         return ev
 
-    def step_e2e(sd, buf):
+    phase = {"load": 0.0, "join": 0.0, "raster": 0.0, "query": 0.0, "out": 0.0}
+
+    def step_e2e(sd, buf, timed=False):
         # rings in from pinned host memory, candidates by the GPU MBR join,
         # rasterize, filter + refine, and the pairs with their results out
+        # (host wall time per phase: each phase ends in a synchronisation of
+        # the store's stream, except the last, which is synchronised here)
+        t = [time.perf_counter()]
         ns, nt = sd["d_sx"].numel(), sd["d_tx"].numel()
         store.load(0, sd["so"], buf[:ns].numpy().reshape(-1, 2))
         store.load(1, sd["to"], buf[ns:ns + nt].numpy().reshape(-1, 2))
+        t.append(time.perf_counter())
         dp = store.mbr_join(device=dev, cap=nmax)
+        t.append(time.perf_counter())
         store.rasterize(vpr=args.vpr, category_count=16, strict=False)
+        t.append(time.perf_counter())
         n = dp.shape[0]
         _, found = store.intersect(dp, out=d_e2e_out[:n])
+        t.append(time.perf_counter())
         hout[:n].copy_(d_e2e_out[:n], non_blocking=True)
         hpairs_out[:n].copy_(dp, non_blocking=True)
         torch.cuda.current_stream().synchronize()
+        t.append(time.perf_counter())
+        if timed:
+            for k, name in enumerate(("load", "join", "raster", "query", "out")):
+                phase[name] += (t[k + 1] - t[k]) * 1000.0
         return found, n
 
-    refill(hbuf[0], order[0]).synchronize()
-    _, n0 = step_e2e(order[0], hbuf[0])  # warm-up of the host path
-    # the GPU join's candidates are the host join's, in its order
-    if n0 != len(order[0]["pairs"]) or not np.array_equal(hpairs_out[:n0].numpy().view(np.uint32),
-                                                          order[0]["pairs"]):
-        raise SystemExit("the GPU MBR join differs from the host join")
+    # warm-up of the host path on every strip the timed steps use (the store's
+    # staging buffers reach their size before timing, as the device steps'
+    # warm-up does for the rasterizer's)
+    seen = set()
+    for sd in order:
+        if sd["strip"] in seen:
+            continue
+        seen.add(sd["strip"])
+        refill(hbuf[0], sd).synchronize()
+        _, n0 = step_e2e(sd, hbuf[0])
+        # the GPU join's candidates are the host join's, in its order
+        if n0 != len(sd["pairs"]) or not np.array_equal(hpairs_out[:n0].numpy().view(np.uint32), sd["pairs"]):
+            raise SystemExit("the GPU MBR join differs from the host join")
     refill(hbuf[0], order[0]).synchronize()
     torch.cuda.synchronize()
     if world > 1:
@@ -606,7 +626,7 @@ def run_ours(args) -> dict:
     t_e2e0 = time.perf_counter()
     for i, sd in enumerate(order):
         ev = refill(hbuf[(i + 1) % 2], order[(i + 1) % len(order)]) if i + 1 < len(order) else None
-        step_e2e(sd, hbuf[i % 2])
+        step_e2e(sd, hbuf[i % 2], timed=True)
         if ev is not None:
             ev.synchronize()
     store.event_record(3)
@@ -631,9 +651,10 @@ def run_ours(args) -> dict:
         "found_in_timed_steps": int(sum(sd.get("found", 0) for sd in order)),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "note": "per step: rings H2D from pinned host memory, the candidate pairs by the GPU MBR join (the "
-                        "host join's set and order, checked once), rasterization, filter + refine, and the pairs "
+                        "host join's set and order, checked once per strip in the warm-up), rasterization, filter + refine, and the pairs "
                         "with their result bytes D2H; the next step's pinned rings are refilled from HBM during "
-                        "the step (inside the timed region)"},
+                        "the step (inside the timed region)",
+                "phase_wall_ms_per_step": {k: v / len(order) for k, v in phase.items()}},
         "gpu_launches": int(launches),
         "clocks": clk,
         "stage_ms": {"load": stage["load_ms"] / args.steps, "raster": stage["raster_ms"] / args.steps,

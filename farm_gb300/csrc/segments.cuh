@@ -108,8 +108,13 @@ __device__ __forceinline__ int warp_owner(uint32_t excl, uint32_t item) {
 //     keeps c - a and c - b and evaluates (d-c) x (c-a), the same products
 //     and difference negated, so its sign code is the reference's negated;
 //   the target segment's own d - c is formed once, by the lane that stages d.
-// Collinear cases are rare; a target chunk that has one (in a valid lane) is
-// walked again with the interval test (inter1, geometry_computation.h:195-212).
+// A group of R < 32 source segments (a pixel's last group, or a small pixel)
+// would leave lanes idle for the whole target walk, so the group is repeated
+// across G = floor(32 / R) slices of lanes and each slice walks its share of
+// every staged chunk of target vertices, starting from the vertex before its
+// share. Every (source segment, target segment) pair is still tested once.
+// Collinear cases are rare; a chunk that has one (in a valid lane) is walked
+// again with the interval test (inter1, geometry_computation.h:195-212).
 // tbuf holds 32 float4 per warp: the vertex and its difference from the
 // vertex before it.
 static __device__ bool refine_pixel_pair(const StoreView &sv, const PolyHdr &S, const PolyHdr &T, uint32_t pa,
@@ -125,8 +130,12 @@ static __device__ bool refine_pixel_pair(const StoreView &sv, const PolyHdr &S, 
         uint32_t total;
         const uint32_t excl = warp_excl_scan(r.y, lane, total);  // r.y segments per sequence
         for (uint32_t sb = 0; sb < total; sb += 32) {
-            const uint32_t f = sb + lane;
-            const bool valid = f < total;
+            // this group's R source segments, repeated over G slices of lanes
+            const uint32_t R = min(32u, total - sb);
+            const uint32_t G = 32u / R;
+            const uint32_t slice = (uint32_t)lane / R;
+            const uint32_t f = sb + (uint32_t)lane % R;
+            const bool valid = slice < G;
             const int owner = warp_owner(excl, f);
             const uint32_t ostart = __shfl_sync(0xffffffffu, r.x, owner);
             const uint32_t oex = __shfl_sync(0xffffffffu, excl, owner);
@@ -137,10 +146,8 @@ static __device__ bool refine_pixel_pair(const StoreView &sv, const PolyHdr &S, 
             }
             const float ex = __fsub_rn(b.x, a.x), ey = __fsub_rn(b.y, a.y);
             bool hit = false;
-            int sxp = 0;  // sign of a.cross(b, previous target vertex)
-            float uxp = 0.f, uyp = 0.f, wxp = 0.f, wyp = 0.f;  // previous target vertex - a, - b
-            float2 cp = make_float2(0.f, 0.f);  // previous target vertex (warp-uniform)
-            bool pseg = false;  // previous target vertex starts a segment
+            float2 cp = make_float2(0.f, 0.f);  // last vertex of the previous chunk (warp-uniform)
+            bool pseg = false;                  // it starts a segment
             for (uint32_t tg = b0; tg < b1; tg += 32) {
                 const uint32_t kk = tg + lane;
                 const uint2 r2 = kk < b1 ? tseq[kk] : make_uint2(0u, 0u);
@@ -166,16 +173,29 @@ static __device__ bool refine_pixel_pair(const StoreView &sv, const PolyHdr &S, 
                     __syncwarp();
                     tbuf[lane] = make_float4(c.x, c.y, __fsub_rn(c.x, px), __fsub_rn(c.y, py));
                     __syncwarp();
-                    const int m = (int)min(32u, total2 - tb);
-                    const float2 cp0 = cp;
-                    const bool pseg0 = pseg;
+                    const uint32_t m = min(32u, total2 - tb);
+                    // this slice's share [j0, j1) of the chunk, and the vertex before it
+                    const uint32_t q = (m + G - 1) / G;
+                    const uint32_t j0 = valid ? min(m, slice * q) : m, j1 = min(m, j0 + q);
+                    float2 pv = cp;
+                    bool ps = pseg;
+                    if (j0 > 0) {
+                        const float4 t = tbuf[j0 - 1];
+                        pv = make_float2(t.x, t.y);
+                        ps = (segmask >> (j0 - 1)) & 1u;
+                    }
+                    float uxp = __fsub_rn(pv.x, a.x), uyp = __fsub_rn(pv.y, a.y);
+                    float wxp = __fsub_rn(pv.x, b.x), wyp = __fsub_rn(pv.y, b.y);
+                    int sxp = sgn_code(__fsub_rn(__fmul_rn(ex, uyp), __fmul_rn(ey, uxp)));
+                    const float2 pv0 = pv;
+                    const bool ps0 = ps;
                     bool coll = false;
 #pragma unroll 4
-                    for (int j = 0; j < m; j++) {
+                    for (uint32_t j = j0; j < j1; j++) {
                         const float4 t = tbuf[j];
                         const float ux = __fsub_rn(t.x, a.x), uy = __fsub_rn(t.y, a.y);
                         const int sxn = sgn_code(__fsub_rn(__fmul_rn(ex, uy), __fmul_rn(ey, ux)));
-                        if (pseg) {  // target segment cp -> t: (t - cp) x (cp - a), (t - cp) x (cp - b)
+                        if (ps) {  // target segment pv -> t: (t - pv) x (pv - a), (t - pv) x (pv - b)
                             const float pa_ = __fsub_rn(__fmul_rn(t.z, uyp), __fmul_rn(t.w, uxp));
                             const float pb_ = __fsub_rn(__fmul_rn(t.z, wyp), __fmul_rn(t.w, wxp));
                             const int sya = sgn_code(pa_), syb = sgn_code(pb_);
@@ -187,15 +207,14 @@ static __device__ bool refine_pixel_pair(const StoreView &sv, const PolyHdr &S, 
                         wxp = __fsub_rn(t.x, b.x);
                         wyp = __fsub_rn(t.y, b.y);
                         sxp = sxn;
-                        pseg = (segmask >> j) & 1u;
+                        ps = (segmask >> j) & 1u;
                     }
-                    cp = make_float2(tbuf[m - 1].x, tbuf[m - 1].y);
                     if (__any_sync(0xffffffffu, coll && valid)) {
-                        float2 cq = cp0;
-                        bool ps = pseg0;
-                        for (int j = 0; j < m; j++) {
+                        float2 cq = pv0;
+                        bool pq = ps0;
+                        for (uint32_t j = j0; j < j1; j++) {
                             const float2 cc = make_float2(tbuf[j].x, tbuf[j].y);
-                            if (ps) {
+                            if (pq) {
                                 const float dx = __fsub_rn(cc.x, cq.x), dy = __fsub_rn(cc.y, cq.y);
                                 const int sya = sgn_code(cross_e(cq, dx, dy, a));
                                 const int syb = sgn_code(cross_e(cq, dx, dy, b));
@@ -203,12 +222,17 @@ static __device__ bool refine_pixel_pair(const StoreView &sv, const PolyHdr &S, 
                                     hit |= inter1f(a.x, b.x, cq.x, cc.x) && inter1f(a.y, b.y, cq.y, cc.y);
                             }
                             cq = cc;
-                            ps = (segmask >> j) & 1u;
+                            pq = (segmask >> j) & 1u;
                         }
                     }
-                    // segment tests of this chunk: one per target vertex whose predecessor starts a segment
-                    const unsigned low = m > 1 ? (segmask & ((1u << (m - 1)) - 1u)) : 0u;
-                    if (valid) tests += (pseg0 ? 1u : 0u) + (unsigned)__popc(low);
+                    // segment tests of this slice: one per vertex of [j0, j1) whose predecessor starts a segment
+                    if (valid && j1 > j0) {
+                        const unsigned below = j1 - 1 > 31u ? 0xffffffffu : ((1u << (j1 - 1)) - 1u);
+                        const unsigned from = j0 > 0 ? ~((1u << (j0 - 1)) - 1u) : 0xffffffffu;
+                        tests += (j0 == 0 && pseg ? 1u : 0u) + (unsigned)__popc(segmask & below & from);
+                    }
+                    cp = make_float2(tbuf[m - 1].x, tbuf[m - 1].y);
+                    pseg = (segmask >> (m - 1)) & 1u;
                     if (__any_sync(0xffffffffu, hit && valid)) return true;
                 }
             }
