@@ -556,12 +556,22 @@ def run_ours(args) -> dict:
     t_dev = ms / 1000.0
     pairs_timed = sum(len(sd["pairs"]) for sd in order)
 
-    # end to end through the C ABI with host buffers: the step's rings come
-    # from pinned host memory (two buffers; the next step's is refilled from
-    # HBM during the current step, inside the timed region) and the result
-    # bytes go back to pinned host memory
-    cap = max(sd["xy_bytes"] for sd in strips) // 4
-    hbuf = [torch.empty(cap, dtype=torch.float32).pin_memory() for _ in range(2)]
+    # end to end through the C ABI with host buffers: each step's rings come
+    # from pinned host memory, where they are placed before timing (one buffer
+    # per distinct strip when a quarter of host memory holds them, else two
+    # buffers, the next step's refilled from HBM during the current step), and
+    # the result bytes go back to pinned host memory
+    distinct = []
+    for sd in order:
+        if all(sd is not x for x in distinct):
+            distinct.append(sd)
+    host_bytes = os.sysconf("SC_PHYS_PAGES") * os.sysconf("SC_PAGE_SIZE")
+    resident = sum(sd["xy_bytes"] for sd in distinct) <= host_bytes // 4
+    nbuf = len(distinct) if resident else 2
+    # a source and a target buffer each (each allocation starts aligned, which
+    # the copy engines need for full speed)
+    caps = max(sd["d_sx"].numel() for sd in strips), max(sd["d_tx"].numel() for sd in strips)
+    hbuf = [tuple(torch.empty(c, dtype=torch.float32).pin_memory() for c in caps) for _ in range(nbuf)]
     nmax = max(len(sd["pairs"]) for sd in strips)
     hout = torch.empty(nmax, dtype=torch.uint8).pin_memory()
     hpairs_out = torch.empty((nmax, 2), dtype=torch.int32).pin_memory()
@@ -569,10 +579,10 @@ def run_ours(args) -> dict:
     side = torch.cuda.Stream(dev)
 
     def refill(buf, sd):
-        ns = sd["d_sx"].numel()
+        ns, nt = sd["d_sx"].numel(), sd["d_tx"].numel()
         with torch.cuda.stream(side):
-            buf[:ns].copy_(sd["d_sx"].view(-1), non_blocking=True)
-            buf[ns:ns + sd["d_tx"].numel()].copy_(sd["d_tx"].view(-1), non_blocking=True)
+            buf[0][:ns].copy_(sd["d_sx"].view(-1), non_blocking=True)
+            buf[1][:nt].copy_(sd["d_tx"].view(-1), non_blocking=True)
         ev = torch.cuda.Event()
         ev.record(side)
         return ev
@@ -586,8 +596,8 @@ def run_ours(args) -> dict:
         # the store's stream, except the last, which is synchronised here)
         t = [time.perf_counter()]
         ns, nt = sd["d_sx"].numel(), sd["d_tx"].numel()
-        store.load(0, sd["so"], buf[:ns].numpy().reshape(-1, 2))
-        store.load(1, sd["to"], buf[ns:ns + nt].numpy().reshape(-1, 2))
+        store.load(0, sd["so"], buf[0][:ns].numpy().reshape(-1, 2))
+        store.load(1, sd["to"], buf[1][:nt].numpy().reshape(-1, 2))
         t.append(time.perf_counter())
         dp = store.mbr_join(device=dev, cap=nmax)
         t.append(time.perf_counter())
@@ -605,28 +615,31 @@ def run_ours(args) -> dict:
                 phase[name] += (t[k + 1] - t[k]) * 1000.0
         return found, n
 
+    def buf_of(i, sd):
+        return hbuf[next(k for k, x in enumerate(distinct) if x is sd)] if resident else hbuf[i % 2]
+
     # warm-up of the host path on every strip the timed steps use (the store's
     # staging buffers reach their size before timing, as the device steps'
     # warm-up does for the rasterizer's)
-    seen = set()
-    for sd in order:
-        if sd["strip"] in seen:
-            continue
-        seen.add(sd["strip"])
-        refill(hbuf[0], sd).synchronize()
-        _, n0 = step_e2e(sd, hbuf[0])
+    for k, sd in enumerate(distinct):
+        b = hbuf[k] if resident else hbuf[0]
+        refill(b, sd).synchronize()
+        _, n0 = step_e2e(sd, b)
         # the GPU join's candidates are the host join's, in its order
         if n0 != len(sd["pairs"]) or not np.array_equal(hpairs_out[:n0].numpy().view(np.uint32), sd["pairs"]):
             raise SystemExit("the GPU MBR join differs from the host join")
-    refill(hbuf[0], order[0]).synchronize()
+    if not resident:
+        refill(hbuf[0], order[0]).synchronize()
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
     store.event_record(2)
     t_e2e0 = time.perf_counter()
     for i, sd in enumerate(order):
-        ev = refill(hbuf[(i + 1) % 2], order[(i + 1) % len(order)]) if i + 1 < len(order) else None
-        step_e2e(sd, hbuf[i % 2], timed=True)
+        ev = None
+        if not resident and i + 1 < len(order):
+            ev = refill(hbuf[(i + 1) % 2], order[i + 1])
+        step_e2e(sd, buf_of(i, sd), timed=True)
         if ev is not None:
             ev.synchronize()
     store.event_record(3)
@@ -652,8 +665,10 @@ def run_ours(args) -> dict:
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "note": "per step: rings H2D from pinned host memory, the candidate pairs by the GPU MBR join (the "
                         "host join's set and order, checked once per strip in the warm-up), rasterization, filter + refine, and the pairs "
-                        "with their result bytes D2H; the next step's pinned rings are refilled from HBM during "
-                        "the step (inside the timed region)",
+                        "with their result bytes D2H; the rings are placed in pinned host memory before timing "
+                        "(one buffer per strip), or, when they do not fit a quarter of host memory, the next "
+                        "step's buffer is refilled from HBM during the step (inside the timed region)",
+                "host_buffers": "per strip" if resident else "two, refilled",
                 "phase_wall_ms_per_step": {k: v / len(order) for k, v in phase.items()}},
         "gpu_launches": int(launches),
         "clocks": clk,
@@ -850,7 +865,9 @@ def within_eval(args) -> dict:
            "found": int((gpu == 1).sum()), "sequence_pairs": stats.get("sequence_pairs"),
            "fp64_rechecks": stats.get("fp64_rechecks"),
            "fp64_recheck_frac": (stats.get("fp64_rechecks", 0) / stats["sequence_pairs"])
-           if stats.get("sequence_pairs") else None}
+           if stats.get("sequence_pairs") else None,
+           "stage_ms": {"descent": stats.get("ms_stage", [0, 0, 0, 0])[1],
+                        "order_and_refine": stats.get("ms_stage", [0, 0, 0, 0])[2]}}
     if not args.no_cpu_baseline:
         res["cpu_baseline"] = within_cpu(U, pairs, gpu, args)
     return res

@@ -888,11 +888,28 @@ static int within_round(farm_store *s, const uint32_t *dpairs, uint64_t n, uint8
     wa.out = dout;
     wa.next = ctr + 0;
     wa.stats = ctr + 2;
+    // device time of the descent and of the ordered refinement (events on the
+    // store's stream, read after the synchronisations below)
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    for (auto &e : ev) cudaEventCreate(&e);
+    struct EvFree {
+        cudaEvent_t *e;
+        ~EvFree() {
+            for (int k = 0; k < 3; k++)
+                if (e[k]) cudaEventDestroy(e[k]);
+        }
+    } ev_free{ev};
+    if (ev[0]) cudaEventRecord(ev[0], st);
     k_within_descend<<<nwarps / 8, 256, 0, st>>>(sv, wa);
     launches++;
+    if (ev[1]) cudaEventRecord(ev[1], st);
     unsigned long long hc[4];
     FARM_CUDA(cudaMemcpyAsync(hc, ctr, 32, cudaMemcpyDeviceToHost, st));
     FARM_CUDA(cudaStreamSynchronize(st));
+    {
+        float ms = 0;
+        if (ev[0] && ev[1] && cudaEventElapsedTime(&ms, ev[0], ev[1]) == cudaSuccess) acc->ms_stage[1] += ms;
+    }
     uint64_t nc = hc[1] < cand_cap ? hc[1] : cand_cap;
     acc->border_pairs += hc[3];
     acc->in_hits += hc[2];  // candidate pixel pairs
@@ -947,9 +964,14 @@ static int within_round(farm_store *s, const uint32_t *dpairs, uint64_t n, uint8
         }
         k_within_refine<<<sm_count() * 8, 256, 0, st>>>(sv, ra);
         launches += 2;
+        if (ev[2]) cudaEventRecord(ev[2], st);
         unsigned long long hs[3];
         FARM_CUDA(cudaMemcpyAsync(hs, ctr + 5, 24, cudaMemcpyDeviceToHost, st));
         FARM_CUDA(cudaStreamSynchronize(st));
+        {
+            float ms = 0;
+            if (ev[1] && ev[2] && cudaEventElapsedTime(&ms, ev[1], ev[2]) == cudaSuccess) acc->ms_stage[2] += ms;
+        }
         acc->sequence_pairs += hs[0];
         acc->segment_tests += hs[1];
         acc->fp64_rechecks += hs[2];
@@ -1068,7 +1090,8 @@ int within(farm_store *s, const uint32_t *pairs, uint64_t n, double distance, in
         float ms = 0;
         cudaEventElapsedTime(&ms, s->ev[6], s->ev[7]);
         st->ms_total = ms;
-        st->ms_stage[1] = ms;
+        st->ms_stage[1] = acc.ms_stage[1];  // the hierarchical descent (filter)
+        st->ms_stage[2] = acc.ms_stage[2];  // candidate order and the ordered refinement
         st->kernel_launches = launches;
     }
     return FARM_OK;
