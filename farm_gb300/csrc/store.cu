@@ -341,10 +341,24 @@ int farm_store_load(farm_store *s, int side, uint64_t n, const uint64_t *off, co
     if (mem == FARM_MEM_DEVICE) {
         src = reinterpret_cast<const float2 *>(xy) + o0;
     } else {
-        FARM_TRY(s->d_xy_in.ensure(side_total * sizeof(float2) + 16));
-        FARM_CUDA(cudaMemcpyAsync(s->d_xy_in.p, xy + 2 * o0, side_total * sizeof(float2), cudaMemcpyHostToDevice,
-                                  s->stream));
-        src = s->d_xy_in.as<float2>();
+        // Pinned host memory is read by the padding kernel itself over the
+        // host link (the device address the runtime reports for it), with no
+        // staging copy; pageable memory is copied into a staging buffer first.
+        cudaPointerAttributes pa;
+        const void *mapped = nullptr;
+        if (cudaPointerGetAttributes(&pa, xy + 2 * o0) == cudaSuccess) {
+            if (pa.type == cudaMemoryTypeHost && pa.devicePointer) mapped = pa.devicePointer;
+        } else {
+            cudaGetLastError();
+        }
+        if (mapped) {
+            src = reinterpret_cast<const float2 *>(mapped);
+        } else {
+            FARM_TRY(s->d_xy_in.ensure(side_total * sizeof(float2) + 16));
+            FARM_CUDA(cudaMemcpyAsync(s->d_xy_in.p, xy + 2 * o0, side_total * sizeof(float2),
+                                      cudaMemcpyHostToDevice, s->stream));
+            src = s->d_xy_in.as<float2>();
+        }
     }
     const uint64_t first_poly = side == 0 ? 0 : s->n_side[0];
     if (n) {
