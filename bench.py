@@ -1209,7 +1209,7 @@ def main():
     ap.add_argument("--learned-epochs", type=int, default=12)
     ap.add_argument("--learned-band", choices=["cost", "plain"], default="cost",
                     help="cost-aware band (spend the error budget on expensive pairs) or a plain probability band")
-    ap.add_argument("--learned-budget", type=float, default=5e-4,
+    ap.add_argument("--learned-budget", type=float, default=1e-3,
                     help="false positives (negatives) allowed above (below) the band, per positive")
     args = ap.parse_args()
     res = run_reference(args) if args.impl == "reference" else run_ours(args)
