@@ -188,8 +188,8 @@ FP32_NOMINAL = 128 * 152 * 2.07e9
 # profiles/dram_traffic_small_strip.md. A step's traffic is the per-unit
 # figure times the step's units.
 TRAFFIC_PER_UNIT = {
-    "edge_walk": 523.1,   # bytes per edge (k_walk_tot + k_walk_fill): 112.0 GB / 2.14e8 edges
-    "refine": 6640.6,     # bytes per candidate pair (k_intersect): 174.8 MB / 26,320 pairs
+    "edge_walk": 199.0,   # bytes per edge (k_walk_tot + k_walk_fill): 42.6 GB / 2.14e8 edges
+    "refine": 6621.8,     # bytes per candidate pair (k_intersect): 174.3 MB / 26,320 pairs
 }
 
 

@@ -114,6 +114,26 @@ __device__ double box_distance(const Box &a, const Box &t, bool geo) {
 // round-to-nearest, so the largest distance is the one built from the
 // largest |dx| and the largest |dy|: the same double, with 2 divisions and
 // one sqrt instead of 32 and 16.
+__device__ __forceinline__ float4 box_corners_f(const Box &a) {
+    return make_float4((float)a.lo0, (float)a.lo1, (float)a.hi0, (float)a.hi1);
+}
+
+// the same from the boxes' float corners (box_corners_f) and a's lo1
+__device__ double box_max_distance_f(const float4 &fa, const float4 &ft, double a_lo1, bool geo) {
+    const float ax0 = fa.x, ax1 = fa.z, ay0 = fa.y, ay1 = fa.w;
+    const float tx0 = ft.x, tx1 = ft.z, ty0 = ft.y, ty1 = ft.w;
+    const float mx = fmaxf(fmaxf(fabsf(__fsub_rn(ax0, tx0)), fabsf(__fsub_rn(ax0, tx1))),
+                           fmaxf(fabsf(__fsub_rn(ax1, tx0)), fabsf(__fsub_rn(ax1, tx1))));
+    const float my = fmaxf(fmaxf(fabsf(__fsub_rn(ay0, ty0)), fabsf(__fsub_rn(ay0, ty1))),
+                           fmaxf(fabsf(__fsub_rn(ay1, ty0)), fabsf(__fsub_rn(ay1, ty1))));
+    double dx = mx, dy = my;
+    if (geo) {
+        dy = dy / DEG_LAT;
+        dx = dx / deg_lon(a_lo1);
+    }
+    return sqrt(dx * dx + dy * dy);
+}
+
 __device__ double box_max_distance(const Box &a, const Box &t, bool geo) {
     const float ax0 = (float)a.lo0, ax1 = (float)a.hi0, ay0 = (float)a.lo1, ay1 = (float)a.hi1;
     const float tx0 = (float)t.lo0, tx1 = (float)t.hi0, ty0 = (float)t.lo1, ty1 = (float)t.hi1;
@@ -248,7 +268,16 @@ struct SideScratch {
     uint32_t *bits;  // cap_pix/32 + 1 words
     uint32_t *q;     // current queued set
     uint32_t *p;     // next level set
+    Box *box;        // the boxes of the pixels in p, and their corners as floats
+    float4 *fbox;    // (lo0, lo1, hi0, hi1)
 };
+
+// u32 words of one warp's scratch: per side the boxes (8 words each) and
+// float corners (4) of up to cap pixels, then per side a bitmap and two lists
+__host__ __device__ inline uint64_t within_scratch_words(uint32_t cap) {
+    const uint64_t w = 24ull * cap + 2 * (((uint64_t)cap >> 5) + 1 + 2ull * cap);
+    return (w + 3) & ~3ull;
+}
 
 // set bit, return whether newly set
 __device__ __forceinline__ void set_bit(uint32_t *bits, uint32_t id) { atomicOr(&bits[id >> 5], 1u << (id & 31)); }
@@ -319,10 +348,14 @@ __global__ void __launch_bounds__(256) k_within_descend(const StoreView sv, With
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int cc = sv.category_count;
     const bool geo = a.geo != 0;
-    uint32_t *base = a.scratch + warp * a.scratch_words;
-    const uint32_t bw = (a.cap_pix >> 5) + 1;
-    SideScratch ss{base, base + bw, base + bw + a.cap_pix};
-    SideScratch ts{base + bw + 2 * a.cap_pix, base + 2 * bw + 2 * a.cap_pix, base + 2 * bw + 3 * a.cap_pix};
+    uint32_t *wbase = a.scratch + warp * a.scratch_words;
+    const uint32_t cap = a.cap_pix;
+    Box *boxes = reinterpret_cast<Box *>(wbase);
+    float4 *fboxes = reinterpret_cast<float4 *>(wbase + 16ull * cap);
+    uint32_t *base = wbase + 24ull * cap;
+    const uint32_t bw = (cap >> 5) + 1;
+    SideScratch ss{base, base + bw, base + bw + cap, boxes, fboxes};
+    SideScratch ts{base + bw + 2 * cap, base + 2 * bw + 2 * cap, base + 2 * bw + 3 * cap, boxes + cap, fboxes + cap};
     unsigned long long my_cand = 0, my_box = 0;
     for (;;) {
         unsigned long long pid = 0;
@@ -374,14 +407,26 @@ __global__ void __launch_bounds__(256) k_within_descend(const StoreView sv, With
             uint32_t np_t = next_set(T, sv.status, t_next, j, ts.q, nqt, ts, lane, cc);
             layer_geom(S, i, gs);
             layer_geom(T, j, gt);
+            // each pixel's box and float corners once per level, for all the
+            // box pairs it is in (the same values as computed per pair)
+            for (uint32_t k = lane; k < np_s; k += 32) {
+                const Box b = pixel_box(gs, (int)ss.p[k]);
+                ss.box[k] = b;
+                ss.fbox[k] = box_corners_f(b);
+            }
+            for (uint32_t k = lane; k < np_t; k += 32) {
+                const Box b = pixel_box(gt, (int)ts.p[k]);
+                ts.box[k] = b;
+                ts.fbox[k] = box_corners_f(b);
+            }
+            __syncwarp();
             // smallest box max-distance; any <= d decides (Ideal.cpp:2557-2570)
             const uint64_t tot = (uint64_t)np_s * np_t;
             double mbd = 100000.0;
             bool hit = false;
             for (uint64_t k = lane; k < tot; k += 32) {
-                Box b1 = pixel_box(gs, (int)ss.p[k / np_t]);
-                Box b2 = pixel_box(gt, (int)ts.p[k % np_t]);
-                double md = box_max_distance(b1, b2, geo);
+                const uint32_t k1 = (uint32_t)(k / np_t), k2 = (uint32_t)(k % np_t);
+                double md = box_max_distance_f(ss.fbox[k1], ts.fbox[k2], ss.box[k1].lo1, geo);
                 if (md <= a.thr) {
                     hit = true;
                     break;
@@ -408,10 +453,11 @@ __global__ void __launch_bounds__(256) k_within_descend(const StoreView sv, With
                 Box b1, b2;
                 double lo = 0;
                 if (k < tot) {
-                    id1 = ss.p[k / np_t];
-                    id2 = ts.p[k % np_t];
-                    b1 = pixel_box(gs, (int)id1);
-                    b2 = pixel_box(gt, (int)id2);
+                    const uint32_t k1 = (uint32_t)(k / np_t), k2 = (uint32_t)(k % np_t);
+                    id1 = ss.p[k1];
+                    id2 = ts.p[k2];
+                    b1 = ss.box[k1];
+                    b2 = ts.box[k2];
                     lo = box_distance(b1, b2, geo);
                     keep = !(lo > a.thr) && lo < mbd;
                 }
@@ -864,8 +910,7 @@ static int within_round(farm_store *s, const uint32_t *dpairs, uint64_t n, uint8
                         farm_stats *acc, int &launches) {
     cudaStream_t st = s->stream;
     StoreView sv = s->view();
-    const uint64_t bw = (cap_pix >> 5) + 1;
-    const uint64_t words = 2 * (bw + 2ull * cap_pix);
+    const uint64_t words = within_scratch_words(cap_pix);
     DevBuf &scr = s->s[Q_SCR0], &cand = s->s[Q_SCR1], &tmp = s->s[Q_SCR2], &first = s->s[Q_SCR3];
     FARM_TRY(scr.ensure(4 * words * (uint64_t)nwarps + 64));
     FARM_CUDA(cudaMemsetAsync(scr.p, 0, 4 * words * (uint64_t)nwarps, st));
@@ -1032,7 +1077,7 @@ int within(farm_store *s, const uint32_t *pairs, uint64_t n, double distance, in
     int nwarps = sm_count() * 8 * 2;
     size_t freeb = 0, totb = 0;
     cudaMemGetInfo(&freeb, &totb);
-    const uint64_t words = 2 * (((cap >> 5) + 1) + 2ull * cap);
+    const uint64_t words = within_scratch_words(cap);
     while (nwarps > 64 && 4ull * words * (uint64_t)nwarps > freeb / 4) nwarps /= 2;
     uint64_t cand_cap = 1ull << 24;
     if (n) FARM_TRY(within_round(s, dpairs, n, dout, distance, geography, mode, tgt_base, cap, nwarps, cand_cap,
