@@ -940,7 +940,7 @@ __global__ void k_edge_cost(const StoreView sv, const PolyHdr *__restrict__ hdr,
             c = fabsf(B.x - A.x) / (float)h.step_x + (x_only ? 0.f : fabsf(B.y - A.y) / (float)h.step_y);
         }
         key[k] = (uint8_t)(c < 255.f ? c : 255.f);
-        idx[k] = (uint32_t)k;
+        if (idx) idx[k] = (uint32_t)k;
     }
 }
 
@@ -1748,7 +1748,7 @@ __global__ void k_cp_cost(const PolyHdr *__restrict__ hdr, const uint64_t *__res
             cost = fabsf(B.y - A.y) / (float)hdr[colpoly[c]].step_y;
         }
         key[j] = (uint8_t)(cost < 255.f ? cost : 255.f);
-        idx[j] = (uint32_t)j;
+        if (idx) idx[j] = (uint32_t)j;
     }
 }
 
@@ -2230,9 +2230,10 @@ static int edge_order(RasterCtx &R, uint32_t p0, uint32_t np, uint64_t e0, uint6
     FARM_TRY(s->s[S_PERM].ensure(8 * ne + 16));
     uint8_t *key = s->s[S_PERM_K].as<uint8_t>(), *key_s = key + ne;
     uint32_t *idx = s->s[S_PERM].as<uint32_t>(), *idx_s = idx + ne;
-    k_edge_cost<<<gb(ne), 256, 0, st>>>(s->view(), R.hdr, R.doff, p0, np, e0, ne, x_only, key, idx);
+    k_edge_cost<<<gb(ne), 256, 0, st>>>(s->view(), R.hdr, R.doff, p0, np, e0, ne, x_only, key, nullptr);
     R.launches++;
     (void)key_s;
+    (void)idx;
     FARM_TRY(local_order(R, key, ne, idx_s));
     *perm = idx_s;
     return FARM_OK;
@@ -2556,9 +2557,10 @@ static int raster_chunk(RasterCtx &R, const Chunk &ch) {
         FARM_TRY(s->s[S_PERM].ensure(8 * nCP + 16));
         uint8_t *key = s->s[S_PERM_K].as<uint8_t>(), *key_s = key + nCP;
         uint32_t *idx = s->s[S_PERM].as<uint32_t>(), *idx_s = idx + nCP;
-        k_cp_cost<<<gb(nCP), 256, 0, st>>>(R.hdr, cpstart, cpoly, cpcol, colpoly, nCP, key, idx);
+        k_cp_cost<<<gb(nCP), 256, 0, st>>>(R.hdr, cpstart, cpoly, cpcol, colpoly, nCP, key, nullptr);
         L++;
         (void)key_s;
+        (void)idx;
         FARM_TRY(local_order(R, key, nCP, idx_s));
         yperm = idx_s;
     }
