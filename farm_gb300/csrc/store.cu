@@ -28,11 +28,7 @@ int DevBuf::ensure(size_t bytes) {
     if (p) cudaFree(p);
     p = nullptr;
     cap = 0;
-    // a buffer that has to grow gets an eighth more than asked for (above
-    // 1 MiB), so that batches whose sizes creep up do not free and allocate
-    // again on every call (each cudaFree synchronises the device)
     size_t want = bytes < 256 ? 256 : bytes;
-    if (cap && want >= (1u << 20)) want += want / 8;
     cudaError_t e = cudaMalloc(&p, want);
     if (e != cudaSuccess) {
         cudaGetLastError();
