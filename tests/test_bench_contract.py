@@ -31,6 +31,10 @@ def test_roofline_block_has_the_contract_keys():
     assert abs(dom["achieved"] - (16 * 1e7 + 16 * 2e7) / 12e-3 / 1e12) < 1e-9
     json.dumps(rl)  # serialisable as it goes into the JSON line
     assert rl["stages"]["refine"]["unit"] == "TFLOP/s" and rl["stages"]["raster_hbm_view"]["unit"] == "GB/s"
+    # traffic: the ncu bytes per edge of the walk times the step's edges
+    assert abs(dom["traffic"] - bench.TRAFFIC_PER_UNIT["edge_walk"] * fake_totals()["vertices"] / 2) < 1e-3
+    # the per-edge traffic is above the walk's algorithmic bytes (ring, crossings, nodes), not below
+    assert bench.TRAFFIC_PER_UNIT["edge_walk"] > 61.0
 
 
 def test_filter_bytes_per_pair_and_pixel():
