@@ -28,6 +28,7 @@ reference or the generator's libm to reproduce them. Usage:
     python tests/golden/make_golden.py        # everything
     python tests/golden/make_golden.py wkt    # the WKT fixture only
     python tests/golden/make_golden.py contain  # the contain fixtures only
+    python tests/golden/make_golden.py sweep    # the -v 128 / 256 fixtures only
 """
 from __future__ import annotations
 
@@ -58,6 +59,17 @@ RASTER_CASES = [
     # the bench's -v 64 on polygons of 2k-20k vertices (below the 65,536-sequence assert)
     ("r_big_v64", StarParams(dom_hi=30.0, n_lo=2000, n_hi=20000), 105, 10, 64, 0),
 ]
+# configuration 2's -v sweep beyond 64 (128 and 256 vertices per pixel): its
+# generator's polygons up to the size below the 65,536-sequence assert
+SWEEP_RASTER_CASES = [
+    ("r_big_v128", StarParams(dom_hi=30.0, n_lo=2000, n_hi=22000), 107, 10, 128, 0),
+    ("r_big_v256", StarParams(dom_hi=30.0, n_lo=2000, n_hi=26000), 108, 10, 256, 0),
+]
+SWEEP_PAIR_CASES = [
+    ("p_intersect_v128", StarParams(dom_hi=12.0, n_lo=16, n_hi=22000), 207, 24, 90, 128, "intersect"),
+    ("p_intersect_v256", StarParams(dom_hi=12.0, n_lo=16, n_hi=26000), 208, 24, 90, 256, "intersect"),
+]
+
 # (name, params, seed, n_source, n_target (0 = self-join), vpr, mode)
 PAIR_CASES = [
     ("p_intersect_v10", StarParams(dom_hi=20.0), 201, 60, 240, 10, "intersect"),
@@ -199,6 +211,58 @@ def make_wkt() -> None:
     print("wrote the WKT fixture")
 
 
+def raster_fixture(harness: Path, tmp: Path, name, prm, seed, n, vpr, hier) -> dict:
+    ps = generate(prm, seed, n)
+    dt = HERE / f"{name}.dt"
+    ps.write_dt(str(dt))
+    out = tmp / f"{name}.rast.bin"
+    subprocess.run([str(harness), "raster", str(dt), str(vpr), str(hier), str(out)], check=True,
+                   stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL, env={"FARM_REF_THREADS": "4"})
+    gz(out, HERE / f"{name}.rast.bin.gz")
+    return {"name": name, "vpr": vpr, "hierarchy": hier, "seed": seed, "count": n, "params": prm.__dict__,
+            "dt_sha256": sha(dt)}
+
+
+def pair_fixture(harness: Path, tmp: Path, name, prm, seed, ns, nt, vpr, mode) -> dict:
+    S = generate(prm, seed, ns)
+    sdt = HERE / f"{name}_S.dt"
+    S.write_dt(str(sdt))
+    if nt:
+        T = generate(prm, seed + 5000, nt)
+        tdt = HERE / f"{name}_T.dt"
+        T.write_dt(str(tdt))
+        targ = str(tdt)
+    else:
+        targ = "-"
+    out = tmp / f"{name}.pairs.bin"
+    subprocess.run([str(harness), mode, str(sdt), targ, str(vpr), str(out)], check=True,
+                   stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL, env={"FARM_REF_THREADS": "4"})
+    gz(out, HERE / f"{name}.pairs.bin.gz")
+    return {"name": name, "mode": mode, "vpr": vpr, "seed": seed, "n_source": ns, "n_target": nt,
+            "self_join": nt == 0, "params": prm.__dict__}
+
+
+def make_sweep() -> None:
+    """The -v 128 and 256 cases alone, replacing their manifest entries."""
+    harness = build.build_ref()
+    if harness is None:
+        raise SystemExit("reference sources not found (set FARM_REF_SRC to the reference's src/)")
+    build.build_host()
+    tmp = Path("/tmp/farm_golden")
+    tmp.mkdir(exist_ok=True)
+    mf = HERE / "manifest.json"
+    manifest = json.loads(mf.read_text())
+    names = {c[0] for c in SWEEP_RASTER_CASES + SWEEP_PAIR_CASES}
+    manifest["raster"] = [c for c in manifest["raster"] if c["name"] not in names]
+    manifest["pairs"] = [c for c in manifest["pairs"] if c["name"] not in names]
+    for case in SWEEP_RASTER_CASES:
+        manifest["raster"].append(raster_fixture(harness, tmp, *case))
+    for case in SWEEP_PAIR_CASES:
+        manifest["pairs"].append(pair_fixture(harness, tmp, *case))
+    mf.write_text(json.dumps(manifest, indent=1))
+    print("wrote", len(SWEEP_RASTER_CASES), "raster and", len(SWEEP_PAIR_CASES), "pair fixtures of the -v sweep")
+
+
 def main() -> None:
     harness = build.build_ref()
     if harness is None:
@@ -207,33 +271,10 @@ def main() -> None:
     manifest = {"raster": [], "pairs": []}
     tmp = Path("/tmp/farm_golden")
     tmp.mkdir(exist_ok=True)
-    for name, prm, seed, n, vpr, hier in RASTER_CASES:
-        ps = generate(prm, seed, n)
-        dt = HERE / f"{name}.dt"
-        ps.write_dt(str(dt))
-        out = tmp / f"{name}.rast.bin"
-        subprocess.run([str(harness), "raster", str(dt), str(vpr), str(hier), str(out)], check=True,
-                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL, env={"FARM_REF_THREADS": "4"})
-        gz(out, HERE / f"{name}.rast.bin.gz")
-        manifest["raster"].append({"name": name, "vpr": vpr, "hierarchy": hier, "seed": seed, "count": n,
-                                   "params": prm.__dict__, "dt_sha256": sha(dt)})
-    for name, prm, seed, ns, nt, vpr, mode in PAIR_CASES:
-        S = generate(prm, seed, ns)
-        sdt = HERE / f"{name}_S.dt"
-        S.write_dt(str(sdt))
-        if nt:
-            T = generate(prm, seed + 5000, nt)
-            tdt = HERE / f"{name}_T.dt"
-            T.write_dt(str(tdt))
-            targ = str(tdt)
-        else:
-            targ = "-"
-        out = tmp / f"{name}.pairs.bin"
-        subprocess.run([str(harness), mode, str(sdt), targ, str(vpr), str(out)], check=True,
-                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL, env={"FARM_REF_THREADS": "4"})
-        gz(out, HERE / f"{name}.pairs.bin.gz")
-        manifest["pairs"].append({"name": name, "mode": mode, "vpr": vpr, "seed": seed, "n_source": ns,
-                                  "n_target": nt, "self_join": nt == 0, "params": prm.__dict__})
+    for case in RASTER_CASES + SWEEP_RASTER_CASES:
+        manifest["raster"].append(raster_fixture(harness, tmp, *case))
+    for case in PAIR_CASES + SWEEP_PAIR_CASES:
+        manifest["pairs"].append(pair_fixture(harness, tmp, *case))
     # the reference's longitude table, as printed in util.h
     util = (REF_SRC / "include" / "util.h").read_text()
     m = re.search(r"degree_per_kilometer_longitude_arr\[\] = \{([^}]*)\}", util)
@@ -241,7 +282,8 @@ def main() -> None:
     manifest["degree_table"] = {"count": len(vals), "sha256_of_6_decimal_text": hashlib.sha256(
         ",".join(vals).encode()).hexdigest()}
     (HERE / "manifest.json").write_text(json.dumps(manifest, indent=1))
-    print("wrote", len(RASTER_CASES), "raster and", len(PAIR_CASES), "pair fixtures")
+    print("wrote", len(RASTER_CASES) + len(SWEEP_RASTER_CASES), "raster and",
+          len(PAIR_CASES) + len(SWEEP_PAIR_CASES), "pair fixtures")
     make_wkt()
     make_contain()
 
@@ -251,5 +293,7 @@ if __name__ == "__main__":
         make_wkt()
     elif sys.argv[1:] == ["contain"]:
         make_contain()
+    elif sys.argv[1:] == ["sweep"]:
+        make_sweep()
     else:
         main()
