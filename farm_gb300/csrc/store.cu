@@ -335,15 +335,23 @@ int farm_store_load(farm_store *s, int side, uint64_t n, const uint64_t *off, co
     FARM_TRY(stage_side(s, side, std::move(h), &ring_first));
     const float2 *src;
     if (mem == FARM_MEM_DEVICE) {
+        // the padding kernel reads whole (x, y) pairs: 8-byte loads
+        if (reinterpret_cast<uintptr_t>(xy + 2 * o0) & 7u) {
+            set_error("farm_store_load: device vertices must start on an 8-byte boundary");
+            return FARM_EINVAL;
+        }
         src = reinterpret_cast<const float2 *>(xy) + o0;
     } else {
         // Pinned host memory is read by the padding kernel itself over the
         // host link (the device address the runtime reports for it), with no
         // staging copy; pageable memory is copied into a staging buffer first.
+        // (only at an 8-byte boundary, as the kernel's loads are of whole pairs)
         cudaPointerAttributes pa;
         const void *mapped = nullptr;
         if (cudaPointerGetAttributes(&pa, xy + 2 * o0) == cudaSuccess) {
-            if (pa.type == cudaMemoryTypeHost && pa.devicePointer) mapped = pa.devicePointer;
+            if (pa.type == cudaMemoryTypeHost && pa.devicePointer &&
+                (reinterpret_cast<uintptr_t>(pa.devicePointer) & 7u) == 0)
+                mapped = pa.devicePointer;
         } else {
             cudaGetLastError();
         }

@@ -94,9 +94,12 @@ void farm_store_destroy(farm_store *s);
  * layout of farm_host.h: off[n+1] (vertex offsets), xy float32 pairs with the
  * closing copy included, exactly as a .dt record stores them. mem says where
  * off/xy live (FARM_MEM_HOST or FARM_MEM_DEVICE). Replaces both sides' data.
- * Host vertices in pinned (page-locked) memory are read by the device over the
- * host link with no staging copy; pageable ones are staged through a device
- * buffer. Either way the call returns once the rings are in place.
+ * xy holds the off[n] - off[0] vertices that the offsets describe. Host
+ * vertices in pinned (page-locked) memory at an 8-byte boundary are read by
+ * the device over the host link with no staging copy; others are staged
+ * through a device buffer. Device vertices must start on an 8-byte boundary
+ * (FARM_EINVAL otherwise). Either way the call returns once the rings are in
+ * place.
  * For a self-join load side 0 only and pass target_is_source to the queries. */
 int farm_store_load(farm_store *s, int side, uint64_t n, const uint64_t *off, const float *xy, int mem);
 

@@ -45,3 +45,31 @@ def test_store_load_pinned_pageable_and_device_agree(gpu_lib):
             for key in ("status", "offset", "seq", "vnodes", "hnodes", "areas"):
                 assert np.array_equal(ra[key], rb[key]), key
         assert np.array_equal(base[1], out) and base[2] == found
+
+
+def test_store_load_alignment(gpu_lib):
+    """Vertices at a 4-byte (not 8-byte) boundary: pinned host ones go
+    through the staging copy and load the same rings; device ones are
+    refused before any device work."""
+    import torch
+    prm = P.StarParams(dom_hi=10.0, n_lo=16, n_hi=2000)
+    S = P.generate(prm, 83, 40)
+    buf = torch.zeros(S.xy.size + 1, dtype=torch.float32).pin_memory()
+    buf[1:] = torch.from_numpy(S.xy.reshape(-1))
+    odd = buf[1:].numpy().reshape(-1, 2)  # starts 4 bytes into the allocation
+    assert odd.ctypes.data % 8 == 4
+    with Store() as a, Store() as b:
+        a.load(0, S.off, odd)
+        b.load(0, S.off, S.xy)
+        a.rasterize(vpr=10, strict=False)
+        b.rasterize(vpr=10, strict=False)
+        for k in (0, S.n - 1):
+            ra, rb = a.fetch_raster(0, k), b.fetch_raster(0, k)
+            for key in ("status", "offset", "seq", "vnodes", "areas"):
+                assert np.array_equal(ra[key], rb[key]), key
+    dev = torch.device("cuda:0")
+    d = torch.zeros(S.xy.size + 1, dtype=torch.float32, device=dev)
+    d[1:] = torch.from_numpy(S.xy.reshape(-1)).to(dev)
+    with Store() as c:
+        with pytest.raises(Exception, match="8-byte"):
+            c.load(0, torch.from_numpy(S.off.view(np.int64)).to(dev), d[1:].view(-1, 2))
