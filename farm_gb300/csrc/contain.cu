@@ -348,6 +348,11 @@ extern "C" int farm_contain_points(farm_store *s, int side, const float *xy, uin
     }
     FARM_TRY(check_pair_limits(s, pairs, n, mem, s->n_side[side], npoints, "farm_contain_points", "polygons",
                                "points"));
+    if (mem == FARM_MEM_DEVICE && n && (reinterpret_cast<uintptr_t>(xy) & 7u)) {
+        // the kernel reads whole (x, y) pairs: 8-byte loads
+        set_error("farm_contain_points: device points must start on an 8-byte boundary");
+        return FARM_EINVAL;
+    }
     cudaStream_t stream = s->stream;
     const uint32_t *dpairs = pairs;
     const float2 *dpts = reinterpret_cast<const float2 *>(xy);

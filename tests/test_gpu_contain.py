@@ -120,3 +120,21 @@ def test_gpu_contain_rejects_out_of_range(gpu_lib):
             st.contain_points(pts, np.array([[T.n, 0]], np.uint32), side=1)
         out, _ = st.contain_points(pts, np.array([[T.n - 1, 4]], np.uint32), side=1)
         assert out.tolist() in ([0], [1])
+
+
+def test_gpu_contain_points_refuses_misaligned_device_points(gpu_lib):
+    import torch
+    from farm_gb300._native import FarmError
+    prm = P.StarParams(dom_hi=10.0, n_hi=200)
+    S = P.generate(prm, 63, 10)
+    dev = torch.device("cuda:0")
+    buf = torch.zeros(11, dtype=torch.float32, device=dev)
+    pts = buf[1:].view(5, 2)  # 4 bytes into the allocation
+    pairs = torch.tensor([[0, 0], [1, 4]], dtype=torch.int32, device=dev)
+    with Store() as st:
+        st.load(0, S.off, S.xy)
+        st.rasterize(vpr=10)
+        with pytest.raises(FarmError, match="8-byte"):
+            st.contain_points(pts, pairs)
+        out, _ = st.contain_points(buf[:10].view(5, 2), pairs)  # aligned: answers
+        assert out.shape[0] == 2
