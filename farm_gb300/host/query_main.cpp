@@ -11,10 +11,12 @@
 // registers); -r and -g are accepted for compatibility, since this engine
 // always rasterizes and always runs the query on the GPU. The pipeline
 // follows the reference's mains (intersect.cpp:41-91, within_polygon.cpp:
-// 51-107, intersection.cpp:55-94): load the .dt files, candidate pairs from
-// MBR overlap (the reference's R-tree search returns the same set; the
-// within join widens each query MBR by the distance and skips a polygon
-// against itself), rasterize, query in batches of -b pairs (0 = all), and
+// 51-107, intersection.cpp:55-94): load the .dt files (streamed into the
+// device store by all -n host threads, farm_store_load_dt), candidate pairs
+// from MBR overlap on the GPU (farm_mbr_join_gpu: the set and order the
+// reference's R-tree search returns; the within join widens each query MBR
+// by the distance and skips a polygon against itself), rasterize, query in
+// batches of -b pairs (0 = all), and
 // print "count-found" as query_context::print_stats does
 // (query_context.cpp:172-173). intersection, whose reference stops before
 // computing areas, prints the number of overlapping pairs and their total
@@ -30,7 +32,6 @@
 #include <vector>
 
 #include "farm_gpu.h"
-#include "farm_host.h"
 
 namespace {
 
@@ -163,37 +164,6 @@ Args parse(int argc, char **argv) {
     return a;
 }
 
-struct Set {
-    uint64_t n = 0, total = 0;
-    std::vector<uint64_t> off;
-    std::vector<float> xy;
-    std::vector<double> mbr;
-};
-
-Set load(const std::string &path, int threads) {
-    Set s;
-    if (farm_dt_read(path.c_str(), &s.n, &s.total, nullptr, nullptr)) die("cannot read", farm_host_last_error());
-    s.off.resize(s.n + 1);
-    s.xy.resize(2 * s.total + 2);
-    if (farm_dt_read(path.c_str(), &s.n, &s.total, s.off.data(), s.xy.data()))
-        die("cannot read", farm_host_last_error());
-    s.mbr.resize(4 * s.n + 4);
-    if (farm_mbr(s.n, s.off.data(), s.xy.data(), s.mbr.data(), threads)) die("mbr", farm_host_last_error());
-    return s;
-}
-
-std::vector<uint32_t> join(const Set &S, const Set &T, double expand, int geography, int skip_same, int threads) {
-    uint64_t np = 0;
-    if (farm_mbr_join(S.n, S.mbr.data(), T.n, T.mbr.data(), expand, geography, skip_same, &np, nullptr, threads))
-        die("mbr join", farm_host_last_error());
-    std::vector<uint32_t> pairs(2 * np + 2);
-    if (np && farm_mbr_join(S.n, S.mbr.data(), T.n, T.mbr.data(), expand, geography, skip_same, &np, pairs.data(),
-                            threads))
-        die("mbr join", farm_host_last_error());
-    pairs.resize(2 * np);
-    return pairs;
-}
-
 void check(int rc, const char *what) {
     if (rc != FARM_OK) die(what, farm_last_error());
 }
@@ -210,27 +180,32 @@ int main(int argc, char **argv) {
     if (a.kind != K_WITHIN && a.target.empty()) die("missing", "-t target.dt");
     if (a.kind == K_WITHIN) a.hierarchy = true;  // the within filter walks the hierarchy's layers
 
-    Set S = load(a.source, a.threads);
-    // within_polygon joins the source set with itself (within_polygon.cpp:9-48)
-    Set T = a.kind == K_WITHIN ? Set() : load(a.target, a.threads);
     double t0 = now_ms();
-    std::vector<uint32_t> pairs = a.kind == K_WITHIN ? join(S, S, (double)a.within_distance, 1, 1, a.threads)
-                                                     : join(S, T, 0.0, 0, 0, a.threads);
-    const uint64_t np = pairs.size() / 2;
+    farm_store *st = nullptr;
+    check(farm_store_create(&st), "farm_store_create");
+    check(farm_store_load_dt(st, 0, a.source.c_str(), a.threads, nullptr), "farm_store_load_dt(source)");
+    // within_polygon joins the source set with itself (within_polygon.cpp:9-48)
+    const int self = a.kind == K_WITHIN ? 1 : 0;
+    if (!self) check(farm_store_load_dt(st, 1, a.target.c_str(), a.threads, nullptr), "farm_store_load_dt(target)");
+    say_t("loading data finished", t0);
+
+    t0 = now_ms();
+    const double expand = self ? (double)a.within_distance : 0.0;
+    uint64_t np = 0;
+    int rc = farm_mbr_join_gpu(st, expand, self, self, nullptr, 0, FARM_MEM_HOST, &np);  // count
+    if (rc != FARM_OK && rc != FARM_EOVERFLOW) check(rc, "farm_mbr_join_gpu");
+    std::vector<uint32_t> pairs(2 * np + 2);
+    if (np) check(farm_mbr_join_gpu(st, expand, self, self, pairs.data(), np, FARM_MEM_HOST, &np), "farm_mbr_join_gpu");
+    pairs.resize(2 * np);
     say_t("rtree filtering finished", t0);
 
     t0 = now_ms();
-    farm_store *st = nullptr;
-    check(farm_store_create(&st), "farm_store_create");
-    check(farm_store_load(st, 0, S.n, S.off.data(), S.xy.data(), FARM_MEM_HOST), "farm_store_load(source)");
-    if (a.kind != K_WITHIN)
-        check(farm_store_load(st, 1, T.n, T.off.data(), T.xy.data(), FARM_MEM_HOST), "farm_store_load(target)");
     farm_raster_opts ro;
     memset(&ro, 0, sizeof ro);
     ro.vpr = a.vpr;
     ro.category_count = a.category_count;
     ro.hierarchy = a.hierarchy ? 1 : 0;
-    int rc = farm_rasterize(st, &ro);
+    rc = farm_rasterize(st, &ro);
     if (rc == FARM_EASSERT)
         say("some polygons fail the reference's raster assertions; their pairs are reported as 2 and not counted");
     else
